@@ -1,0 +1,345 @@
+#!/usr/bin/env python
+"""Band-structure throughput on GB300: k-points/s for silicon with the Cohen-Bergstresser local form
+factors (V3, V8, V11 = -0.21, 0.04, 0.08 Ry, a = 5.43 A), plane-wave basis of 137 vectors (10 shells),
+the lowest 16 bands at the 2000 k-points of the path L-G-X-W-K-U-L-W-X-K-G.
+
+One step = one solve of the whole 2000-point batch. Reported:
+  value        mixed-precision path (FP32 reduction + FP64 Rayleigh-Ritz), inputs resident in HBM,
+               whose max eigenvalue error against the plain FP64 path is checked in the same run
+               (<= 1e-6 eV, reported as mixed_max_err_ev)
+  fp64         the plain FP64 drop-in path on the same batch
+  e2e          the same metric through the C ABI uepm_solve with pinned host buffers (k in, E out)
+  roofline     the dominant kernel of the headline path, timed with CUDA events on its stream
+  cpu_baseline the oracle (CPU restatement of the reference path) on this host's cores
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "k-points/s, Si nb=16 basis 137 (FP64 vs mixed @1e-6 eV); serve p50/p99 ms"
+WORKLOAD = "Si Cohen-Bergstresser local EPM, basis 137 (10 shells), 16 bands, 2000 k on LGXWKULWXKG"
+NB = 16
+SHELLS = 10
+NPOINTS = 2000
+PATH = "LGXWKULWXKG"
+PARAM_FILE = os.path.join(ROOT, "params", "si-cohen-bergstresser.yaml")
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def emit(d):
+    print(json.dumps(d), flush=True)
+
+
+# ------------------------------------------------------------------------------------------------
+def workload_inputs():
+    from ultimateepm_gb300 import Materials, SymmetryPoints, generate_basis_vectors
+
+    mats = Materials()
+    mats.load_material_parameters(PARAM_FILE)
+    si = mats.materials["Si"]
+    G = generate_basis_vectors(SHELLS)
+    k, _ = SymmetryPoints().GeneratePoints(list(PATH), NPOINTS)
+    return si, G, k
+
+
+def cpu_time_oracle(nthreads: int, budget_s: float):
+    """Times the oracle on the workload; whole 2000-point passes until budget_s elapsed."""
+    from oracle import oracle as O
+
+    O.build()
+    mat = O.load_materials(PARAM_FILE)["Si"]
+    G = O.generate_basis(SHELLS)
+    k, _ = O.generate_path(PATH, NPOINTS)
+    O.band_structure(mat, G, k[:64], NB, nthreads=nthreads)  # warm-up (thread pool, caches)
+    done, t0 = 0, time.perf_counter()
+    while True:
+        O.band_structure(mat, G, k, NB, nthreads=nthreads)
+        done += len(k)
+        if time.perf_counter() - t0 >= budget_s:
+            break
+    dt = time.perf_counter() - t0
+    return done / dt, done, dt
+
+
+class Clocks:
+    """nvidia-smi clock / throttle sampling during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.idx = gpu_index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.idx), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if not self.proc:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        rows = []
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 9:
+                rows.append(parts)
+        os.unlink(self.path)
+        if not rows:
+            return None
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        smax = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower().startswith("active")})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+# ------------------------------------------------------------------------------------------------
+def run_ours(args):
+    import torch
+
+    ws, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    if ws > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    from ultimateepm_gb300 import _native as N
+    from ultimateepm_gb300 import api
+
+    L = N.load()
+    si, G, k = workload_inputs()
+    nk = len(k)
+    stream = torch.cuda.current_stream()
+    sp = C.c_void_p(stream.cuda_stream)
+    dk = torch.from_numpy(k).cuda()
+    dE = torch.zeros((nk, NB), dtype=torch.float64, device="cuda")
+    dst = torch.zeros(nk, dtype=torch.int32, device="cuda")
+    flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device="cuda")  # > 129 MB L2
+
+    def barrier():
+        torch.cuda.synchronize()
+        if ws > 1:
+            import torch.distributed as dist
+
+            dist.barrier()
+
+    def timed(prec):
+        ctx = api._Context(si, G, False, False, prec)
+        call = lambda: N.check(L.uepm_solve_device(ctx.h, C.c_void_p(dk.data_ptr()), nk, NB, N.UEPM_WANT_VALUES,
+                                                    C.c_void_p(dE.data_ptr()), None, None,
+                                                    C.c_void_p(dst.data_ptr()), sp))
+        for _ in range(args.warmup):
+            call()
+        barrier()
+        N.check(L.uepm_ctx_set_profiling(ctx.h, 1))
+        launches0 = L.uepm_kernel_launches()
+        times = []
+        for _ in range(args.steps):
+            flush.zero_()
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            call()
+            b.record(stream)
+            b.synchronize()
+            times.append(a.elapsed_time(b))
+        barrier()
+        launches = L.uepm_kernel_launches() - launches0
+        ms = (C.c_double * N.KERNEL_KINDS)()
+        cnt = (C.c_uint64 * N.KERNEL_KINDS)()
+        N.check(L.uepm_ctx_read_profile(ctx.h, ms, cnt, N.KERNEL_KINDS))
+        prof = {L.uepm_kernel_name(q).decode(): (ms[q], int(cnt[q])) for q in range(N.KERNEL_KINDS) if cnt[q]}
+        assert not dst.any().item(), "a k-point reported a non-zero status"
+        E = dE.cpu().numpy().copy()
+        ctx.close()
+        return times, prof, launches, E
+
+    clocks = Clocks(local)
+    clocks.start()
+    t_mixed, prof_mixed, launches_mixed, E_mixed = timed(N.UEPM_PREC_MIXED)
+    t_fp64, prof_fp64, launches_fp64, E_fp64 = timed(N.UEPM_PREC_FP64)
+    clk = clocks.stop()
+
+    def max_over_ranks(x):
+        if ws == 1:
+            return x
+        import torch.distributed as dist
+
+        t = torch.tensor([x], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+
+    ms_mixed = max_over_ranks(sum(t_mixed) / len(t_mixed))
+    ms_fp64 = max_over_ranks(sum(t_fp64) / len(t_fp64))
+    err = float(np.abs(E_mixed - E_fp64).max())
+
+    # end to end through the public C ABI with pinned host buffers: k in, E and status out
+    ctx = api._Context(si, G, False, False, N.UEPM_PREC_MIXED)
+    hk = torch.from_numpy(k).pin_memory()
+    hE = torch.zeros((nk, NB), dtype=torch.float64).pin_memory()
+    hs = torch.zeros(nk, dtype=torch.int32).pin_memory()
+    dpp = lambda t: C.cast(C.c_void_p(t.data_ptr()), C.POINTER(C.c_double))
+    e2e_call = lambda: N.check(L.uepm_solve(ctx.h, dpp(hk), nk, NB, N.UEPM_WANT_VALUES, dpp(hE), None, None,
+                                            C.cast(C.c_void_p(hs.data_ptr()), C.POINTER(C.c_int32))))
+    for _ in range(args.warmup):
+        e2e_call()
+    barrier()
+    e2e_times = []
+    for _ in range(args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        e2e_call()
+        e2e_times.append(time.perf_counter() - t0)
+    barrier()
+    e2e_s = max_over_ranks(sum(e2e_times) / len(e2e_times))
+    ctx.close()
+
+    if rank != 0:
+        return
+    # roofline of the dominant kernel of the headline (mixed) path
+    n, m = len(G), min(len(G), NB + 4)
+    flops_per_k = {
+        # FP64: Y = H X (n^2 m complex MACs), S and A (2 n m(m+1)/2), 8 real flops per complex MAC
+        "refine": 8.0 * n * n * m + 8.0 * n * m * (m + 1),
+        # FP32 Householder reduction: 16/3 n^3
+        "tridiag_fp32": 16.0 / 3.0 * n ** 3,
+        "tridiag_fp64": 16.0 / 3.0 * n ** 3,
+    }
+    dom = max(prof_mixed, key=lambda q: prof_mixed[q][0])
+    dom_ms = prof_mixed[dom][0] / max(prof_mixed[dom][1], 1)
+    peak64 = C.c_double()
+    peak32 = C.c_double()
+    N.check(L.uepm_measure_peak(N.UEPM_PREC_FP64, C.byref(peak64)))
+    N.check(L.uepm_measure_peak(N.UEPM_PREC_MIXED, C.byref(peak32)))
+    pipe = "fp32" if dom == "tridiag_fp32" else "fp64"
+    peak = peak32.value if pipe == "fp32" else peak64.value
+    achieved = flops_per_k.get(dom, 0.0) * nk / (dom_ms * 1e-3) / 1e12
+    fp64_dom = "tridiag_fp64"
+    fp64_ms = prof_fp64[fp64_dom][0] / max(prof_fp64[fp64_dom][1], 1)
+    fp64_ach = flops_per_k[fp64_dom] * nk / (fp64_ms * 1e-3) / 1e12
+
+    cores = os.cpu_count() or 1
+    cpu_v, cpu_done, cpu_dt = cpu_time_oracle(cores, args.cpu_budget)
+    value = nk * ws / (ms_mixed * 1e-3)
+    out = {
+        "metric": METRIC,
+        "value": value,
+        "unit": "k-points/s",
+        "n_gpus": ws,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": ms_mixed,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "fp32+fp64",
+        "data": "synthetic (deterministic k-path; no dataset)",
+        "config": {"workload": WORKLOAD, "k_points_per_gpu": nk, "bands": NB, "basis": n,
+                   "precision": "mixed: FP32 reduction + FP64 Rayleigh-Ritz", "l2": "flushed (256 MB write) "
+                   "between timed steps", "parallelism": f"replicas x{ws}"},
+        "mixed_max_err_ev": err,
+        "fp64": {"value": nk * ws / (ms_fp64 * 1e-3), "ms_per_step": ms_fp64, "dtype": "f64",
+                 "roofline": {"bound": "fp64_pipe", "kernel": fp64_dom, "achieved": fp64_ach,
+                              "peak": peak64.value, "unit": "TFLOP/s", "frac": fp64_ach / peak64.value,
+                              "peak_source": "measured in-run (pure-FMA kernel, uepm_measure_peak)"},
+                 "kernels_ms": {q: v[0] / max(v[1], 1) for q, v in prof_fp64.items()},
+                 "gpu_launches": launches_fp64},
+        "mixed_speedup_vs_fp64": ms_fp64 / ms_mixed,
+        "e2e": {"value": nk * ws / e2e_s, "unit": "k-points/s", "h2d_bytes_per_step": int(hk.numel() * 8),
+                "d2h_bytes_per_step": int(hE.numel() * 8 + hs.numel() * 4), "entry_point": "uepm_solve"},
+        "roofline": {"bound": f"{pipe}_pipe", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                     "frac": achieved / peak, "traffic": None,
+                     "peak_source": "measured in-run (pure-FMA kernel, uepm_measure_peak)"},
+        "kernels_ms": {q: v[0] / max(v[1], 1) for q, v in prof_mixed.items()},
+        "gpu_launches": launches_mixed,
+        "cpu_baseline": {"value": cpu_v, "unit": "k-points/s", "cores": cores, "kind": "port",
+                         "sample": f"{cpu_done} k-points ({cpu_done // nk} passes over the 2000-point path), "
+                                   f"{cpu_dt:.1f} s, FP64 eigenvalues only"},
+        "clocks": clk,
+    }
+    emit(out)
+
+
+def run_reference(args):
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return
+    from oracle import oracle as O
+
+    O.build()
+    mat = O.load_materials(PARAM_FILE)["Si"]
+    G = O.generate_basis(SHELLS)
+    k, _ = O.generate_path(PATH, NPOINTS)
+    cores = os.cpu_count() or 1
+    for _ in range(args.warmup):
+        O.band_structure(mat, G, k[:256], NB, nthreads=cores)
+    times = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        O.band_structure(mat, G, k, NB, nthreads=cores)
+        times.append(time.perf_counter() - t0)
+    s = sum(times) / len(times)
+    v = len(k) / s
+    emit({
+        "impl": "reference", "metric": METRIC, "value": v, "unit": "k-points/s", "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": s * 1e3, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (deterministic k-path; no dataset)",
+        "config": {"workload": WORKLOAD, "k_points_per_gpu": len(k), "bands": NB, "basis": len(G)},
+        "cpu_baseline": {"value": v, "unit": "k-points/s", "cores": cores, "kind": "port",
+                         "sample": f"{len(k)} k-points per step (the whole path), FP64 eigenvalues only"},
+        "e2e": {"value": v, "unit": "k-points/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    })
+
+
+def main():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=10)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    p.add_argument("--cpu-budget", type=float, default=10.0, help="seconds of oracle timing for cpu_baseline")
+    args = p.parse_args()
+    args.warmup = max(args.warmup, 3)
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

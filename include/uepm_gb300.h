@@ -1,0 +1,161 @@
+/*
+ * uepm_gb300.h -- C ABI of the GB300 (sm_103a) band-structure engine.
+ *
+ * This is the drop-in boundary for UltimateEPM's per-k-point hot path: H(k) assembly plus the
+ * Hermitian eigensolve, batched over k-points on one GPU. Every entry point takes plain pointers and
+ * sizes and returns an int status; the C++ adapter (include/uepm/*.h) rethrows the same exception
+ * types the reference throws. Energies are in eV, k in reduced units of 2*pi/a, gradients in eV*m,
+ * exactly as in the reference's src/EPP.
+ *
+ * Reference interfaces replaced (paths relative to the reference project root):
+ *   uepm_generate_basis        BandStructure::GenerateBasisVectors     src/EPP/BandStructure.cpp:26-57
+ *   uepm_generate_path         SymmetryPoints::GeneratePoints          src/EPP/SymmetryPoints.cpp:47-147
+ *   uepm_materials_load        Materials::load_material_parameters     src/EPP/Material.cpp:33-71
+ *   uepm_ctx_create            Hamiltonian::Hamiltonian + SetConstantNonDiagonalMatrix
+ *                                                                       src/EPP/Hamiltonian.cpp:18-48
+ *   uepm_solve / _device       BandStructure::Compute_parallel, i.e. per k: Hamiltonian::SetMatrix
+ *                              + Diagonalize + compute_gradient_at_level
+ *                                                                       src/EPP/BandStructure.cpp:151-201,
+ *                                                                       src/EPP/Hamiltonian.cpp:50-194
+ *   uepm_assemble_device       Hamiltonian::SetMatrix + the hermitisation in Diagonalize
+ *                                                                       src/EPP/Hamiltonian.cpp:50-127
+ *   uepm_adjust_values         BandStructure::AdjustValues / FindBandGap
+ *                                                                       src/EPP/BandStructure.cpp:203-262
+ */
+#ifndef UEPM_GB300_H
+#define UEPM_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Return codes. The C++ adapter maps them onto the reference's exception types. */
+#define UEPM_OK 0
+#define UEPM_ERR_INVALID (-1)      /* std::invalid_argument (bad path label, x < 0, ...)       */
+#define UEPM_ERR_RUNTIME (-2)      /* std::runtime_error (bad basis, unsupported SOC period)  */
+#define UEPM_ERR_OUT_OF_RANGE (-3) /* std::out_of_range (band index)                          */
+#define UEPM_ERR_CUDA (-4)         /* a CUDA call failed; uepm_last_error() has the text      */
+#define UEPM_ERR_NOMEM (-5)        /* device allocation failed                               */
+#define UEPM_ERR_NOT_CONVERGED (-6)/* at least one k-point reported a non-zero status        */
+
+/* Per-k-point status values written by the solve. */
+#define UEPM_K_OK 0
+#define UEPM_K_NOCONVERGE 1 /* an iteration cap was reached                                   */
+#define UEPM_K_NONFINITE 2  /* NaN/Inf appeared in H(k) or in the reduction                  */
+
+/* Context flags (Hamiltonian::SetMatrix's add_non_local_correction / enable_soc). */
+#define UEPM_NONLOCAL 1u
+#define UEPM_SOC 2u
+
+/* What a solve computes. Values are always produced. */
+#define UEPM_WANT_VALUES 1u
+#define UEPM_WANT_VECTORS 2u  /* X: the nb lowest eigenvectors                              */
+#define UEPM_WANT_GRADIENT 4u /* Hellmann-Feynman kinetic gradient, as compute_gradient_at_level */
+
+/* Arithmetic of the solve. */
+#define UEPM_PREC_FP64 0  /* plain FP64 path: the drop-in                                   */
+#define UEPM_PREC_MIXED 1 /* FP32 reduction + FP64 residual and Rayleigh-Ritz refinement    */
+
+/*
+ * Material parameters in the units the reference holds after loading a YAML file
+ * (src/EPP/Material.cpp:33-71, NonLocalParameters.hpp:91-116, SpinOrbitParameters.hpp:74-81):
+ * lattice constant in Angstrom; V* in eV; alpha_0 and A2 in eV; beta_0 raw; radii in metres;
+ * spin-orbit periods, radial extents (bohr units), alpha and mu raw. nl_well: 0 unknown,
+ * 1 square, 2 gaussian.
+ */
+typedef struct uepm_material {
+    double lattice_constant;
+    double V3S, V4S, V8S, V11S, V3A, V4A, V8A, V11A;
+    int32_t nl_well;
+    int32_t has_nonlocal;
+    double alpha0_cation, beta0_cation, A2_cation, alpha0_anion, beta0_anion, A2_anion;
+    double R0_cation, R2_cation, R0_anion, R2_anion;
+    uint32_t period_anion, period_cation;
+    int32_t has_soc;
+    int32_t _pad;
+    double radial_extent_anion, radial_extent_cation, alpha_soc, mu_soc;
+} uepm_material;
+
+typedef struct uepm_ctx uepm_ctx;
+
+/* Library identity and the last error message of the calling thread. */
+int uepm_version(void);
+const char* uepm_last_error(void);
+int uepm_material_size(void);
+
+/* BandStructure::GenerateBasisVectors: writes up to `capacity` int32 triples (x,y,z) in the
+ * reference's i->j->k loop order and returns the basis size N, or UEPM_ERR_RUNTIME when `shells`
+ * is outside [2, table size]. Pass capacity 0 to query N. Host-only. */
+int uepm_generate_basis(unsigned shells, int32_t* G, int capacity);
+
+/* SymmetryPoints::GeneratePoints for single-letter labels from {L,G,X,W,K,U} (e.g. "LGXWKULWXKG"):
+ * writes up to `capacity` k triples and strlen(labels) node positions, returns the point count or
+ * UEPM_ERR_INVALID where the reference throws std::invalid_argument. Host-only. */
+int uepm_generate_path(const char* labels, unsigned n_points, double* k, int capacity, uint32_t* sym_pos);
+
+/* Materials::load_material_parameters: parses the reference's YAML layout. Writes up to
+ * `capacity` materials and their symbols (each `symbol_stride` bytes, NUL-terminated) in file
+ * order; returns the number of materials in the file or a negative code. Host-only. */
+int uepm_materials_load(const char* path, uepm_material* out, char* symbols, int symbol_stride, int capacity);
+
+/* Hamiltonian ctor: uploads the material and the basis G (N int32 triples) to the current CUDA
+ * device and precomputes the k-independent local form-factor matrix. flags: UEPM_NONLOCAL,
+ * UEPM_SOC. Fails with UEPM_ERR_RUNTIME for SOC on a material whose atomic periods are not 2-4
+ * (the reference throws from SpinOrbitCorrection::compute_lambda_1/2). */
+int uepm_ctx_create(const uepm_material* mat, const int32_t* G, int N, uint32_t flags, uepm_ctx** out);
+int uepm_ctx_destroy(uepm_ctx* ctx);
+int uepm_ctx_set_precision(uepm_ctx* ctx, int precision);
+/* Matrix order n: N, or 2N with SOC. */
+int uepm_ctx_order(const uepm_ctx* ctx);
+/* Upper bound, in bytes, of device workspace a solve may hold (default 8 GiB). */
+int uepm_ctx_set_workspace_limit(uepm_ctx* ctx, size_t bytes);
+
+/*
+ * Batched solve over nk k-points (reduced units, nk x 3 row-major), keeping the nb lowest bands:
+ *   E      nk x nb, ascending per k                                   (required)
+ *   X      nk x nb x n complex128 (re, im interleaved), eigenvector b of k in X[k][b][:]
+ *                                                       (UEPM_WANT_VECTORS, else may be NULL)
+ *   grad   nk x nb x 3, eV*m                             (UEPM_WANT_GRADIENT, else may be NULL)
+ *   status nk int32 per-k status                         (may be NULL)
+ * nb must be in [1, n]. uepm_solve takes HOST buffers and copies in and out; uepm_solve_device
+ * takes DEVICE buffers and enqueues on `stream` (a cudaStream_t, NULL = legacy default stream)
+ * without synchronising.
+ */
+int uepm_solve(uepm_ctx* ctx, const double* k, size_t nk, int nb, uint32_t want, double* E, double* X, double* grad,
+               int32_t* status);
+int uepm_solve_device(uepm_ctx* ctx, const double* d_k, size_t nk, int nb, uint32_t want, double* d_E, double* d_X,
+                      double* d_grad, int32_t* d_status, void* stream);
+
+/* H(k) after SetMatrix and Diagonalize's hermitisation, for nk k-points: d_H is nk x n x n
+ * complex128, column-major per k, both triangles filled. Device buffers, enqueued on `stream`. */
+int uepm_assemble_device(uepm_ctx* ctx, const double* d_k, size_t nk, double* d_H, void* stream);
+
+/* BandStructure::AdjustValues (FindBandGap + shift) on host E (nk x nb). Returns the gap via *gap
+ * and whether FindBandGap succeeded via *found. soc selects 8 instead of 4 valence bands. */
+int uepm_adjust_values(double* E, size_t nk, int nb, int soc, int min_cond_zero, double* gap, int* found);
+
+/* Launch counters (kernels enqueued by this library since load), for launch accounting. */
+uint64_t uepm_kernel_launches(void);
+
+/* Per-kernel device timing for profiling (no reference counterpart; the reference only has
+ * whole-second wall timers, BandStructure.cpp:126-148). When on, every kernel a solve enqueues is
+ * bracketed by CUDA events on the launching stream. uepm_ctx_read_profile waits for the recorded
+ * events and returns, per kernel kind, the accumulated milliseconds and launch counts since
+ * profiling was switched on. Kinds: see uepm_kernel_name (0..UEPM_KERNEL_KINDS-1). */
+#define UEPM_KERNEL_KINDS 8
+int uepm_ctx_set_profiling(uepm_ctx* ctx, int on);
+int uepm_ctx_read_profile(uepm_ctx* ctx, double* ms, uint64_t* launches, int capacity);
+const char* uepm_kernel_name(int kind);
+
+/* Calibration (no reference counterpart): sustained FMA throughput of the current device's FP64
+ * pipe (precision UEPM_PREC_FP64) or FP32 pipe (UEPM_PREC_MIXED), in TFLOP/s, measured with a
+ * pure-FMA kernel. Used as the roofline denominator of the compute-bound kernels. */
+int uepm_measure_peak(int precision, double* tflops);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* UEPM_GB300_H */

@@ -1,0 +1,626 @@
+// capi.cu -- the C ABI (include/uepm_gb300.h): context set-up, device workspace and the batched
+// solve pipeline over chunks of k-points.
+//
+// Pipeline per chunk (all on one stream, no host round trips):
+//   FP64  k_rows -> k_assemble -> k_tridiag<double> -> k_bisect<double> (writes E in place)
+//         [-> k_invit<double> -> k_backtransform<double> (X, gradient)]
+//   MIXED k_rows -> k_assemble (FP64 + FP32 copy) -> k_tridiag<float> -> k_bisect<float>
+//         -> k_invit<float> -> k_backtransform<float> -> k_refine (FP64 Rayleigh-Ritz: E, X, gradient)
+#include <cuda_runtime.h>
+
+#include <atomic>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "uepm_common.cuh"
+#include "uepm_gb300.h"
+#include "uepm_kernels.h"
+
+namespace uepm {
+
+static thread_local std::string g_last_error;
+static std::atomic<uint64_t>    g_launches{0};
+
+void set_error(const std::string& msg) { g_last_error = msg; }
+void count_launch(int n) { g_launches.fetch_add((uint64_t)n, std::memory_order_relaxed); }
+
+// src/Common/physical_constants.hpp:18-44
+namespace pc {
+constexpr double h           = 6.62607015e-34;
+constexpr double q_e         = 1.602176634e-19;
+constexpr double pi          = 3.141592653589793238462643383279502884;
+constexpr double h_bar       = h / (2.0 * pi);
+constexpr double m_e         = 9.1093837015e-31;
+constexpr double bohr_radius = 5.29177210903e-11;
+}  // namespace pc
+
+constexpr int kMaxOrder   = 512;  // largest matrix order n the kernels are instantiated for
+constexpr int kGuardBands = 4;    // extra FP32 bands kept in the mixed-precision subspace
+constexpr size_t kMaxChunk = 32768;  // k-points per launch: the assembly grid's z extent is <= 65535
+
+}  // namespace uepm
+
+using namespace uepm;
+
+struct uepm_ctx {
+    int           device    = 0;
+    uepm_material mat{};
+    DevParams     P{};
+    int           N = 0, n = 0;
+    uint32_t      flags     = 0;
+    int           precision = UEPM_PREC_FP64;
+    size_t        ws_limit  = (size_t)8 << 30;
+    int*          d_G       = nullptr;
+    cx<double>*   d_Vloc    = nullptr;
+    double2*      d_phNL    = nullptr;
+    double2*      d_phSO    = nullptr;
+    void*         d_ws      = nullptr;
+    size_t        ws_bytes  = 0;
+    // buffers of the host-pointer entry point
+    cudaStream_t  stream    = nullptr;
+    void*         d_io      = nullptr;
+    size_t        io_bytes  = 0;
+    std::vector<int32_t> G;
+    // per-kernel timing (uepm_ctx_set_profiling)
+    struct Rec {
+        int         kind;
+        cudaEvent_t a, b;
+    };
+    int                      profiling = 0;
+    std::vector<Rec>         pending;
+    std::vector<cudaEvent_t> pool;
+    double                   prof_ms[UEPM_KERNEL_KINDS] = {0};
+    uint64_t                 prof_n[UEPM_KERNEL_KINDS]  = {0};
+};
+
+namespace {
+
+enum KernelKind { KK_ROWS = 0, KK_ASSEMBLE, KK_TRIDIAG64, KK_TRIDIAG32, KK_BISECT, KK_INVIT, KK_BACKTRANSFORM, KK_REFINE };
+const char* kKernelNames[UEPM_KERNEL_KINDS] = {"rows", "assemble", "tridiag_fp64", "tridiag_fp32",
+                                               "bisect", "invit", "backtransform", "refine"};
+
+cudaEvent_t take_event(uepm_ctx* ctx) {
+    if (!ctx->pool.empty()) {
+        cudaEvent_t e = ctx->pool.back();
+        ctx->pool.pop_back();
+        return e;
+    }
+    cudaEvent_t e = nullptr;
+    cudaEventCreate(&e);
+    return e;
+}
+
+// Brackets the kernels launched in its scope with events on `s` when profiling is on.
+struct ProfScope {
+    uepm_ctx*    ctx;
+    cudaStream_t s;
+    int          kind;
+    cudaEvent_t  a = nullptr;
+    ProfScope(uepm_ctx* c, cudaStream_t st, int k) : ctx(c), s(st), kind(k) {
+        if (ctx->profiling) {
+            a = take_event(ctx);
+            cudaEventRecord(a, s);
+        }
+    }
+    ~ProfScope() {
+        if (ctx->profiling && a) {
+            cudaEvent_t b = take_event(ctx);
+            cudaEventRecord(b, s);
+            ctx->pending.push_back({kind, a, b});
+        }
+    }
+};
+
+}  // namespace
+
+#define UEPM_CUDA(call)                                                                                   \
+    do {                                                                                                  \
+        cudaError_t err_ = (call);                                                                        \
+        if (err_ != cudaSuccess) {                                                                        \
+            set_error(std::string(#call) + ": " + cudaGetErrorString(err_));                              \
+            return UEPM_ERR_CUDA;                                                                         \
+        }                                                                                                 \
+    } while (0)
+
+namespace {
+
+// Pseudopotential::GetValue (src/EPP/Pseudopotential.cpp:24-56), same operand order, glibc cos/sin.
+void pp_value(const uepm_material& m, int gx, int gy, int gz, double tau, double a, double* re, double* im) {
+    const int    G2   = gx * gx + gy * gy + gz * gz;
+    const double kfac = 2.0 * pc::pi / a;
+    const double Gtau = kfac * (tau * gx + tau * gy + tau * gz);
+    double       VS = 0.0, VA = 0.0;
+    switch (G2) {
+        case 3: VS = m.V3S; VA = m.V3A; break;
+        case 4: VS = m.V4S; VA = m.V4A; break;
+        case 8: VS = m.V8S; VA = m.V8A; break;
+        case 11: VS = m.V11S; VA = m.V11A; break;
+        default: break;
+    }
+    *re = VS * std::cos(Gtau);
+    *im = VA * std::sin(Gtau);
+}
+
+size_t align_up(size_t x) { return (x + 255) & ~(size_t)255; }
+
+struct Layout {
+    size_t rows, H, H32, d, e, tq, ev, work, z, X32, refine, total;
+};
+
+// Bytes of workspace one chunk of `c` matrices needs, with the offset of every region.
+Layout plan(const uepm_ctx* ctx, int nb, uint32_t want, size_t c) {
+    const size_t n = ctx->n, N = ctx->N;
+    const bool   mixed = ctx->precision == UEPM_PREC_MIXED;
+    const bool   vecs  = (want & (UEPM_WANT_VECTORS | UEPM_WANT_GRADIENT)) != 0;
+    const size_t m     = mixed ? std::min<size_t>(n, (size_t)nb + kGuardBands) : (size_t)nb;
+    const size_t rs    = mixed ? sizeof(float) : sizeof(double);
+    Layout       L{};
+    size_t       off = 0;
+    auto         take = [&](size_t bytes) {
+        const size_t o = off;
+        off            = align_up(off + bytes);
+        return o;
+    };
+    L.rows = take(c * N * ROW_STRIDE * sizeof(double));
+    L.H    = take(c * n * n * sizeof(cx<double>));
+    L.H32  = mixed ? take(c * n * n * sizeof(cx<float>)) : 0;
+    L.d    = take(c * n * rs);
+    L.e    = take(c * n * rs);
+    L.tq   = take(c * n * 2 * rs);
+    L.ev   = mixed ? take(c * m * rs) : 0;
+    if (mixed || vecs) {
+        L.work = take(c * (mixed ? invit_work_elems<float>((int)n) : invit_work_elems<double>((int)n)) * rs);
+        L.z    = take(c * m * n * rs);
+    }
+    if (mixed) {
+        L.X32    = take(c * m * n * sizeof(cx<float>));
+        L.refine = take(c * refine_work_elems((int)n, (int)m) * sizeof(cx<double>));
+    }
+    L.total = off;
+    return L;
+}
+
+int ensure_ws(uepm_ctx* ctx, size_t bytes) {
+    if (bytes <= ctx->ws_bytes) return UEPM_OK;
+    if (ctx->d_ws) cudaFree(ctx->d_ws);
+    ctx->d_ws     = nullptr;
+    ctx->ws_bytes = 0;
+    if (cudaMalloc(&ctx->d_ws, bytes) != cudaSuccess) {
+        cudaGetLastError();
+        set_error("device workspace allocation of " + std::to_string(bytes) + " bytes failed");
+        return UEPM_ERR_NOMEM;
+    }
+    ctx->ws_bytes = bytes;
+    return UEPM_OK;
+}
+
+int check_launch() {
+    const cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) {
+        set_error(std::string("kernel launch failed: ") + cudaGetErrorString(e));
+        return UEPM_ERR_CUDA;
+    }
+    return UEPM_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int uepm_version(void) { return 10000; }
+const char* uepm_last_error(void) { return g_last_error.c_str(); }
+uint64_t uepm_kernel_launches(void) { return g_launches.load(); }
+
+int uepm_ctx_create(const uepm_material* mat, const int32_t* G, int N, uint32_t flags, uepm_ctx** out) {
+    if (!mat || !G || !out || N <= 0) {
+        set_error("uepm_ctx_create: null argument or empty basis");
+        return UEPM_ERR_INVALID;
+    }
+    const bool soc = (flags & UEPM_SOC) != 0, nl = (flags & UEPM_NONLOCAL) != 0;
+    const int  n   = soc ? 2 * N : N;
+    if (n > kMaxOrder) {
+        set_error("matrix order " + std::to_string(n) + " exceeds the supported maximum " + std::to_string(kMaxOrder));
+        return UEPM_ERR_INVALID;
+    }
+    if (soc && (mat->period_cation < 2 || mat->period_cation > 4)) {
+        set_error("SpinOrbitCorrection::compute_lambda_1: Unsupported period for cation.");
+        return UEPM_ERR_RUNTIME;
+    }
+    if (soc && (mat->period_anion < 2 || mat->period_anion > 4)) {
+        set_error("SpinOrbitCorrection::compute_lambda_2: Unsupported period for anion.");
+        return UEPM_ERR_RUNTIME;
+    }
+    auto* ctx  = new uepm_ctx();
+    ctx->mat   = *mat;
+    ctx->N     = N;
+    ctx->n     = n;
+    ctx->flags = flags;
+    ctx->G.assign(G, G + 3 * (size_t)N);
+    cudaGetDevice(&ctx->device);
+
+    // Derived constants, each with the reference's own expression.
+    const double a             = 1.0e-10 * mat->lattice_constant;          // Material.h:108-111
+    const double two_pi_over_a = 2.0 * M_PI / a;                           // Hamiltonian.cpp:56
+    const double diag_factor   = (pc::h_bar * pc::h_bar) / (2.0 * pc::m_e * pc::q_e);
+    DevParams&   P             = ctx->P;
+    P.N            = N;
+    P.n            = n;
+    P.nl           = nl ? 1 : 0;
+    P.soc          = soc ? 1 : 0;
+    P.square       = (mat->nl_well == 1) ? 1 : 0;
+    P.kin_pref     = two_pi_over_a * two_pi_over_a * diag_factor;
+    P.grad_pref    = 2.0 * diag_factor * (two_pi_over_a * two_pi_over_a);  // Hamiltonian.cpp:167
+    P.frac_to_phys = 1.0 / two_pi_over_a;
+    const double volume = (1.0 / 8.0) * pow(a, 3.0);                     // Material.h:130
+    const double kF     = pow(96 * M_PI * M_PI, 1.0 / 3.0) / a;           // Material.h:170
+    P.ff      = 2.0 * M_PI / a;
+    P.nl_df   = pow(pc::h_bar, 2) / (2.0 * pc::m_e * pc::q_e);
+    P.Vpre    = 4.0 * M_PI / volume;
+    P.kF2     = pow(kF, 2.0);
+    P.alpha0a = mat->alpha0_anion;
+    P.beta0a  = mat->beta0_anion;
+    P.A2a     = mat->A2_anion;
+    P.alpha0c = mat->alpha0_cation;
+    P.beta0c  = mat->beta0_cation;
+    P.A2c     = mat->A2_cation;
+    P.R0a     = mat->R0_anion;
+    P.R0c     = mat->R0_cation;
+    P.R2a     = mat->R2_anion;
+    P.R2c     = mat->R2_cation;
+    P.has_R0a = (mat->R0_anion != 0.0);
+    P.has_R0c = (mat->R0_cation != 0.0);
+    P.has_A2a = (mat->A2_anion != 0.0);
+    P.has_A2c = (mat->A2_cation != 0.0);
+    P.R0a2 = pow(P.R0a, 2.0);
+    P.R0c2 = pow(P.R0c, 2.0);
+    P.R2a2 = pow(P.R2a, 2.0);
+    P.R2c2 = pow(P.R2c, 2.0);
+    P.R0a3h = pow(P.R0a, 3.0) / (2.0);
+    P.R0c3h = pow(P.R0c, 3.0) / (2.0);
+    P.R2a3h = pow(P.R2a, 3.0) / (2.0);
+    P.R2c3h = pow(P.R2c, 3.0) / (2.0);
+    P.R0a3t = pow(P.R0a, 3.0) / (3.0);
+    P.R0c3t = pow(P.R0c, 3.0) / (3.0);
+    P.gpre_a = 5.0 * pow(M_PI, 1.5) * (pow(P.R2a, 3.0) / volume);
+    P.gpre_c = 5.0 * pow(M_PI, 1.5) * (pow(P.R2c, 3.0) / volume);
+    P.pa        = mat->period_anion;
+    P.pc        = mat->period_cation;
+    P.ra        = mat->radial_extent_anion;
+    P.rc        = mat->radial_extent_cation;
+    P.alpha_soc = mat->alpha_soc;
+    P.mu_soc    = mat->mu_soc;
+    P.kfac      = (2.0 * M_PI) / a;
+    P.bohr      = pc::bohr_radius;
+
+    // k-independent tables: local form factors (SetConstantNonDiagonalMatrix, Hamiltonian.cpp:32-48)
+    // and the structure phases of the nonlocal and spin-orbit terms.
+    const double         tau = (1.0 / 8.0) * a;
+    std::vector<double2> V((size_t)N * N), phNL, phSO;
+    if (nl) phNL.resize((size_t)N * N);
+    if (soc) phSO.resize((size_t)N * N);
+    for (int j = 0; j < N; ++j)
+        for (int i = 0; i < N; ++i) {
+            const int dx = G[3 * i] - G[3 * j], dy = G[3 * i + 1] - G[3 * j + 1], dz = G[3 * i + 2] - G[3 * j + 2];
+            double    re, im;
+            pp_value(*mat, dx, dy, dz, tau, a, &re, &im);
+            V[(size_t)j * N + i] = make_double2(re, im);
+            if (nl) {
+                // Material.cpp:202-205: 2 pi (tau / a).(G_i - G_j), with tau / a = 1/8 exactly
+                const double ta = tau / a;
+                const double Gt = ta * (double)dx + ta * (double)dy + ta * (double)dz;
+                phNL[(size_t)j * N + i] = make_double2(cos(2.0 * M_PI * Gt), sin(2.0 * M_PI * Gt));
+            }
+            if (soc) {
+                // SpinOrbitFunctional.cpp:132: kfac * (tau . (G - G'))
+                const double g = P.kfac * (tau * (double)dx + tau * (double)dy + tau * (double)dz);
+                phSO[(size_t)j * N + i] = make_double2(std::cos(g), std::sin(g));
+            }
+        }
+    auto fail = [&](cudaError_t e, const char* what) {
+        set_error(std::string(what) + ": " + cudaGetErrorString(e));
+        uepm_ctx_destroy(ctx);
+        return UEPM_ERR_CUDA;
+    };
+    cudaError_t e;
+    if ((e = cudaMalloc(&ctx->d_G, sizeof(int) * 3 * N)) != cudaSuccess) return fail(e, "cudaMalloc(G)");
+    if ((e = cudaMemcpy(ctx->d_G, G, sizeof(int) * 3 * N, cudaMemcpyHostToDevice)) != cudaSuccess) return fail(e, "copy G");
+    if ((e = cudaMalloc(&ctx->d_Vloc, sizeof(double2) * V.size())) != cudaSuccess) return fail(e, "cudaMalloc(V)");
+    if ((e = cudaMemcpy(ctx->d_Vloc, V.data(), sizeof(double2) * V.size(), cudaMemcpyHostToDevice)) != cudaSuccess)
+        return fail(e, "copy V");
+    if (nl) {
+        if ((e = cudaMalloc(&ctx->d_phNL, sizeof(double2) * phNL.size())) != cudaSuccess) return fail(e, "cudaMalloc(phNL)");
+        if ((e = cudaMemcpy(ctx->d_phNL, phNL.data(), sizeof(double2) * phNL.size(), cudaMemcpyHostToDevice)) != cudaSuccess)
+            return fail(e, "copy phNL");
+    }
+    if (soc) {
+        if ((e = cudaMalloc(&ctx->d_phSO, sizeof(double2) * phSO.size())) != cudaSuccess) return fail(e, "cudaMalloc(phSO)");
+        if ((e = cudaMemcpy(ctx->d_phSO, phSO.data(), sizeof(double2) * phSO.size(), cudaMemcpyHostToDevice)) != cudaSuccess)
+            return fail(e, "copy phSO");
+    }
+    *out = ctx;
+    return UEPM_OK;
+}
+
+int uepm_ctx_destroy(uepm_ctx* ctx) {
+    if (!ctx) return UEPM_OK;
+    if (ctx->d_G) cudaFree(ctx->d_G);
+    if (ctx->d_Vloc) cudaFree(ctx->d_Vloc);
+    if (ctx->d_phNL) cudaFree(ctx->d_phNL);
+    if (ctx->d_phSO) cudaFree(ctx->d_phSO);
+    if (ctx->d_ws) cudaFree(ctx->d_ws);
+    if (ctx->d_io) cudaFree(ctx->d_io);
+    if (ctx->stream) cudaStreamDestroy(ctx->stream);
+    for (auto& r : ctx->pending) {
+        cudaEventDestroy(r.a);
+        cudaEventDestroy(r.b);
+    }
+    for (auto e : ctx->pool) cudaEventDestroy(e);
+    delete ctx;
+    return UEPM_OK;
+}
+
+int uepm_ctx_set_precision(uepm_ctx* ctx, int precision) {
+    if (!ctx || (precision != UEPM_PREC_FP64 && precision != UEPM_PREC_MIXED)) {
+        set_error("uepm_ctx_set_precision: bad context or precision");
+        return UEPM_ERR_INVALID;
+    }
+    ctx->precision = precision;
+    return UEPM_OK;
+}
+
+int uepm_ctx_order(const uepm_ctx* ctx) { return ctx ? ctx->n : UEPM_ERR_INVALID; }
+
+int uepm_ctx_set_workspace_limit(uepm_ctx* ctx, size_t bytes) {
+    if (!ctx || bytes == 0) return UEPM_ERR_INVALID;
+    ctx->ws_limit = bytes;
+    return UEPM_OK;
+}
+
+int uepm_solve_device(uepm_ctx* ctx, const double* d_k, size_t nk, int nb, uint32_t want, double* d_E, double* d_X,
+                      double* d_grad, int32_t* d_status, void* stream) {
+    if (!ctx || (!d_k && nk) || (!d_E && nk)) {
+        set_error("uepm_solve_device: null argument");
+        return UEPM_ERR_INVALID;
+    }
+    if (nb < 1 || nb > ctx->n) {
+        set_error("uepm_solve_device: nb must be in [1, n]");
+        return UEPM_ERR_OUT_OF_RANGE;
+    }
+    if ((want & UEPM_WANT_VECTORS) && !d_X) {
+        set_error("uepm_solve_device: UEPM_WANT_VECTORS without an X buffer");
+        return UEPM_ERR_INVALID;
+    }
+    if ((want & UEPM_WANT_GRADIENT) && !d_grad) {
+        set_error("uepm_solve_device: UEPM_WANT_GRADIENT without a gradient buffer");
+        return UEPM_ERR_INVALID;
+    }
+    const bool mixed = ctx->precision == UEPM_PREC_MIXED;
+    const int  n     = ctx->n;
+    const int  m     = mixed ? std::min(n, nb + kGuardBands) : nb;
+    if (mixed && m > kRefineMaxSubspace) {
+        set_error("mixed precision supports at most " + std::to_string(kRefineMaxSubspace - kGuardBands) + " bands");
+        return UEPM_ERR_INVALID;
+    }
+    if (nk == 0) return UEPM_OK;
+    cudaStream_t s = (cudaStream_t)stream;
+
+    // chunk size from the workspace budget
+    const size_t per   = plan(ctx, nb, want, 1).total;
+    size_t       chunk = std::max<size_t>(1, ctx->ws_limit / std::max<size_t>(per, 1));
+    chunk              = std::min(std::min(chunk, nk), kMaxChunk);
+    const Layout L     = plan(ctx, nb, want, chunk);
+    int          rc    = ensure_ws(ctx, L.total);
+    if (rc) return rc;
+    char* ws = static_cast<char*>(ctx->d_ws);
+    if (d_status) UEPM_CUDA(cudaMemsetAsync(d_status, 0, sizeof(int32_t) * nk, s));
+
+    const bool   want_vec  = (want & UEPM_WANT_VECTORS) != 0;
+    const bool   want_grad = (want & UEPM_WANT_GRADIENT) != 0;
+    const size_t mstride   = (size_t)n * n;
+    for (size_t off = 0; off < nk; off += chunk) {
+        const int     c    = (int)std::min(chunk, nk - off);
+        const double* kk   = d_k + 3 * off;
+        int*          st   = d_status ? d_status + off : nullptr;
+        double*       E    = d_E + off * nb;
+        auto*         rows = reinterpret_cast<double*>(ws + L.rows);
+        auto*         H    = reinterpret_cast<cx<double>*>(ws + L.H);
+        cx<double>*   Xo   = want_vec ? reinterpret_cast<cx<double>*>(d_X) + off * nb * n : nullptr;
+        double*       gr   = want_grad ? d_grad + off * nb * 3 : nullptr;
+        {
+            ProfScope p(ctx, s, KK_ROWS);
+            launch_rows(ctx->P, kk, ctx->d_G, rows, c, s);
+        }
+        if (!mixed) {
+            {
+                ProfScope p(ctx, s, KK_ASSEMBLE);
+                launch_assemble(ctx->P, ctx->d_Vloc, ctx->d_phNL, ctx->d_phSO, rows, H, n, mstride, nullptr, 0, c, s);
+            }
+            auto* d  = reinterpret_cast<double*>(ws + L.d);
+            auto* e  = reinterpret_cast<double*>(ws + L.e);
+            auto* tq = reinterpret_cast<cx<double>*>(ws + L.tq);
+            {
+                ProfScope p(ctx, s, KK_TRIDIAG64);
+                launch_tridiag<double>(H, n, n, mstride, d, e, tq, st, c, s);
+            }
+            {
+                ProfScope p(ctx, s, KK_BISECT);
+                launch_bisect<double>(d, e, n, nb, E, nb, c, s);
+            }
+            if (want_vec || want_grad) {
+                auto* work = reinterpret_cast<double*>(ws + L.work);
+                auto* z    = reinterpret_cast<double*>(ws + L.z);
+                {
+                    ProfScope p(ctx, s, KK_INVIT);
+                    launch_invit<double>(d, e, E, nb, n, nb, work, z, st, c, s);
+                }
+                ProfScope p(ctx, s, KK_BACKTRANSFORM);
+                launch_backtransform<double>(H, n, n, mstride, tq, z, nb, Xo, ctx->P, kk, ctx->d_G, gr, nullptr, nullptr, c, s);
+            }
+        } else {
+            auto* H32 = reinterpret_cast<cx<float>*>(ws + L.H32);
+            {
+                ProfScope p(ctx, s, KK_ASSEMBLE);
+                launch_assemble(ctx->P, ctx->d_Vloc, ctx->d_phNL, ctx->d_phSO, rows, H, n, mstride, H32, mstride, c, s);
+            }
+            auto* d    = reinterpret_cast<float*>(ws + L.d);
+            auto* e    = reinterpret_cast<float*>(ws + L.e);
+            auto* tq   = reinterpret_cast<cx<float>*>(ws + L.tq);
+            auto* ev   = reinterpret_cast<float*>(ws + L.ev);
+            auto* work = reinterpret_cast<float*>(ws + L.work);
+            auto* z    = reinterpret_cast<float*>(ws + L.z);
+            auto* X32  = reinterpret_cast<cx<float>*>(ws + L.X32);
+            auto* rw   = reinterpret_cast<cx<double>*>(ws + L.refine);
+            {
+                ProfScope p(ctx, s, KK_TRIDIAG32);
+                launch_tridiag<float>(H32, n, n, mstride, d, e, tq, st, c, s);
+            }
+            {
+                ProfScope p(ctx, s, KK_BISECT);
+                launch_bisect<float>(d, e, n, m, ev, m, c, s);
+            }
+            {
+                ProfScope p(ctx, s, KK_INVIT);
+                launch_invit<float>(d, e, ev, m, n, m, work, z, st, c, s);
+            }
+            {
+                ProfScope p(ctx, s, KK_BACKTRANSFORM);
+                launch_backtransform<float>(H32, n, n, mstride, tq, z, m, X32, ctx->P, kk, ctx->d_G, nullptr, nullptr, nullptr, c, s);
+            }
+            {
+                ProfScope p(ctx, s, KK_REFINE);
+                launch_refine(H, n, n, mstride, X32, m, nb, E, Xo, gr, ctx->P, kk, ctx->d_G, rw, st, c, s);
+            }
+        }
+        if ((rc = check_launch())) return rc;
+    }
+    return UEPM_OK;
+}
+
+int uepm_assemble_device(uepm_ctx* ctx, const double* d_k, size_t nk, double* d_H, void* stream) {
+    if (!ctx || (nk && (!d_k || !d_H))) {
+        set_error("uepm_assemble_device: null argument");
+        return UEPM_ERR_INVALID;
+    }
+    if (nk == 0) return UEPM_OK;
+    cudaStream_t s   = (cudaStream_t)stream;
+    const int    n   = ctx->n;
+    const size_t per = (size_t)ctx->N * ROW_STRIDE * sizeof(double);
+    size_t       chunk = std::min(std::min<size_t>(nk, std::max<size_t>(1, ctx->ws_limit / per)), kMaxChunk);
+    int          rc    = ensure_ws(ctx, align_up(chunk * per));
+    if (rc) return rc;
+    const size_t mstride = (size_t)n * n;
+    UEPM_CUDA(cudaMemsetAsync(d_H, 0, sizeof(cx<double>) * mstride * nk, s));
+    for (size_t off = 0; off < nk; off += chunk) {
+        const int c    = (int)std::min(chunk, nk - off);
+        auto*     rows = reinterpret_cast<double*>(ctx->d_ws);
+        auto*     H    = reinterpret_cast<cx<double>*>(d_H) + off * mstride;
+        launch_rows(ctx->P, d_k + 3 * off, ctx->d_G, rows, c, s);
+        launch_assemble(ctx->P, ctx->d_Vloc, ctx->d_phNL, ctx->d_phSO, rows, H, n, mstride, nullptr, 0, c, s);
+        launch_mirror_upper(H, n, n, mstride, c, s);
+        if ((rc = check_launch())) return rc;
+    }
+    return UEPM_OK;
+}
+
+int uepm_ctx_set_profiling(uepm_ctx* ctx, int on) {
+    if (!ctx) return UEPM_ERR_INVALID;
+    ctx->profiling = on ? 1 : 0;
+    for (int q = 0; q < UEPM_KERNEL_KINDS; ++q) {
+        ctx->prof_ms[q] = 0.0;
+        ctx->prof_n[q]  = 0;
+    }
+    return UEPM_OK;
+}
+
+int uepm_ctx_read_profile(uepm_ctx* ctx, double* ms, uint64_t* launches, int capacity) {
+    if (!ctx) return UEPM_ERR_INVALID;
+    for (auto& r : ctx->pending) {
+        UEPM_CUDA(cudaEventSynchronize(r.b));
+        float t = 0.f;
+        UEPM_CUDA(cudaEventElapsedTime(&t, r.a, r.b));
+        ctx->prof_ms[r.kind] += t;
+        ctx->prof_n[r.kind] += 1;
+        ctx->pool.push_back(r.a);
+        ctx->pool.push_back(r.b);
+    }
+    ctx->pending.clear();
+    for (int q = 0; q < capacity && q < UEPM_KERNEL_KINDS; ++q) {
+        if (ms) ms[q] = ctx->prof_ms[q];
+        if (launches) launches[q] = ctx->prof_n[q];
+    }
+    return UEPM_KERNEL_KINDS;
+}
+
+const char* uepm_kernel_name(int kind) { return (kind >= 0 && kind < UEPM_KERNEL_KINDS) ? kKernelNames[kind] : ""; }
+
+int uepm_solve(uepm_ctx* ctx, const double* k, size_t nk, int nb, uint32_t want, double* E, double* X, double* grad,
+               int32_t* status) {
+    if (!ctx || (nk && (!k || !E))) {
+        set_error("uepm_solve: null argument");
+        return UEPM_ERR_INVALID;
+    }
+    if (nb < 1 || nb > ctx->n) {
+        set_error("uepm_solve: nb must be in [1, n]");
+        return UEPM_ERR_OUT_OF_RANGE;
+    }
+    if (nk == 0) return UEPM_OK;
+    if ((want & UEPM_WANT_VECTORS) && !X) {
+        set_error("uepm_solve: UEPM_WANT_VECTORS without an X buffer");
+        return UEPM_ERR_INVALID;
+    }
+    if ((want & UEPM_WANT_GRADIENT) && !grad) {
+        set_error("uepm_solve: UEPM_WANT_GRADIENT without a gradient buffer");
+        return UEPM_ERR_INVALID;
+    }
+    if (!ctx->stream) UEPM_CUDA(cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking));
+    const bool   wv = (want & UEPM_WANT_VECTORS) != 0, wg = (want & UEPM_WANT_GRADIENT) != 0;
+    const size_t bk = align_up(sizeof(double) * 3 * nk), bE = align_up(sizeof(double) * nk * nb);
+    const size_t bX = wv ? align_up(sizeof(double) * 2 * nk * nb * ctx->n) : 0;
+    const size_t bg = wg ? align_up(sizeof(double) * 3 * nk * nb) : 0;
+    const size_t bs = align_up(sizeof(int32_t) * nk);
+    const size_t need = bk + bE + bX + bg + bs;
+    if (need > ctx->io_bytes) {
+        if (ctx->d_io) cudaFree(ctx->d_io);
+        ctx->d_io     = nullptr;
+        ctx->io_bytes = 0;
+        if (cudaMalloc(&ctx->d_io, need) != cudaSuccess) {
+            cudaGetLastError();
+            set_error("uepm_solve: device I/O allocation failed");
+            return UEPM_ERR_NOMEM;
+        }
+        ctx->io_bytes = need;
+    }
+    char*   io  = static_cast<char*>(ctx->d_io);
+    double* dk  = reinterpret_cast<double*>(io);
+    double* dE  = reinterpret_cast<double*>(io + bk);
+    double* dX  = wv ? reinterpret_cast<double*>(io + bk + bE) : nullptr;
+    double* dg  = wg ? reinterpret_cast<double*>(io + bk + bE + bX) : nullptr;
+    auto*   dst = reinterpret_cast<int32_t*>(io + bk + bE + bX + bg);
+    cudaStream_t s = ctx->stream;
+    UEPM_CUDA(cudaMemcpyAsync(dk, k, sizeof(double) * 3 * nk, cudaMemcpyHostToDevice, s));
+    int rc = uepm_solve_device(ctx, dk, nk, nb, want, dE, dX, dg, dst, s);
+    if (rc) return rc;
+    UEPM_CUDA(cudaMemcpyAsync(E, dE, sizeof(double) * nk * nb, cudaMemcpyDeviceToHost, s));
+    if (wv) UEPM_CUDA(cudaMemcpyAsync(X, dX, sizeof(double) * 2 * nk * nb * ctx->n, cudaMemcpyDeviceToHost, s));
+    if (wg) UEPM_CUDA(cudaMemcpyAsync(grad, dg, sizeof(double) * 3 * nk * nb, cudaMemcpyDeviceToHost, s));
+    std::vector<int32_t> hs;
+    int32_t*             so = status;
+    if (!so) {
+        hs.resize(nk);
+        so = hs.data();
+    }
+    UEPM_CUDA(cudaMemcpyAsync(so, dst, sizeof(int32_t) * nk, cudaMemcpyDeviceToHost, s));
+    UEPM_CUDA(cudaStreamSynchronize(s));
+    for (size_t q = 0; q < nk; ++q)
+        if (so[q] != 0) {
+            set_error("uepm_solve: k-point " + std::to_string(q) + " reported status " + std::to_string(so[q]));
+            return UEPM_ERR_NOT_CONVERGED;
+        }
+    return UEPM_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,286 @@
+// tridiag_eig.cu -- eigenvalues and eigenvectors of the real symmetric tridiagonal T from tridiag.cu.
+//
+// The reference computes ALL n eigenvalues with Eigen's implicit QR (Hamiltonian.cpp:125-134) and
+// then keeps the first nb (BandStructure.cpp:183-184). Here only the nb lowest are computed:
+//
+//   k_bisect  Sturm-count bisection (one warp per matrix, one lane per eigenvalue index), with
+//             LAPACK dstebz's pivot guard and absolute/relative stopping tolerances. Each value is
+//             the j-th smallest eigenvalue of T to about eps * ||T||.
+//   k_invit   inverse iteration (one warp per matrix, one lane per eigenvalue): LU with partial
+//             pivoting of T - lambda I, three solves from a deterministic pseudo-random start,
+//             LAPACK dstein's shift perturbation for (near-)equal eigenvalues and modified
+//             Gram-Schmidt inside clusters (consecutive gaps <= 1e-3 ||T||_1), so degenerate
+//             bands (Kramers pairs with SOC, the Gamma-point triplets) get an orthonormal basis of
+//             their eigenspace. Iteration counts are fixed: nothing here can spin.
+#include "uepm_common.cuh"
+#include "uepm_kernels.h"
+
+namespace uepm {
+
+constexpr int kBisectWarpsPerBlock = 4;
+constexpr int kInvitWarpsPerBlock  = 2;
+constexpr int kInvitIters          = 3;
+
+template <typename T>
+__device__ __forceinline__ int sturm_count(const T* __restrict__ d, const T* __restrict__ e2, int n, T x, T pivmin) {
+    T   q   = d[0] - x;
+    if (fabs(q) <= pivmin) q = -pivmin;
+    int cnt = (q < T(0));
+    for (int i = 1; i < n; ++i) {
+        q = (d[i] - x) - e2[i - 1] / q;
+        if (fabs(q) <= pivmin) q = -pivmin;
+        cnt += (q < T(0));
+    }
+    return cnt;
+}
+
+template <typename T>
+__global__ void k_bisect(const T* __restrict__ dIn, const T* __restrict__ eIn, int n, int nb, T* __restrict__ evOut, int ev_ld,
+                         int batch) {
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int b    = blockIdx.x * kBisectWarpsPerBlock + warp;
+    extern __shared__ __align__(16) unsigned char smraw[];
+    T* d  = reinterpret_cast<T*>(smraw) + (size_t)warp * 2 * n;
+    T* e2 = d + n;
+    if (b >= batch) return;
+    const T* dg = dIn + (size_t)b * n;
+    const T* eg = eIn + (size_t)b * n;
+    T        lo = T(3.0e38), hi = T(-3.0e38), emax2 = T(0);
+    for (int i = lane; i < n; i += 32) {
+        const T di = dg[i];
+        const T em = (i > 0) ? fabs(eg[i - 1]) : T(0);
+        const T ep = (i < n - 1) ? fabs(eg[i]) : T(0);
+        d[i]       = di;
+        if (i < n - 1) {
+            e2[i] = eg[i] * eg[i];
+            emax2 = max(emax2, e2[i]);
+        }
+        lo = min(lo, di - em - ep);
+        hi = max(hi, di + em + ep);
+    }
+    lo    = warp_min(lo);
+    hi    = warp_max(hi);
+    emax2 = warp_max(emax2);
+    __syncwarp();
+    const T eps    = num<T>::eps();
+    const T pivmin = num<T>::tiny() * max(T(1), emax2);
+    const T tnorm  = max(fabs(lo), fabs(hi));
+    const T widen  = T(2) * eps * tnorm * T(n) + T(2) * pivmin;
+    lo -= widen;
+    hi += widen;
+    const T atol = eps * tnorm;
+    for (int j = lane; j < nb; j += 32) {
+        T a = lo, c = hi;
+        // count(a) <= j < count(c) holds throughout; at most ~log2(range / atol) < 200 steps.
+        for (int it = 0; it < 200; ++it) {
+            const T mid = T(0.5) * (a + c);
+            const T tol = max(atol, T(2) * eps * max(fabs(a), fabs(c)));
+            if (c - a <= tol || mid <= a || mid >= c) break;
+            if (sturm_count(d, e2, n, mid, pivmin) > j) c = mid;
+            else a = mid;
+        }
+        evOut[(size_t)b * ev_ld + j] = T(0.5) * (a + c);
+    }
+}
+
+template <typename T>
+void launch_bisect(const T* d, const T* e, int n, int nb, T* ev, int ev_ld, int batch, cudaStream_t s) {
+    const int    blocks = (batch + kBisectWarpsPerBlock - 1) / kBisectWarpsPerBlock;
+    const size_t smem   = sizeof(T) * 2 * (size_t)n * kBisectWarpsPerBlock;
+    k_bisect<T><<<blocks, 32 * kBisectWarpsPerBlock, smem, s>>>(d, e, n, nb, ev, ev_ld, batch);
+    count_launch();
+}
+
+// ------------------------------------------------------------------------------------------------
+// Inverse iteration. Per matrix the workspace holds 5 arrays of n x 32 values, interleaved by
+// lane ([i][lane]) so that the 32 lanes of a warp touch consecutive addresses at every step i:
+// U0, U1, U2 (the upper-triangular factor's three diagonals), Y (forward-eliminated right-hand
+// side) and Z (the current iterate).
+
+__device__ __forceinline__ unsigned hash32(unsigned x) {
+    x ^= x >> 16;
+    x *= 0x7feb352dU;
+    x ^= x >> 15;
+    x *= 0x846ca68bU;
+    x ^= x >> 16;
+    return x;
+}
+
+template <typename T>
+__global__ void k_invit(const T* __restrict__ dIn, const T* __restrict__ eIn, const T* __restrict__ ev, int ev_ld, int n,
+                        int nb, T* __restrict__ work, T* __restrict__ zOut, int* __restrict__ status, int batch) {
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int b    = blockIdx.x * kInvitWarpsPerBlock + warp;
+    __shared__ T   s_lam[kInvitWarpsPerBlock][33];
+    __shared__ int s_gs[kInvitWarpsPerBlock][33];
+    if (b >= batch) return;
+    const T* d = dIn + (size_t)b * n;
+    const T* e = eIn + (size_t)b * n;
+    T*       W = work + (size_t)b * invit_work_elems<T>(n);
+    T *U0 = W, *U1 = W + (size_t)n * 32, *U2 = W + (size_t)2 * n * 32, *Y = W + (size_t)3 * n * 32, *Z = W + (size_t)4 * n * 32;
+    T* zb = zOut + (size_t)b * nb * n;  // final vectors, [j][i]
+
+    // ||T||_1 for the cluster tolerance and the tiny-pivot replacement (dstein / dlagts).
+    T onenrm = 0;
+    for (int i = lane; i < n; i += 32) {
+        const T r = fabs(d[i]) + (i > 0 ? fabs(e[i - 1]) : T(0)) + (i < n - 1 ? fabs(e[i]) : T(0));
+        onenrm    = max(onenrm, r);
+    }
+    onenrm          = warp_max(onenrm);
+    const T eps     = num<T>::eps();
+    const T ortol   = T(1e-3) * onenrm;
+    const T pivtiny = eps * onenrm;
+    bool    bad     = false;
+
+    // carried across groups of 32: the previous (perturbed) shift and cluster start
+    T   prev_lam = T(0);
+    int prev_gs  = 0;
+    for (int g0 = 0; g0 < nb; g0 += 32) {
+        const int gn = min(32, nb - g0);
+        if (lane == 0) {
+            T   pl = prev_lam;
+            int pg = prev_gs;
+            for (int q = 0; q < gn; ++q) {
+                const int j  = g0 + q;
+                T         xj = ev[(size_t)b * ev_ld + j];
+                if (j > 0) {
+                    const T pertol = T(10) * fabs(eps * xj);
+                    if (xj - pl < pertol) xj = pl + pertol;
+                    if (xj - pl > ortol) pg = j;
+                } else {
+                    pg = 0;
+                }
+                s_lam[warp][q] = xj;
+                s_gs[warp][q]  = pg;
+                pl             = xj;
+            }
+            prev_lam = pl;
+            prev_gs  = pg;
+        }
+        __syncwarp();
+        prev_lam = __shfl_sync(0xffffffffu, prev_lam, 0);
+        prev_gs  = __shfl_sync(0xffffffffu, prev_gs, 0);
+        const bool active = lane < gn;
+        const T    lam    = active ? s_lam[warp][lane] : T(0);
+        const int  j      = g0 + lane;
+
+        // deterministic start vector in (-1, 1)
+        if (active)
+            for (int i = 0; i < n; ++i) {
+                const unsigned h = hash32((unsigned)(j * 7919 + 13) ^ hash32((unsigned)i + 0x9e3779b9U));
+                Z[(size_t)i * 32 + lane] = T(2) * T(h & 0xffffff) / T(16777216) - T(1) + T(1e-3);
+            }
+        __syncwarp();
+
+        for (int it = 0; it < kInvitIters; ++it) {
+            if (active) {
+                // LU with partial pivoting of T - lam I, applied to the right-hand side Z -> Y.
+                T p0 = d[0] - lam, p1 = (n > 1) ? e[0] : T(0), p2 = T(0), rp = Z[lane];
+                for (int i = 0; i < n - 1; ++i) {
+                    const T s0 = e[i], s1 = d[i + 1] - lam, s2 = (i + 1 < n - 1) ? e[i + 1] : T(0);
+                    const T rs = Z[(size_t)(i + 1) * 32 + lane];
+                    T       n0, n1, nr;
+                    if (fabs(p0) >= fabs(s0)) {
+                        if (p0 == T(0)) p0 = pivtiny;
+                        const T l = s0 / p0;
+                        U0[(size_t)i * 32 + lane] = p0;
+                        U1[(size_t)i * 32 + lane] = p1;
+                        U2[(size_t)i * 32 + lane] = p2;
+                        Y[(size_t)i * 32 + lane]  = rp;
+                        n0 = s1 - l * p1;
+                        n1 = s2 - l * p2;
+                        nr = rs - l * rp;
+                    } else {
+                        const T l = p0 / s0;
+                        U0[(size_t)i * 32 + lane] = s0;
+                        U1[(size_t)i * 32 + lane] = s1;
+                        U2[(size_t)i * 32 + lane] = s2;
+                        Y[(size_t)i * 32 + lane]  = rs;
+                        n0 = p1 - l * s1;
+                        n1 = p2 - l * s2;
+                        nr = rp - l * rs;
+                    }
+                    p0 = n0;
+                    p1 = n1;
+                    p2 = T(0);
+                    rp = nr;
+                }
+                if (fabs(p0) < pivtiny) p0 = (p0 < T(0)) ? -pivtiny : pivtiny;
+                // back substitution into Z, scaled by the largest entry to stay in range
+                T z2 = T(0), z1 = rp / p0;
+                Z[(size_t)(n - 1) * 32 + lane] = z1;
+                T zmax = fabs(z1);
+                for (int i = n - 2; i >= 0; --i) {
+                    T u0 = U0[(size_t)i * 32 + lane];
+                    if (fabs(u0) < pivtiny) u0 = (u0 < T(0)) ? -pivtiny : pivtiny;
+                    const T zi = (Y[(size_t)i * 32 + lane] - U1[(size_t)i * 32 + lane] * z1 - U2[(size_t)i * 32 + lane] * z2) / u0;
+                    Z[(size_t)i * 32 + lane] = zi;
+                    zmax = max(zmax, fabs(zi));
+                    z2   = z1;
+                    z1   = zi;
+                }
+                // normalise to unit 2-norm (first by the max entry, then exactly)
+                const T inv = (zmax > T(0) && isfinite(zmax)) ? T(1) / zmax : T(0);
+                if (!(zmax > T(0)) || !isfinite(zmax)) bad = true;
+                T ss = T(0);
+                for (int i = 0; i < n; ++i) {
+                    const T zi = Z[(size_t)i * 32 + lane] * inv;
+                    Z[(size_t)i * 32 + lane] = zi;
+                    ss = fma(zi, zi, ss);
+                }
+                const T rn = (ss > T(0)) ? T(1) / sqrt(ss) : T(0);
+                for (int i = 0; i < n; ++i) Z[(size_t)i * 32 + lane] *= rn;
+            }
+            __syncwarp();
+            // modified Gram-Schmidt inside clusters, in index order (warp-cooperative)
+            for (int q = 0; q < gn; ++q) {
+                const int jq = g0 + q;
+                const int gs = s_gs[warp][q];
+                if (gs >= jq) continue;
+                for (int p = gs; p < jq; ++p) {
+                    // previous vector: this group's Z column, or an earlier group's final output
+                    T dot = T(0);
+                    for (int i = lane; i < n; i += 32) {
+                        const T zp = (p >= g0) ? Z[(size_t)i * 32 + (p - g0)] : zb[(size_t)p * n + i];
+                        dot        = fma(zp, Z[(size_t)i * 32 + q], dot);
+                    }
+                    dot = warp_sum(dot);
+                    for (int i = lane; i < n; i += 32) {
+                        const T zp = (p >= g0) ? Z[(size_t)i * 32 + (p - g0)] : zb[(size_t)p * n + i];
+                        Z[(size_t)i * 32 + q] -= dot * zp;
+                    }
+                    __syncwarp();
+                }
+                T ss = T(0);
+                for (int i = lane; i < n; i += 32) ss = fma(Z[(size_t)i * 32 + q], Z[(size_t)i * 32 + q], ss);
+                ss        = warp_sum(ss);
+                const T r = (ss > T(0)) ? T(1) / sqrt(ss) : T(0);
+                for (int i = lane; i < n; i += 32) Z[(size_t)i * 32 + q] *= r;
+                __syncwarp();
+            }
+        }
+        // write this group's vectors ([j][i], coalesced over i)
+        for (int q = 0; q < gn; ++q)
+            for (int i = lane; i < n; i += 32) zb[(size_t)(g0 + q) * n + i] = Z[(size_t)i * 32 + q];
+        __syncwarp();
+    }
+    bad = __any_sync(0xffffffffu, bad);
+    if (bad && lane == 0 && status) status[b] |= 2;  // UEPM_K_NONFINITE
+}
+
+template <typename T>
+void launch_invit(const T* d, const T* e, const T* ev, int ev_ld, int n, int nb, T* work, T* z, int* status, int batch,
+                  cudaStream_t s) {
+    const int blocks = (batch + kInvitWarpsPerBlock - 1) / kInvitWarpsPerBlock;
+    k_invit<T><<<blocks, 32 * kInvitWarpsPerBlock, 0, s>>>(d, e, ev, ev_ld, n, nb, work, z, status, batch);
+    count_launch();
+}
+
+template void launch_bisect<double>(const double*, const double*, int, int, double*, int, int, cudaStream_t);
+template void launch_bisect<float>(const float*, const float*, int, int, float*, int, int, cudaStream_t);
+template void launch_invit<double>(const double*, const double*, const double*, int, int, int, double*, double*, int*, int,
+                                   cudaStream_t);
+template void launch_invit<float>(const float*, const float*, const float*, int, int, int, float*, float*, int*, int,
+                                  cudaStream_t);
+
+}  // namespace uepm

@@ -1,0 +1,160 @@
+// uepm_common.cuh -- shared device types and helpers for the sm_103a band-structure kernels.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <cfloat>
+
+namespace uepm {
+
+// ------------------------------------------------------------------------------------------------
+// Complex arithmetic on (re, im) pairs, written with explicit fused multiply-adds: on GB300 every
+// FP64 instruction (add, mul or fma) costs one slot of the narrow FP64 pipe, so a complex
+// multiply-accumulate is exactly 4 FMAs and nothing else.
+template <typename T>
+struct cx {
+    T x, y;
+};
+
+template <typename T>
+__host__ __device__ __forceinline__ cx<T> mk(T x, T y) {
+    cx<T> r;
+    r.x = x;
+    r.y = y;
+    return r;
+}
+template <typename T>
+__device__ __forceinline__ cx<T> cadd(cx<T> a, cx<T> b) {
+    return mk(a.x + b.x, a.y + b.y);
+}
+template <typename T>
+__device__ __forceinline__ cx<T> csub(cx<T> a, cx<T> b) {
+    return mk(a.x - b.x, a.y - b.y);
+}
+template <typename T>
+__device__ __forceinline__ cx<T> cmul(cx<T> a, cx<T> b) {
+    return mk(fma(a.x, b.x, -a.y * b.y), fma(a.x, b.y, a.y * b.x));
+}
+// c + a * b
+template <typename T>
+__device__ __forceinline__ cx<T> cfma(cx<T> a, cx<T> b, cx<T> c) {
+    return mk(fma(a.x, b.x, fma(-a.y, b.y, c.x)), fma(a.x, b.y, fma(a.y, b.x, c.y)));
+}
+// c + conj(a) * b
+template <typename T>
+__device__ __forceinline__ cx<T> cfmac(cx<T> a, cx<T> b, cx<T> c) {
+    return mk(fma(a.x, b.x, fma(a.y, b.y, c.x)), fma(a.x, b.y, fma(-a.y, b.x, c.y)));
+}
+// c - a * conj(b)
+template <typename T>
+__device__ __forceinline__ cx<T> cfms_conjb(cx<T> a, cx<T> b, cx<T> c) {
+    return mk(fma(-a.x, b.x, fma(-a.y, b.y, c.x)), fma(-a.y, b.x, fma(a.x, b.y, c.y)));
+}
+template <typename T>
+__device__ __forceinline__ cx<T> cscale(cx<T> a, T s) {
+    return mk(a.x * s, a.y * s);
+}
+
+// 16-byte (double) / 8-byte (float) vector loads and stores of one complex element.
+__device__ __forceinline__ cx<double> ldc(const cx<double>* p) {
+    double2 v = *reinterpret_cast<const double2*>(p);
+    return mk(v.x, v.y);
+}
+__device__ __forceinline__ cx<float> ldc(const cx<float>* p) {
+    float2 v = *reinterpret_cast<const float2*>(p);
+    return mk(v.x, v.y);
+}
+__device__ __forceinline__ void stc(cx<double>* p, cx<double> a) { *reinterpret_cast<double2*>(p) = make_double2(a.x, a.y); }
+__device__ __forceinline__ void stc(cx<float>* p, cx<float> a) { *reinterpret_cast<float2*>(p) = make_float2(a.x, a.y); }
+
+template <typename T>
+__device__ __forceinline__ T warp_sum(T v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+template <typename T>
+__device__ __forceinline__ cx<T> warp_sum(cx<T> v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        v.x += __shfl_xor_sync(0xffffffffu, v.x, o);
+        v.y += __shfl_xor_sync(0xffffffffu, v.y, o);
+    }
+    return v;
+}
+template <typename T>
+__device__ __forceinline__ T warp_max(T v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = max(v, __shfl_xor_sync(0xffffffffu, v, o));
+    return v;
+}
+template <typename T>
+__device__ __forceinline__ T warp_min(T v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = min(v, __shfl_xor_sync(0xffffffffu, v, o));
+    return v;
+}
+
+template <typename T>
+struct num;
+template <>
+struct num<double> {
+    static __host__ __device__ constexpr double eps() { return DBL_EPSILON; }
+    static __host__ __device__ constexpr double tiny() { return DBL_MIN; }
+};
+template <>
+struct num<float> {
+    static __host__ __device__ constexpr float eps() { return FLT_EPSILON; }
+    static __host__ __device__ constexpr float tiny() { return FLT_MIN; }
+};
+
+// ------------------------------------------------------------------------------------------------
+// Device-side material constants. Every derived constant is computed on the host in double with the
+// reference's own expression (Material.h / Material.cpp / Hamiltonian.cpp / SpinOrbitFunctional.cpp),
+// so the kernels start from bit-identical constants.
+struct DevParams {
+    int N;        // scalar basis size
+    int n;        // matrix order (N or 2N)
+    int nl;       // nonlocal correction on
+    int soc;      // spin-orbit blocks on
+    int square;   // nonlocal well: 1 square, 0 gaussian
+    int has_R0a, has_R0c, has_A2a, has_A2c;
+    double kin_pref;      // two_pi_over_a * two_pi_over_a * diag_factor      (Hamiltonian.cpp:68-72)
+    double grad_pref;     // 2 * diag_factor * (2pi/a)^2                      (Hamiltonian.cpp:167)
+    double frac_to_phys;  // 1 / (2pi/a)                                      (Hamiltonian.cpp:190)
+    // nonlocal (Material.cpp:139-208)
+    double ff;            // fourier factor 2pi/a (1/m)
+    double nl_df;         // pow(h_bar,2)/(2 m_e q_e)
+    double Vpre;          // 4 pi / atomic volume
+    double kF2;           // pow(fermi momentum, 2)
+    double alpha0a, beta0a, A2a, alpha0c, beta0c, A2c;
+    double R0a, R0c, R2a, R2c;
+    double R0a2, R0c2, R2a2, R2c2;         // pow(R, 2.0)
+    double R0a3h, R0c3h, R2a3h, R2c3h;     // pow(R, 3.0) / 2
+    double R0a3t, R0c3t;                   // pow(R, 3.0) / 3
+    double gpre_a, gpre_c;                 // 5 pi^1.5 (R2^3 / volume)
+    // spin-orbit (SpinOrbitFunctional.cpp:20-138)
+    unsigned pa, pc;
+    double ra, rc, alpha_soc, mu_soc, kfac, bohr;
+};
+
+// Per-(k, basis vector) quantities computed once per k in the row kernel and read by the
+// element kernel. Layout: rows[(b * N + i) * ROW_STRIDE + field].
+enum RowField {
+    RF_KGX = 0, RF_KGY, RF_KGZ,   // k + G_i, reduced
+    RF_KX, RF_KY, RF_KZ,          // (k + G_i) * 2pi/a, 1/m
+    RF_NK,                        // |K_i|
+    RF_KIN,                       // kinetic diagonal C |k+G_i|^2
+    RF_J0A,                       // j_{-1}, j_0, j_1 at |K| R0_anion
+    RF_J0C = RF_J0A + 3,          // j_{-1}, j_0, j_1 at |K| R0_cation
+    RF_J2A = RF_J0C + 3,          // j_1, j_2, j_3 at |K| R2_anion (square well)
+    RF_J2C = RF_J2A + 3,          // j_1, j_2, j_3 at |K| R2_cation (square well)
+    RF_GEA = RF_J2C + 3,          // exp(-0.25 |K|^2 R2a^2) (gaussian well)
+    RF_GEC,                       // exp(-0.25 |K|^2 R2c^2)
+    RF_BC,                        // SOC radial factor B_period(|K|), cation
+    RF_BA,                        // anion
+    ROW_STRIDE = 24
+};
+
+}  // namespace uepm
