@@ -112,6 +112,12 @@ int uepm_ctx_set_precision(uepm_ctx* ctx, int precision);
 int uepm_ctx_order(const uepm_ctx* ctx);
 /* Upper bound, in bytes, of device workspace a solve may hold (default 8 GiB). */
 int uepm_ctx_set_workspace_limit(uepm_ctx* ctx, size_t bytes);
+/* When H(k) is exactly real for the context's material and flags (no SOC, all antisymmetric form
+ * factors zero, identical anion/cation nonlocal parameters: elemental diamond-structure crystals),
+ * the solve runs real-symmetric kernels, a quarter of the complex arithmetic, with the same results.
+ * on != 0 forces the complex kernels (for cross-checks). Returns 1 if the real kernels will run,
+ * 0 otherwise. */
+int uepm_ctx_force_complex(uepm_ctx* ctx, int on);
 
 /*
  * Batched solve over nk k-points (reduced units, nk x 3 row-major), keeping the nb lowest bands:
@@ -145,7 +151,7 @@ uint64_t uepm_kernel_launches(void);
  * bracketed by CUDA events on the launching stream. uepm_ctx_read_profile waits for the recorded
  * events and returns, per kernel kind, the accumulated milliseconds and launch counts since
  * profiling was switched on. Kinds: see uepm_kernel_name (0..UEPM_KERNEL_KINDS-1). */
-#define UEPM_KERNEL_KINDS 8
+#define UEPM_KERNEL_KINDS 10
 int uepm_ctx_set_profiling(uepm_ctx* ctx, int on);
 int uepm_ctx_read_profile(uepm_ctx* ctx, double* ms, uint64_t* launches, int capacity);
 const char* uepm_kernel_name(int kind);

@@ -26,8 +26,8 @@ def _mat(orm):
     return api.Material("m", raw=N.UepmMaterial.from_buffer_copy(bytes(orm)))
 
 
-def _ctx(orm, G, nl, soc, precision=N.UEPM_PREC_FP64):
-    return api._Context(_mat(orm), G, nl, soc, precision)
+def _ctx(orm, G, nl, soc, precision=N.UEPM_PREC_FP64, force_complex=False):
+    return api._Context(_mat(orm), G, nl, soc, precision, force_complex)
 
 
 def _kset(oracle, seed, n):
@@ -49,9 +49,11 @@ def _clusters(E, nb, tol=DEGEN):
 
 
 CASES = {
-    # name: (material key, shells, nl, soc)
+    # name: (material key, shells, nl, soc[, force the complex kernels])
     "si_cb_local_137": ("Si-CB", 10, False, False),
+    "si_cb_local_137_cx": ("Si-CB", 10, False, False, True),
     "si_d_nonlocal_137": ("Si-d", 10, True, False),
+    "si_d_nonlocal_137_cx": ("Si-d", 10, True, False, True),
     "ge_nl_soc_181": ("Ge", 12, True, True),
     "gaas_nl_soc_89": ("GaAs", 8, True, True),
     "inp_nl_113": ("InP", 9, True, False),
@@ -61,12 +63,17 @@ CASES = {
 }
 
 
+def _case(case):
+    key, shells, nl, soc, *cx = CASES[case]
+    return key, shells, nl, soc, bool(cx and cx[0])
+
+
 @pytest.mark.parametrize("case", ["si_cb_local_137", "si_d_nonlocal_137", "ge_nl_soc_181", "gaas_nl_soc_89",
                                   "inp_nl_113", "gap_soc_89"])
 def test_assembly_matches_oracle(gpu, oracle, mats, case):
     import torch
 
-    key, shells, nl, soc = CASES[case]
+    key, shells, nl, soc, _ = _case(case)
     G = oracle.generate_basis(shells)
     ks = _kset(oracle, 5, 4)
     ctx = _ctx(mats[key], G, nl, soc)
@@ -84,14 +91,15 @@ def test_assembly_matches_oracle(gpu, oracle, mats, case):
         assert err <= tol, f"{case} k={k}: max |dH| = {err:.3e} (tol {tol:.1e})"
 
 
-@pytest.mark.parametrize("case,nb,nk", [("si_cb_local_137", 16, 40), ("si_d_nonlocal_137", 12, 24),
+@pytest.mark.parametrize("case,nb,nk", [("si_cb_local_137", 16, 40), ("si_cb_local_137_cx", 16, 40),
+                                        ("si_d_nonlocal_137", 12, 24), ("si_d_nonlocal_137_cx", 12, 24),
                                         ("ge_nl_soc_181", 16, 6), ("gaas_nl_soc_89", 16, 12), ("inp_nl_113", 12, 16),
                                         ("alas_local_169", 16, 12), ("sn_nl_229", 12, 6), ("gap_soc_89", 16, 12)])
 def test_fp64_eigenvalues_match_oracle(gpu, oracle, mats, case, nb, nk):
-    key, shells, nl, soc = CASES[case]
+    key, shells, nl, soc, fcx = _case(case)
     G = oracle.generate_basis(shells)
     ks = _kset(oracle, 11, nk)
-    E, _, _, st = _ctx(mats[key], G, nl, soc).solve(ks, nb)
+    E, _, _, st = _ctx(mats[key], G, nl, soc, force_complex=fcx).solve(ks, nb)
     Eo = oracle.band_structure(mats[key], G, ks, nb, nl=nl, soc=soc)["E"]
     assert not st.any()
     err = np.abs(E - Eo).max()
@@ -108,13 +116,13 @@ def test_fp64_path_workload_matches_oracle(gpu, oracle, mats):
     assert np.abs(E - Eo).max() <= EV_TOL
 
 
-@pytest.mark.parametrize("case,nb", [("si_cb_local_137", 16), ("si_d_nonlocal_137", 12), ("ge_nl_soc_181", 16),
-                                     ("gaas_nl_soc_89", 16)])
+@pytest.mark.parametrize("case,nb", [("si_cb_local_137", 16), ("si_cb_local_137_cx", 16), ("si_d_nonlocal_137", 12),
+                                     ("ge_nl_soc_181", 16), ("gaas_nl_soc_89", 16)])
 def test_fp64_vectors_and_gradients_match_oracle(gpu, oracle, mats, case, nb):
-    key, shells, nl, soc = CASES[case]
+    key, shells, nl, soc, fcx = _case(case)
     G = oracle.generate_basis(shells)
     ks = _kset(oracle, 23, 3)
-    E, X, g, st = _ctx(mats[key], G, nl, soc).solve(ks, nb, vectors=True, gradient=True)
+    E, X, g, st = _ctx(mats[key], G, nl, soc, force_complex=fcx).solve(ks, nb, vectors=True, gradient=True)
     ref = oracle.band_structure(mats[key], G, ks, nb + 2, nl=nl, soc=soc, grad=True, vectors=True)
     assert not st.any()
     gscale = np.abs(ref["grad"]).max()  # physical gradient scale (eV m) over all k and bands
@@ -130,19 +138,22 @@ def test_fp64_vectors_and_gradients_match_oracle(gpu, oracle, mats, case, nb):
             Xo = ref["vecs"][q][grp].T
             Po = Xo @ Xo.conj().T
             assert np.abs(Pg - Po).max() <= PROJ_TOL, (case, k, grp)
-            # the kinetic gradient is well defined for non-degenerate bands, and for isolated
-            # Kramers pairs (it is the same for every vector of the pair)
-            if len(grp) == 1 or (soc and len(grp) == 2):
+            # the kinetic gradient is well defined for non-degenerate bands, and, with inversion
+            # symmetry (elemental Si/Ge), for isolated Kramers pairs (it is the same for every vector
+            # of the pair); zinc-blende pairs that touch at symmetry points have no such invariance
+            inversion = key in ("Si-CB", "Si-d", "Ge")
+            if len(grp) == 1 or (soc and inversion and len(grp) == 2):
                 np.testing.assert_allclose(g[q][grp], ref["grad"][q][grp], rtol=0, atol=1e-8 * gscale)
 
 
-@pytest.mark.parametrize("case,nb,nk", [("si_cb_local_137", 16, 60), ("si_d_nonlocal_137", 12, 30),
-                                        ("ge_nl_soc_181", 16, 8), ("gaas_nl_soc_89", 16, 12), ("alas_local_169", 16, 12)])
+@pytest.mark.parametrize("case,nb,nk", [("si_cb_local_137", 16, 60), ("si_cb_local_137_cx", 16, 60),
+                                        ("si_d_nonlocal_137", 12, 30), ("ge_nl_soc_181", 16, 8), ("gaas_nl_soc_89", 16, 12),
+                                        ("alas_local_169", 16, 12)])
 def test_mixed_precision_eigenvalues_within_1e6(gpu, oracle, mats, case, nb, nk):
-    key, shells, nl, soc = CASES[case]
+    key, shells, nl, soc, fcx = _case(case)
     G = oracle.generate_basis(shells)
     ks = _kset(oracle, 31, nk)
-    E, _, _, st = _ctx(mats[key], G, nl, soc, N.UEPM_PREC_MIXED).solve(ks, nb)
+    E, _, _, st = _ctx(mats[key], G, nl, soc, N.UEPM_PREC_MIXED, fcx).solve(ks, nb)
     Eo = oracle.band_structure(mats[key], G, ks, nb, nl=nl, soc=soc)["E"]
     assert not st.any()
     err = np.abs(E - Eo).max()
@@ -254,3 +265,22 @@ def test_soc_doubles_bands_like_the_reference(gpu, oracle, mats):
     Eo = oracle.band_structure(mats["Ge"], oracle.generate_basis(8), ks, 16, nl=True, soc=True)["E"]
     assert np.abs(E - Eo).max() <= EV_TOL
     np.testing.assert_allclose(E[:, 0::2], E[:, 1::2], atol=1e-9)  # Kramers pairs
+
+
+def test_real_kernels_are_chosen_exactly_when_h_is_real(gpu, oracle, mats):
+    G = oracle.generate_basis(8)
+    assert _ctx(mats["Si-CB"], G, False, False).real
+    assert _ctx(mats["Si-d"], G, True, False).real
+    assert not _ctx(mats["Si-CB"], G, False, True).real  # SOC blocks are complex
+    assert not _ctx(mats["GaAs"], G, False, False).real  # antisymmetric form factors
+    assert not _ctx(mats["InP"], G, True, False).real
+    assert not _ctx(mats["Si-CB"], G, False, False, force_complex=True).real
+
+
+def test_real_and_complex_kernels_agree(gpu, oracle, mats):
+    G = oracle.generate_basis(10)
+    ks = _kset(oracle, 17, 30)
+    for prec, tol in ((N.UEPM_PREC_FP64, 1e-11), (N.UEPM_PREC_MIXED, 1e-7)):
+        Er, _, gr, _ = _ctx(mats["Si-d"], G, True, False, prec).solve(ks, 12, gradient=True)
+        Ec, _, gc, _ = _ctx(mats["Si-d"], G, True, False, prec, True).solve(ks, 12, gradient=True)
+        assert np.abs(Er - Ec).max() <= tol

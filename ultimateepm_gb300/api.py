@@ -112,7 +112,8 @@ def generate_basis_vectors(shells: int) -> np.ndarray:
 class _Context:
     """One uepm_ctx: the material, basis and flags resident on the GPU."""
 
-    def __init__(self, material: Material, G: np.ndarray, nl: bool, soc: bool, precision: int = N.UEPM_PREC_FP64):
+    def __init__(self, material: Material, G: np.ndarray, nl: bool, soc: bool, precision: int = N.UEPM_PREC_FP64,
+                 force_complex: bool = False):
         L = N.load()
         self.G = np.ascontiguousarray(G, dtype=np.int32)
         flags = (N.UEPM_NONLOCAL if nl else 0) | (N.UEPM_SOC if soc else 0)
@@ -120,6 +121,7 @@ class _Context:
         _ok(L.uepm_ctx_create(C.byref(material.raw), _ip(self.G), self.G.shape[0], flags, C.byref(h)))
         self.h = h
         self.n = L.uepm_ctx_order(h)
+        self.real = bool(_ok(L.uepm_ctx_force_complex(h, int(force_complex))))
         self.set_precision(precision)
 
     def set_precision(self, precision: int):

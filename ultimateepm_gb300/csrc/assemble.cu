@@ -15,8 +15,10 @@
 //               quantities that depend on a single plane wave (spherical Bessel values at |K| R,
 //               gaussian-well exponentials, spin-orbit radial factors B(|K|)).
 //   k_assemble  one thread per lower-triangle element (i >= j) of the scalar N x N problem; writes
-//               the lower triangle of the n x n column-major H (n = 2N with SOC: UU, DD and the
-//               full DU block), optionally also an FP32 copy for the mixed-precision path.
+//               the element and its Hermitian mirror into the FULL n x n column-major H (n = 2N
+//               with SOC: [[UU, UD], [DU, DD]]), optionally also an FP32 copy for the mixed path.
+//               When H(k) is exactly real (no SOC, no antisymmetric form factors, identical
+//               anion/cation nonlocal parameters) only the real parts are stored.
 #include "uepm_common.cuh"
 #include "uepm_kernels.h"
 
@@ -217,10 +219,29 @@ __device__ void soc_element(const DevParams& P, const double* Ri, const double* 
     s[3] = mk((-cz) * phr - 0.0 * phi, (-cz) * phi + 0.0 * phr);
 }
 
-template <bool NL, bool SOC, bool F32>
+// Element writers: the real path stores only the real part (its imaginary part is exactly zero).
+__device__ __forceinline__ void put(double* p, cx<double> h) { *p = h.x; }
+__device__ __forceinline__ void put(cx<double>* p, cx<double> h) { *p = h; }
+__device__ __forceinline__ void put(float* p, cx<double> h) { *p = (float)h.x; }
+__device__ __forceinline__ void put(cx<float>* p, cx<double> h) { *p = mk((float)h.x, (float)h.y); }
+__device__ __forceinline__ cx<double> conjd(cx<double> a) { return mk(a.x, -a.y); }
+
+// Writes element (r, c) of the full matrix and, when r != c, its Hermitian mirror (c, r).
+template <typename SO, typename SF>
+__device__ __forceinline__ void put_pair(SO* Hb, SF* Fb, int ld, int r, int c, cx<double> h) {
+    put(Hb + (size_t)c * ld + r, h);
+    if (Fb) put(Fb + (size_t)c * ld + r, h);
+    if (r != c) {
+        put(Hb + (size_t)r * ld + c, conjd(h));
+        if (Fb) put(Fb + (size_t)r * ld + c, conjd(h));
+    }
+}
+
+template <bool NL, bool SOC, typename SO>
 __global__ void k_assemble(const DevParams P, const cx<double>* __restrict__ Vloc, const double2* __restrict__ phNL,
-                           const double2* __restrict__ phSO, const double* __restrict__ rows, cx<double>* __restrict__ H,
-                           int ld, size_t mstride, cx<float>* __restrict__ H32, size_t mstride32, int batch) {
+                           const double2* __restrict__ phSO, const double* __restrict__ rows, SO* __restrict__ H, int ld,
+                           size_t mstride, typename Lower<SO>::type* __restrict__ H32, size_t mstride32, int batch) {
+    using SF    = typename Lower<SO>::type;
     const int i = blockIdx.x * 32 + threadIdx.x;
     const int j = blockIdx.y * 8 + threadIdx.y;
     const int b = blockIdx.z;
@@ -236,47 +257,20 @@ __global__ void k_assemble(const DevParams P, const cx<double>* __restrict__ Vlo
         h.x                 = h.x + v.x;
         h.y                 = h.y + v.y;
     }
-    cx<double>* Hb = H + (size_t)b * mstride;
+    SO* Hb = H + (size_t)b * mstride;
+    SF* Fb = H32 ? H32 + (size_t)b * mstride32 : nullptr;
     if (!SOC) {
-        Hb[(size_t)j * ld + i] = h;
-        if (F32) H32[(size_t)b * mstride32 + (size_t)j * ld + i] = mk((float)h.x, (float)h.y);
+        put_pair(Hb, Fb, ld, i, j, h);
         return;
     }
+    // 2N x 2N: [[UU, UD], [DU, DD]] with UU = H + s00, DD = H + s11, DU = s10, UD = DU^H
     const double2 ph = phSO[(size_t)j * N + i];
     cx<double>    s[4];
     soc_element(P, Ri, Rj, ph.x, ph.y, s);
-    const cx<double> uu = mk(h.x + s[0].x, h.y + s[0].y);
-    const cx<double> dd = mk(h.x + s[3].x, h.y + s[3].y);
-    const cx<double> du = s[2];
-    const size_t     e_uu = (size_t)j * ld + i, e_dd = (size_t)(j + N) * ld + (i + N), e_du = (size_t)j * ld + (i + N);
-    Hb[e_uu] = uu;
-    Hb[e_dd] = dd;
-    Hb[e_du] = du;
-    cx<float>* H32b = F32 ? H32 + (size_t)b * mstride32 : nullptr;
-    if (F32) {
-        H32b[e_uu] = mk((float)uu.x, (float)uu.y);
-        H32b[e_dd] = mk((float)dd.x, (float)dd.y);
-        H32b[e_du] = mk((float)du.x, (float)du.y);
-    }
-    if (i > j) {
-        // DU(j, i) = conj(UD(i, j)) = conj(s01(i, j)): the lower triangle of the 2N matrix holds
-        // the whole DU block.
-        const cx<double> du2 = mk(s[1].x, -s[1].y);
-        const size_t     e2  = (size_t)i * ld + (j + N);
-        Hb[e2]               = du2;
-        if (F32) H32b[e2] = mk((float)du2.x, (float)du2.y);
-    }
-}
-
-// Fills the strict upper triangle with the conjugate of the lower one (debug/export path).
-__global__ void k_mirror_upper(cx<double>* __restrict__ H, int n, int ld, size_t mstride, int batch) {
-    const int i = blockIdx.x * 32 + threadIdx.x;
-    const int j = blockIdx.y * 8 + threadIdx.y;
-    const int b = blockIdx.z;
-    if (i >= n || j >= n || i <= j || b >= batch) return;
-    cx<double>*      Hb = H + (size_t)b * mstride;
-    const cx<double> a  = Hb[(size_t)j * ld + i];
-    Hb[(size_t)i * ld + j] = mk(a.x, -a.y);
+    put_pair(Hb, Fb, ld, i, j, mk(h.x + s[0].x, h.y + s[0].y));          // UU(i, j), UU(j, i)
+    put_pair(Hb, Fb, ld, i + N, j + N, mk(h.x + s[3].x, h.y + s[3].y));  // DD(i, j), DD(j, i)
+    put_pair(Hb, Fb, ld, i + N, j, s[2]);                                // DU(i, j), UD(j, i)
+    if (i > j) put_pair(Hb, Fb, ld, j + N, i, conjd(s[1]));             // DU(j, i) = conj(UD(i, j))
 }
 
 // ------------------------------------------------------------------------------------------------
@@ -286,29 +280,23 @@ void launch_rows(const DevParams& P, const double* d_k, const int* d_G, double* 
     count_launch();
 }
 
+template <typename SO>
 void launch_assemble(const DevParams& P, const cx<double>* Vloc, const double2* phNL, const double2* phSO, const double* rows,
-                     cx<double>* H, int ld, size_t mstride, cx<float>* H32, size_t mstride32, int batch, cudaStream_t s) {
+                     SO* H, int ld, size_t mstride, typename Lower<SO>::type* H32, size_t mstride32, int batch,
+                     cudaStream_t s) {
     dim3 blk(32, 8), grd((P.N + 31) / 32, (P.N + 7) / 8, batch);
-    const bool f32 = (H32 != nullptr);
-#define UEPM_ASM(NL_, SO_, F_) \
-    k_assemble<NL_, SO_, F_><<<grd, blk, 0, s>>>(P, Vloc, phNL, phSO, rows, H, ld, mstride, H32, mstride32, batch)
-    if (P.nl && P.soc) {
-        if (f32) UEPM_ASM(true, true, true); else UEPM_ASM(true, true, false);
-    } else if (P.nl) {
-        if (f32) UEPM_ASM(true, false, true); else UEPM_ASM(true, false, false);
-    } else if (P.soc) {
-        if (f32) UEPM_ASM(false, true, true); else UEPM_ASM(false, true, false);
-    } else {
-        if (f32) UEPM_ASM(false, false, true); else UEPM_ASM(false, false, false);
-    }
+#define UEPM_ASM(NL_, SO_) k_assemble<NL_, SO_, SO><<<grd, blk, 0, s>>>(P, Vloc, phNL, phSO, rows, H, ld, mstride, H32, mstride32, batch)
+    if (P.nl && P.soc) UEPM_ASM(true, true);
+    else if (P.nl) UEPM_ASM(true, false);
+    else if (P.soc) UEPM_ASM(false, true);
+    else UEPM_ASM(false, false);
 #undef UEPM_ASM
     count_launch();
 }
 
-void launch_mirror_upper(cx<double>* H, int n, int ld, size_t mstride, int batch, cudaStream_t s) {
-    dim3 blk(32, 8), grd((n + 31) / 32, (n + 7) / 8, batch);
-    k_mirror_upper<<<grd, blk, 0, s>>>(H, n, ld, mstride, batch);
-    count_launch();
-}
+template void launch_assemble<double>(const DevParams&, const cx<double>*, const double2*, const double2*, const double*,
+                                      double*, int, size_t, float*, size_t, int, cudaStream_t);
+template void launch_assemble<cx<double>>(const DevParams&, const cx<double>*, const double2*, const double2*, const double*,
+                                          cx<double>*, int, size_t, cx<float>*, size_t, int, cudaStream_t);
 
 }  // namespace uepm

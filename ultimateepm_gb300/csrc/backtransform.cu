@@ -4,57 +4,62 @@
 //
 // One CTA per matrix; each warp carries whole eigenvectors in registers (lane owns rows
 // r = lane + 32 t) through all n-1 reflectors, so warps never synchronise with each other.
-// Per reflector and vector: v^H z (4 FMA per row) and z -= (tau v^H z) v (4 FMA per row), i.e. the
-// 8 n^2 nb algorithmic flops of the back-transformation.
+// Per reflector and vector: v^H z and z -= (tau v^H z) v over the reflector's rows, i.e. the
+// 8 n^2 nb algorithmic flops of the back-transformation (2 n^2 nb for real symmetric matrices).
+// Output vectors are complex (the C ABI layout) whatever the arithmetic.
 #include "uepm_common.cuh"
 #include "uepm_kernels.h"
 
 namespace uepm {
 
-template <typename T, int NT, int MAXT>
-__global__ void __launch_bounds__(NT) k_backtransform(const cx<T>* __restrict__ H, int n, int ld, size_t mstride,
-                                                      const cx<T>* __restrict__ tq, const T* __restrict__ z, int nb,
-                                                      cx<T>* __restrict__ Xout, const DevParams P, const double* __restrict__ kpts,
-                                                      const int* __restrict__ G, double* __restrict__ grad, int batch) {
+template <typename S, int NT, int MAXT>
+__global__ void __launch_bounds__(NT) k_backtransform(const S* __restrict__ H, int n, int ld, size_t mstride,
+                                                      const S* __restrict__ tq, const typename ST<S>::R* __restrict__ z, int nb,
+                                                      cx<typename ST<S>::R>* __restrict__ Xout, const DevParams P,
+                                                      const double* __restrict__ kpts, const int* __restrict__ G,
+                                                      double* __restrict__ grad, int batch) {
+    using R          = typename ST<S>::R;
     constexpr int NW = NT / 32;
     const int     b  = blockIdx.x;
     if (b >= batch) return;
-    const int    lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const cx<T>* A    = H + (size_t)b * mstride;
-    const cx<T>* tb   = tq + (size_t)b * n;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const S*  A    = H + (size_t)b * mstride;
+    const S*  tb   = tq + (size_t)b * n;
     for (int j = warp; j < nb; j += NW) {
-        cx<T> zr[MAXT];
+        S zr[MAXT];
 #pragma unroll
         for (int t = 0; t < MAXT; ++t) {
             const int r = lane + 32 * t;
-            zr[t]       = mk<T>(r < n ? z[((size_t)b * nb + j) * n + r] : T(0), T(0));
+            zr[t]       = ST<S>::make(r < n ? z[((size_t)b * nb + j) * n + r] : R(0), R(0));
         }
         for (int i = n - 2; i >= 0; --i) {
-            const cx<T> tau = tb[i];
-            if (tau.x == T(0) && tau.y == T(0)) continue;
-            const cx<T>* vc = A + (size_t)i * ld;
-            cx<T>        vr[MAXT];
-            cx<T>        dot = mk<T>(0, 0);
+            const S tau = tb[i];
+            if (ST<S>::re(tau) == R(0) && ST<S>::im(tau) == R(0)) continue;
+            const S*  vc = A + (size_t)i * ld;
+            const int t0 = (i + 1) >> 5;  // first chunk holding a row > i (warp-uniform)
+            S         vr[MAXT];
+            S         dot = ST<S>::zero();
 #pragma unroll
             for (int t = 0; t < MAXT; ++t) {
-                const int r = lane + 32 * t;
-                vr[t]       = mk<T>(0, 0);
-                if (r > i && r < n) {
-                    vr[t] = (r == i + 1) ? mk<T>(1, 0) : ldc(vc + r);
-                    dot   = cfmac(vr[t], zr[t], dot);
+                vr[t] = ST<S>::zero();
+                if (t >= t0) {
+                    const int r = lane + 32 * t;
+                    if (r > i && r < n) vr[t] = (r == i + 1) ? ST<S>::one() : ldc(vc + r);
+                    dot = cfmac(vr[t], zr[t], dot);
                 }
             }
-            dot           = warp_sum(dot);
-            const cx<T> s = cmul(tau, dot);
+            dot         = warp_sum(dot);
+            const S sdt = ST<S>::neg(cmul(tau, dot));
 #pragma unroll
-            for (int t = 0; t < MAXT; ++t) zr[t] = cfma(mk<T>(-vr[t].x, -vr[t].y), s, zr[t]);
+            for (int t = 0; t < MAXT; ++t)
+                if (t >= t0) zr[t] = cfma(vr[t], sdt, zr[t]);
         }
         if (Xout) {
-            cx<T>* xo = Xout + ((size_t)b * nb + j) * n;
+            cx<R>* xo = Xout + ((size_t)b * nb + j) * n;
 #pragma unroll
             for (int t = 0; t < MAXT; ++t) {
                 const int r = lane + 32 * t;
-                if (r < n) stc(xo + r, zr[t]);
+                if (r < n) stc(xo + r, mk<R>(ST<S>::re(zr[t]), ST<S>::im(zr[t])));
             }
         }
         if (grad) {
@@ -65,7 +70,7 @@ __global__ void __launch_bounds__(NT) k_backtransform(const cx<T>* __restrict__ 
                 const int r = lane + 32 * t;
                 if (r < n) {
                     const int    bi = (r < P.N) ? r : r - P.N;
-                    const double w  = (double)zr[t].x * (double)zr[t].x + (double)zr[t].y * (double)zr[t].y;
+                    const double w  = (double)ST<S>::norm(zr[t]);
                     sx += (k[0] + G[3 * bi]) * w;
                     sy += (k[1] + G[3 * bi + 1]) * w;
                     sz += (k[2] + G[3 * bi + 2]) * w;
@@ -84,30 +89,33 @@ __global__ void __launch_bounds__(NT) k_backtransform(const cx<T>* __restrict__ 
     }
 }
 
-template <typename T, int MAXT>
-static void bt_launch(const cx<T>* H, int n, int ld, size_t mstride, const cx<T>* tq, const T* z, int nb, cx<T>* Xout,
-                      const DevParams& P, const double* d_k, const int* d_G, double* grad, int batch, cudaStream_t s) {
+template <typename S, int MAXT>
+static void bt_launch(const S* H, int n, int ld, size_t mstride, const S* tq, const typename ST<S>::R* z, int nb,
+                      cx<typename ST<S>::R>* Xout, const DevParams& P, const double* d_k, const int* d_G, double* grad,
+                      int batch, cudaStream_t s) {
     constexpr int NT = 256;
-    k_backtransform<T, NT, MAXT><<<batch, NT, 0, s>>>(H, n, ld, mstride, tq, z, nb, Xout, P, d_k, d_G, grad, batch);
+    k_backtransform<S, NT, MAXT><<<batch, NT, 0, s>>>(H, n, ld, mstride, tq, z, nb, Xout, P, d_k, d_G, grad, batch);
     count_launch();
 }
 
-template <typename T>
-void launch_backtransform(const cx<T>* H, int n, int ld, size_t mstride, const cx<T>* tq, const T* z, int nb, cx<T>* Xout,
-                          const DevParams& P, const double* d_k, const int* d_G, double* grad, const T*, double*, int batch,
-                          cudaStream_t s) {
-    if (n <= 128) bt_launch<T, 4>(H, n, ld, mstride, tq, z, nb, Xout, P, d_k, d_G, grad, batch, s);
-    else if (n <= 160) bt_launch<T, 5>(H, n, ld, mstride, tq, z, nb, Xout, P, d_k, d_G, grad, batch, s);
-    else if (n <= 256) bt_launch<T, 8>(H, n, ld, mstride, tq, z, nb, Xout, P, d_k, d_G, grad, batch, s);
-    else if (n <= 384) bt_launch<T, 12>(H, n, ld, mstride, tq, z, nb, Xout, P, d_k, d_G, grad, batch, s);
-    else bt_launch<T, 16>(H, n, ld, mstride, tq, z, nb, Xout, P, d_k, d_G, grad, batch, s);
+template <typename S>
+void launch_backtransform(const S* H, int n, int ld, size_t mstride, const S* tq, const typename ST<S>::R* z, int nb,
+                          cx<typename ST<S>::R>* Xout, const DevParams& P, const double* d_k, const int* d_G, double* grad,
+                          int batch, cudaStream_t s) {
+    if (n <= 128) bt_launch<S, 4>(H, n, ld, mstride, tq, z, nb, Xout, P, d_k, d_G, grad, batch, s);
+    else if (n <= 160) bt_launch<S, 5>(H, n, ld, mstride, tq, z, nb, Xout, P, d_k, d_G, grad, batch, s);
+    else if (n <= 256) bt_launch<S, 8>(H, n, ld, mstride, tq, z, nb, Xout, P, d_k, d_G, grad, batch, s);
+    else if (n <= 384) bt_launch<S, 12>(H, n, ld, mstride, tq, z, nb, Xout, P, d_k, d_G, grad, batch, s);
+    else bt_launch<S, 16>(H, n, ld, mstride, tq, z, nb, Xout, P, d_k, d_G, grad, batch, s);
 }
 
-template void launch_backtransform<double>(const cx<double>*, int, int, size_t, const cx<double>*, const double*, int,
-                                           cx<double>*, const DevParams&, const double*, const int*, double*, const double*,
-                                           double*, int, cudaStream_t);
-template void launch_backtransform<float>(const cx<float>*, int, int, size_t, const cx<float>*, const float*, int, cx<float>*,
-                                          const DevParams&, const double*, const int*, double*, const float*, double*, int,
-                                          cudaStream_t);
+#define UEPM_BT_INST(S)                                                                                          \
+    template void launch_backtransform<S>(const S*, int, int, size_t, const S*, const ST<S>::R*, int, cx<ST<S>::R>*, \
+                                          const DevParams&, const double*, const int*, double*, int, cudaStream_t);
+UEPM_BT_INST(double)
+UEPM_BT_INST(float)
+UEPM_BT_INST(cx<double>)
+UEPM_BT_INST(cx<float>)
+#undef UEPM_BT_INST
 
 }  // namespace uepm

@@ -53,6 +53,9 @@ struct uepm_ctx {
     int           N = 0, n = 0;
     uint32_t      flags     = 0;
     int           precision = UEPM_PREC_FP64;
+    bool          real_h    = false;  // H(k) is exactly real for this material and flags
+    bool          force_cx  = false;  // run the complex kernels even when H(k) is real
+    bool          real      = false;  // real_h && !force_cx
     size_t        ws_limit  = (size_t)8 << 30;
     int*          d_G       = nullptr;
     cx<double>*   d_Vloc    = nullptr;
@@ -79,9 +82,20 @@ struct uepm_ctx {
 
 namespace {
 
-enum KernelKind { KK_ROWS = 0, KK_ASSEMBLE, KK_TRIDIAG64, KK_TRIDIAG32, KK_BISECT, KK_INVIT, KK_BACKTRANSFORM, KK_REFINE };
-const char* kKernelNames[UEPM_KERNEL_KINDS] = {"rows", "assemble", "tridiag_fp64", "tridiag_fp32",
-                                               "bisect", "invit", "backtransform", "refine"};
+enum KernelKind {
+    KK_ROWS = 0,
+    KK_ASSEMBLE,
+    KK_TRIDIAG64,
+    KK_TRIDIAG32,
+    KK_BISECT,
+    KK_INVIT,
+    KK_BACKTRANSFORM,
+    KK_REFINE_PROJECT,
+    KK_SMALL_EIGH,
+    KK_REFINE_VECTORS
+};
+const char* kKernelNames[UEPM_KERNEL_KINDS] = {"rows",   "assemble",      "tridiag_fp64",   "tridiag_fp32", "bisect",
+                                               "invit",  "backtransform", "refine_project", "small_eigh",   "refine_vectors"};
 
 cudaEvent_t take_event(uepm_ctx* ctx) {
     if (!ctx->pool.empty()) {
@@ -148,7 +162,7 @@ void pp_value(const uepm_material& m, int gx, int gy, int gz, double tau, double
 size_t align_up(size_t x) { return (x + 255) & ~(size_t)255; }
 
 struct Layout {
-    size_t rows, H, H32, d, e, tq, ev, work, z, X32, refine, total;
+    size_t rows, H, H32, d, e, tq, ev, work, z, X32, refine, small, total;
 };
 
 // Bytes of workspace one chunk of `c` matrices needs, with the offset of every region.
@@ -157,7 +171,9 @@ Layout plan(const uepm_ctx* ctx, int nb, uint32_t want, size_t c) {
     const bool   mixed = ctx->precision == UEPM_PREC_MIXED;
     const bool   vecs  = (want & (UEPM_WANT_VECTORS | UEPM_WANT_GRADIENT)) != 0;
     const size_t m     = mixed ? std::min<size_t>(n, (size_t)nb + kGuardBands) : (size_t)nb;
-    const size_t rs    = mixed ? sizeof(float) : sizeof(double);
+    const size_t es    = ctx->real ? sizeof(double) : sizeof(cx<double>);  // FP64 matrix scalar
+    const size_t es32  = ctx->real ? sizeof(float) : sizeof(cx<float>);   // FP32 matrix scalar
+    const size_t rs    = mixed ? sizeof(float) : sizeof(double);           // real type of the reduction
     Layout       L{};
     size_t       off = 0;
     auto         take = [&](size_t bytes) {
@@ -166,19 +182,20 @@ Layout plan(const uepm_ctx* ctx, int nb, uint32_t want, size_t c) {
         return o;
     };
     L.rows = take(c * N * ROW_STRIDE * sizeof(double));
-    L.H    = take(c * n * n * sizeof(cx<double>));
-    L.H32  = mixed ? take(c * n * n * sizeof(cx<float>)) : 0;
+    L.H    = take(c * n * n * es);
+    L.H32  = mixed ? take(c * n * n * es32) : 0;
     L.d    = take(c * n * rs);
     L.e    = take(c * n * rs);
-    L.tq   = take(c * n * 2 * rs);
+    L.tq   = take(c * n * (mixed ? es32 : es));
     L.ev   = mixed ? take(c * m * rs) : 0;
     if (mixed || vecs) {
-        L.work = take(c * (mixed ? invit_work_elems<float>((int)n) : invit_work_elems<double>((int)n)) * rs);
+        L.work = take(c * invit_work_elems<double>((int)n) * rs);
         L.z    = take(c * m * n * rs);
     }
     if (mixed) {
         L.X32    = take(c * m * n * sizeof(cx<float>));
-        L.refine = take(c * refine_work_elems((int)n, (int)m) * sizeof(cx<double>));
+        L.refine = take(c * refine_work_elems((int)n, (int)m) * es);
+        L.small  = take(c * refine_small_elems((int)m, nb) * es);
     }
     L.total = off;
     return L;
@@ -205,6 +222,94 @@ int check_launch() {
         return UEPM_ERR_CUDA;
     }
     return UEPM_OK;
+}
+
+
+// One chunk of c k-points through the pipeline, FP64 (S = double for real H, cx<double> otherwise)
+// or mixed precision (FP32 reduction in Lower<S>, FP64 Rayleigh-Ritz in S).
+template <typename S>
+void run_chunk(uepm_ctx* ctx, const Layout& L, char* ws, const double* kk, int c, int nb, int m, bool vec, double* E,
+               cx<double>* Xo, double* gr, int* st, cudaStream_t s) {
+    using S32            = typename Lower<S>::type;
+    const int    n       = ctx->n;
+    const size_t mstride = (size_t)n * n;
+    auto*        rows    = reinterpret_cast<double*>(ws + L.rows);
+    auto*        H       = reinterpret_cast<S*>(ws + L.H);
+    {
+        ProfScope p(ctx, s, KK_ROWS);
+        launch_rows(ctx->P, kk, ctx->d_G, rows, c, s);
+    }
+    if (ctx->precision != UEPM_PREC_MIXED) {
+        {
+            ProfScope p(ctx, s, KK_ASSEMBLE);
+            launch_assemble<S>(ctx->P, ctx->d_Vloc, ctx->d_phNL, ctx->d_phSO, rows, H, n, mstride, nullptr, 0, c, s);
+        }
+        auto* d  = reinterpret_cast<double*>(ws + L.d);
+        auto* e  = reinterpret_cast<double*>(ws + L.e);
+        auto* tq = reinterpret_cast<S*>(ws + L.tq);
+        {
+            ProfScope p(ctx, s, KK_TRIDIAG64);
+            launch_tridiag<S>(H, n, n, mstride, d, e, tq, st, c, s);
+        }
+        {
+            ProfScope p(ctx, s, KK_BISECT);
+            launch_bisect<double>(d, e, n, nb, E, nb, c, s);
+        }
+        if (vec) {
+            auto* work = reinterpret_cast<double*>(ws + L.work);
+            auto* z    = reinterpret_cast<double*>(ws + L.z);
+            {
+                ProfScope p(ctx, s, KK_INVIT);
+                launch_invit<double>(d, e, E, nb, n, nb, work, z, st, c, s);
+            }
+            ProfScope p(ctx, s, KK_BACKTRANSFORM);
+            launch_backtransform<S>(H, n, n, mstride, tq, z, nb, Xo, ctx->P, kk, ctx->d_G, gr, c, s);
+        }
+        return;
+    }
+    auto* H32 = reinterpret_cast<S32*>(ws + L.H32);
+    {
+        ProfScope p(ctx, s, KK_ASSEMBLE);
+        launch_assemble<S>(ctx->P, ctx->d_Vloc, ctx->d_phNL, ctx->d_phSO, rows, H, n, mstride, H32, mstride, c, s);
+    }
+    auto* d     = reinterpret_cast<float*>(ws + L.d);
+    auto* e     = reinterpret_cast<float*>(ws + L.e);
+    auto* tq    = reinterpret_cast<S32*>(ws + L.tq);
+    auto* ev    = reinterpret_cast<float*>(ws + L.ev);
+    auto* work  = reinterpret_cast<float*>(ws + L.work);
+    auto* z     = reinterpret_cast<float*>(ws + L.z);
+    auto* X32   = reinterpret_cast<cx<float>*>(ws + L.X32);
+    auto* rw    = reinterpret_cast<S*>(ws + L.refine);
+    auto* small = reinterpret_cast<S*>(ws + L.small);
+    {
+        ProfScope p(ctx, s, KK_TRIDIAG32);
+        launch_tridiag<S32>(H32, n, n, mstride, d, e, tq, st, c, s);
+    }
+    {
+        ProfScope p(ctx, s, KK_BISECT);
+        launch_bisect<float>(d, e, n, m, ev, m, c, s);
+    }
+    {
+        ProfScope p(ctx, s, KK_INVIT);
+        launch_invit<float>(d, e, ev, m, n, m, work, z, st, c, s);
+    }
+    {
+        ProfScope p(ctx, s, KK_BACKTRANSFORM);
+        launch_backtransform<S32>(H32, n, n, mstride, tq, z, m, X32, ctx->P, kk, ctx->d_G, nullptr, c, s);
+    }
+    {
+        ProfScope p(ctx, s, KK_REFINE_PROJECT);
+        launch_refine_project<S>(H, n, n, mstride, X32, m, rw, small, c, s);
+    }
+    S* W = small + (size_t)4 * m * m * c;
+    {
+        ProfScope p(ctx, s, KK_SMALL_EIGH);
+        launch_small_eigh<S>(small, m, nb, E, vec ? W : nullptr, st, c, s);
+    }
+    if (vec) {
+        ProfScope p(ctx, s, KK_REFINE_VECTORS);
+        launch_refine_vectors<S>(n, m, nb, rw, W, Xo, gr, ctx->P, kk, ctx->d_G, c, s);
+    }
 }
 
 }  // namespace
@@ -240,6 +345,14 @@ int uepm_ctx_create(const uepm_material* mat, const int32_t* G, int N, uint32_t 
     ctx->n     = n;
     ctx->flags = flags;
     ctx->G.assign(G, G + 3 * (size_t)N);
+    // H(k) is exactly real when nothing contributes an imaginary part: no spin-orbit blocks, no
+    // antisymmetric local form factors (VA * sin = 0), and a nonlocal term whose antisymmetric part
+    // (V_anion - V_cation) / 2 vanishes identically because both atoms carry the same parameters.
+    const bool same_nl = !nl || (mat->alpha0_anion == mat->alpha0_cation && mat->beta0_anion == mat->beta0_cation &&
+                                 mat->A2_anion == mat->A2_cation && mat->R0_anion == mat->R0_cation &&
+                                 mat->R2_anion == mat->R2_cation);
+    ctx->real_h = !soc && mat->V3A == 0.0 && mat->V4A == 0.0 && mat->V8A == 0.0 && mat->V11A == 0.0 && same_nl;
+    ctx->real   = ctx->real_h;
     cudaGetDevice(&ctx->device);
 
     // Derived constants, each with the reference's own expression.
@@ -374,6 +487,13 @@ int uepm_ctx_set_precision(uepm_ctx* ctx, int precision) {
 
 int uepm_ctx_order(const uepm_ctx* ctx) { return ctx ? ctx->n : UEPM_ERR_INVALID; }
 
+int uepm_ctx_force_complex(uepm_ctx* ctx, int on) {
+    if (!ctx) return UEPM_ERR_INVALID;
+    ctx->force_cx = on != 0;
+    ctx->real     = ctx->real_h && !ctx->force_cx;
+    return ctx->real ? 1 : 0;
+}
+
 int uepm_ctx_set_workspace_limit(uepm_ctx* ctx, size_t bytes) {
     if (!ctx || bytes == 0) return UEPM_ERR_INVALID;
     ctx->ws_limit = bytes;
@@ -418,83 +538,17 @@ int uepm_solve_device(uepm_ctx* ctx, const double* d_k, size_t nk, int nb, uint3
     char* ws = static_cast<char*>(ctx->d_ws);
     if (d_status) UEPM_CUDA(cudaMemsetAsync(d_status, 0, sizeof(int32_t) * nk, s));
 
-    const bool   want_vec  = (want & UEPM_WANT_VECTORS) != 0;
-    const bool   want_grad = (want & UEPM_WANT_GRADIENT) != 0;
-    const size_t mstride   = (size_t)n * n;
+    const bool want_vec  = (want & UEPM_WANT_VECTORS) != 0;
+    const bool want_grad = (want & UEPM_WANT_GRADIENT) != 0;
     for (size_t off = 0; off < nk; off += chunk) {
-        const int     c    = (int)std::min(chunk, nk - off);
-        const double* kk   = d_k + 3 * off;
-        int*          st   = d_status ? d_status + off : nullptr;
-        double*       E    = d_E + off * nb;
-        auto*         rows = reinterpret_cast<double*>(ws + L.rows);
-        auto*         H    = reinterpret_cast<cx<double>*>(ws + L.H);
-        cx<double>*   Xo   = want_vec ? reinterpret_cast<cx<double>*>(d_X) + off * nb * n : nullptr;
-        double*       gr   = want_grad ? d_grad + off * nb * 3 : nullptr;
-        {
-            ProfScope p(ctx, s, KK_ROWS);
-            launch_rows(ctx->P, kk, ctx->d_G, rows, c, s);
-        }
-        if (!mixed) {
-            {
-                ProfScope p(ctx, s, KK_ASSEMBLE);
-                launch_assemble(ctx->P, ctx->d_Vloc, ctx->d_phNL, ctx->d_phSO, rows, H, n, mstride, nullptr, 0, c, s);
-            }
-            auto* d  = reinterpret_cast<double*>(ws + L.d);
-            auto* e  = reinterpret_cast<double*>(ws + L.e);
-            auto* tq = reinterpret_cast<cx<double>*>(ws + L.tq);
-            {
-                ProfScope p(ctx, s, KK_TRIDIAG64);
-                launch_tridiag<double>(H, n, n, mstride, d, e, tq, st, c, s);
-            }
-            {
-                ProfScope p(ctx, s, KK_BISECT);
-                launch_bisect<double>(d, e, n, nb, E, nb, c, s);
-            }
-            if (want_vec || want_grad) {
-                auto* work = reinterpret_cast<double*>(ws + L.work);
-                auto* z    = reinterpret_cast<double*>(ws + L.z);
-                {
-                    ProfScope p(ctx, s, KK_INVIT);
-                    launch_invit<double>(d, e, E, nb, n, nb, work, z, st, c, s);
-                }
-                ProfScope p(ctx, s, KK_BACKTRANSFORM);
-                launch_backtransform<double>(H, n, n, mstride, tq, z, nb, Xo, ctx->P, kk, ctx->d_G, gr, nullptr, nullptr, c, s);
-            }
-        } else {
-            auto* H32 = reinterpret_cast<cx<float>*>(ws + L.H32);
-            {
-                ProfScope p(ctx, s, KK_ASSEMBLE);
-                launch_assemble(ctx->P, ctx->d_Vloc, ctx->d_phNL, ctx->d_phSO, rows, H, n, mstride, H32, mstride, c, s);
-            }
-            auto* d    = reinterpret_cast<float*>(ws + L.d);
-            auto* e    = reinterpret_cast<float*>(ws + L.e);
-            auto* tq   = reinterpret_cast<cx<float>*>(ws + L.tq);
-            auto* ev   = reinterpret_cast<float*>(ws + L.ev);
-            auto* work = reinterpret_cast<float*>(ws + L.work);
-            auto* z    = reinterpret_cast<float*>(ws + L.z);
-            auto* X32  = reinterpret_cast<cx<float>*>(ws + L.X32);
-            auto* rw   = reinterpret_cast<cx<double>*>(ws + L.refine);
-            {
-                ProfScope p(ctx, s, KK_TRIDIAG32);
-                launch_tridiag<float>(H32, n, n, mstride, d, e, tq, st, c, s);
-            }
-            {
-                ProfScope p(ctx, s, KK_BISECT);
-                launch_bisect<float>(d, e, n, m, ev, m, c, s);
-            }
-            {
-                ProfScope p(ctx, s, KK_INVIT);
-                launch_invit<float>(d, e, ev, m, n, m, work, z, st, c, s);
-            }
-            {
-                ProfScope p(ctx, s, KK_BACKTRANSFORM);
-                launch_backtransform<float>(H32, n, n, mstride, tq, z, m, X32, ctx->P, kk, ctx->d_G, nullptr, nullptr, nullptr, c, s);
-            }
-            {
-                ProfScope p(ctx, s, KK_REFINE);
-                launch_refine(H, n, n, mstride, X32, m, nb, E, Xo, gr, ctx->P, kk, ctx->d_G, rw, st, c, s);
-            }
-        }
+        const int     c  = (int)std::min(chunk, nk - off);
+        const double* kk = d_k + 3 * off;
+        int*          st = d_status ? d_status + off : nullptr;
+        double*       E  = d_E + off * nb;
+        cx<double>*   Xo = want_vec ? reinterpret_cast<cx<double>*>(d_X) + off * nb * n : nullptr;
+        double*       gr = want_grad ? d_grad + off * nb * 3 : nullptr;
+        if (ctx->real) run_chunk<double>(ctx, L, ws, kk, c, nb, m, want_vec || want_grad, E, Xo, gr, st, s);
+        else run_chunk<cx<double>>(ctx, L, ws, kk, c, nb, m, want_vec || want_grad, E, Xo, gr, st, s);
         if ((rc = check_launch())) return rc;
     }
     return UEPM_OK;
@@ -513,14 +567,12 @@ int uepm_assemble_device(uepm_ctx* ctx, const double* d_k, size_t nk, double* d_
     int          rc    = ensure_ws(ctx, align_up(chunk * per));
     if (rc) return rc;
     const size_t mstride = (size_t)n * n;
-    UEPM_CUDA(cudaMemsetAsync(d_H, 0, sizeof(cx<double>) * mstride * nk, s));
     for (size_t off = 0; off < nk; off += chunk) {
         const int c    = (int)std::min(chunk, nk - off);
         auto*     rows = reinterpret_cast<double*>(ctx->d_ws);
         auto*     H    = reinterpret_cast<cx<double>*>(d_H) + off * mstride;
         launch_rows(ctx->P, d_k + 3 * off, ctx->d_G, rows, c, s);
-        launch_assemble(ctx->P, ctx->d_Vloc, ctx->d_phNL, ctx->d_phSO, rows, H, n, mstride, nullptr, 0, c, s);
-        launch_mirror_upper(H, n, n, mstride, c, s);
+        launch_assemble<cx<double>>(ctx->P, ctx->d_Vloc, ctx->d_phNL, ctx->d_phSO, rows, H, n, mstride, nullptr, 0, c, s);
         if ((rc = check_launch())) return rc;
     }
     return UEPM_OK;

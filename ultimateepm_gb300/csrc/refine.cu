@@ -3,245 +3,240 @@
 // No reference counterpart: the reference only has the FP64 Eigen solve. Given FP32 approximations
 // X (n x m, m = nb + guard bands) to the lowest eigenvectors of the FP64 Hermitian H, this computes
 // in FP64
-//   Y = H X,  S = X^H X,  A = X^H Y,
-// solves the m x m pencil A c = lambda S c (Cholesky S = L L^H, C = L^-1 A L^-H, cyclic complex
-// Jacobi on C), and returns the nb lowest Ritz values (and, on request, the Ritz vectors X L^-H V and
-// their Hellmann-Feynman gradients). Ritz values err by about ||H x - lambda x||^2 / gap, where the
-// gap is to the first eigenvalue outside the subspace; the guard bands keep that gap open.
+//   k_refine_project   Y = H X, S = X^H X, A = X^H Y            (one CTA per matrix)
+//   k_small_eigh       the m x m pencil A c = lambda S c: Cholesky S = L L^H, C = L^-1 A L^-H,
+//                      cyclic Jacobi on C, ascending sort, W = L^-H V   (one THREAD per matrix:
+//                      GB300's FP64 pipe costs the same per warp instruction whatever the lane mask,
+//                      so the small dense solve runs 32 matrices per warp instead of one matrix per
+//                      warp)
+//   k_refine_vectors   Ritz vectors X W and their Hellmann-Feynman gradients (on request)
+// Ritz values err by about ||H x - lambda x||^2 / gap, where the gap is to the first eigenvalue
+// outside the subspace; the guard bands keep that gap open.
 //
-// One CTA per matrix. FP64 work per matrix: 4 n^2 m FMA for Y, 4 n m(m+1) for S and A, O(m^3) for the
-// small solve (one warp), 4 n m nb for the refined vectors.
+// FP64 work per matrix (complex): 4 n^2 m FMA for Y, 4 n m(m+1) for S and A, O(m^3) for the small
+// solve, 4 n m nb for the refined vectors. Real symmetric matrices need a quarter of that.
 #include "uepm_common.cuh"
 #include "uepm_kernels.h"
 
 namespace uepm {
 
-constexpr int kRefineNT  = 256;
-constexpr int kRefineMax = 40;  // largest subspace (nb + guard) handled by the warp solver
+constexpr int kProjNT = 256;
 
-__device__ __forceinline__ cx<double> cconj(cx<double> a) { return mk(a.x, -a.y); }
+// interleaved small-matrix storage: element e of matrix b at base[e * batch + b]
+#define SM(base, e) (base)[(size_t)(e) * batch + b]
 
-__global__ void __launch_bounds__(kRefineNT) k_refine(const cx<double>* __restrict__ H, int n, int ld, size_t mstride,
-                                                      const cx<float>* __restrict__ X32, int m, int nb,
-                                                      double* __restrict__ Eout, cx<double>* __restrict__ Xout,
-                                                      double* __restrict__ grad, const DevParams P, const double* __restrict__ kpts,
-                                                      const int* __restrict__ G, cx<double>* __restrict__ work,
-                                                      int* __restrict__ status, int batch) {
+template <typename S>
+__global__ void __launch_bounds__(kProjNT) k_refine_project(const S* __restrict__ H, int n, int ld, size_t mstride,
+                                                            const cx<float>* __restrict__ X32, int m, S* __restrict__ work,
+                                                            S* __restrict__ small, int batch) {
     const int b = blockIdx.x;
     if (b >= batch) return;
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const cx<double>* A  = H + (size_t)b * mstride;
-    cx<double>*       X  = work + (size_t)b * refine_work_elems(n, m);  // [r][j]
-    cx<double>*       Y  = X + (size_t)n * m;                             // [r][j]
-    extern __shared__ __align__(16) unsigned char smraw[];
-    const int   mp = m + 1;  // padded row length of the m x m scratch matrices
-    cx<double>* sSb = reinterpret_cast<cx<double>*>(smraw);
-    cx<double>* sAb = sSb + (size_t)m * mp;
-    cx<double>* sVb = sAb + (size_t)m * mp;
-    double*     sE  = reinterpret_cast<double*>(sVb + (size_t)m * mp);
-    int*        sOrd = reinterpret_cast<int*>(sE + kRefineMax);
-    __shared__ int sBad;
-#define sS(i, j) sSb[(size_t)(i) * mp + (j)]
-#define sA(i, j) sAb[(size_t)(i) * mp + (j)]
-#define sV(i, j) sVb[(size_t)(i) * mp + (j)]
-    if (tid == 0) sBad = 0;
-
-    // X (FP32, [j][r]) -> FP64, [r][j]
-    for (int q = tid; q < n * m; q += kRefineNT) {
+    const int tid = threadIdx.x;
+    const S*  A   = H + (size_t)b * mstride;
+    S*        X   = work + (size_t)b * refine_work_elems(n, m);  // [r][j]
+    S*        Y   = X + (size_t)n * m;                             // [r][j]
+    for (int q = tid; q < n * m; q += kProjNT) {
         const int       j = q / n, r = q - j * n;
         const cx<float> x = X32[((size_t)b * m + j) * n + r];
-        X[(size_t)r * m + j] = mk((double)x.x, (double)x.y);
+        X[(size_t)r * m + j] = ST<S>::make((double)x.x, (double)x.y);
     }
     __syncthreads();
-
-    // Y = H X, H Hermitian from its lower triangle; item = (4-vector block, row r)
+    // Y = H X (H in full storage): item = (block of 4 vectors, row r); H(r, c) coalesced over r
     const int nblk = (m + 3) / 4;
-    for (int item = tid; item < nblk * n; item += kRefineNT) {
-        const int  jb = item / n, r = item - jb * n;
-        const int  j0 = jb * 4;
-        cx<double> acc[4];
+    for (int item = tid; item < nblk * n; item += kProjNT) {
+        const int jb = item / n, r = item - jb * n;
+        const int j0 = jb * 4;
+        S         acc[4];
 #pragma unroll
-        for (int q = 0; q < 4; ++q) acc[q] = mk(0.0, 0.0);
-        for (int c = 0; c < n; ++c) {
-            const cx<double>  h  = (c <= r) ? ldc(A + (size_t)c * ld + r) : cconj(ldc(A + (size_t)r * ld + c));
-            const cx<double>* xr = X + (size_t)c * m + j0;
+        for (int q = 0; q < 4; ++q) acc[q] = ST<S>::zero();
+        if (j0 + 4 <= m) {
+            for (int c = 0; c < n; ++c) {
+                const S  h  = ldc(A + (size_t)c * ld + r);
+                const S* xr = X + (size_t)c * m + j0;
 #pragma unroll
-            for (int q = 0; q < 4; ++q)
-                if (j0 + q < m) acc[q] = cfma(h, xr[q], acc[q]);
+                for (int q = 0; q < 4; ++q) acc[q] = cfma(h, xr[q], acc[q]);
+            }
+        } else {
+            for (int c = 0; c < n; ++c) {
+                const S  h  = ldc(A + (size_t)c * ld + r);
+                const S* xr = X + (size_t)c * m + j0;
+                for (int q = 0; q < m - j0; ++q) acc[q] = cfma(h, xr[q], acc[q]);
+            }
         }
-#pragma unroll
-        for (int q = 0; q < 4; ++q)
-            if (j0 + q < m) Y[(size_t)r * m + j0 + q] = acc[q];
+        for (int q = 0; q < 4 && j0 + q < m; ++q) Y[(size_t)r * m + j0 + q] = acc[q];
     }
     __syncthreads();
-
-    // S = X^H X and A = X^H Y (upper triangles, p <= q), one (p, q) per thread
-    for (int pq = tid; pq < m * m; pq += kRefineNT) {
-        const int p = pq / m, q = pq - p * m;
-        if (p > q) continue;
-        cx<double> s = mk(0.0, 0.0), a = mk(0.0, 0.0);
+    // S = X^H X and A = X^H Y, upper triangles (p <= q) only
+    S*        Sg = small;
+    S*        Ag = small + (size_t)m * m * batch;
+    const int np = m * (m + 1) / 2;
+    for (int k = tid; k < np; k += kProjNT) {
+        int p = 0, rest = k;
+        while (rest >= m - p) {
+            rest -= m - p;
+            ++p;
+        }
+        const int q = p + rest;
+        S         s = ST<S>::zero(), a = ST<S>::zero();
         for (int r = 0; r < n; ++r) {
-            const cx<double> xp = X[(size_t)r * m + p];
-            s                   = cfmac(xp, X[(size_t)r * m + q], s);
-            a                   = cfmac(xp, Y[(size_t)r * m + q], a);
+            const S xp = X[(size_t)r * m + p];
+            s          = cfmac(xp, X[(size_t)r * m + q], s);
+            a          = cfmac(xp, Y[(size_t)r * m + q], a);
         }
-        sS(p, q) = s;
-        sA(p, q) = a;
-        sS(q, p) = cconj(s);
-        sA(q, p) = cconj(a);
+        SM(Sg, p * m + q) = s;
+        SM(Ag, p * m + q) = a;
+        SM(Sg, q * m + p) = ST<S>::conj(s);
+        SM(Ag, q * m + p) = ST<S>::conj(a);
     }
-    __syncthreads();
+}
 
-    if (warp == 0) {
-        // Cholesky S = L L^H, L stored in the lower triangle of sS (lanes over rows).
-        for (int k = 0; k < m; ++k) {
-            double dkk = sS(k, k).x;
-            for (int j = 0; j < k; ++j) dkk -= sS(k, j).x * sS(k, j).x + sS(k, j).y * sS(k, j).y;
-            if (!(dkk > 0.0)) {
-                if (lane == 0) sBad = 1;
-                dkk = 1.0;
-            }
-            const double lkk = sqrt(dkk);
-            __syncwarp();
-            for (int i = k + 1 + lane; i < m; i += 32) {
-                cx<double> s = sS(i, k);
-                for (int j = 0; j < k; ++j) s = cfms_conjb(sS(i, j), sS(k, j), s);
-                sS(i, k) = cscale(s, 1.0 / lkk);
-            }
-            __syncwarp();
-            if (lane == 0) sS(k, k) = mk(lkk, 0.0);
-            __syncwarp();
+// One thread per matrix. small = [S | A | M | C] (m x m each, interleaved), W = m x nb (interleaved).
+template <typename S>
+__global__ void k_small_eigh(S* __restrict__ small, int m, int nb, double* __restrict__ Eout, S* __restrict__ Wout,
+                             int* __restrict__ status, int batch) {
+    using R     = double;
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= batch) return;
+    S*   Sg  = small;                              // S, then L (lower)
+    S*   Ag  = small + (size_t)m * m * batch;      // A, then the Jacobi matrix C
+    S*   Mg  = small + (size_t)2 * m * m * batch;  // M = L^-1 A, then V
+    S*   Cg  = small + (size_t)3 * m * m * batch;  // C before symmetrisation
+    bool bad = false;
+    // Cholesky S = L L^H
+    for (int k = 0; k < m; ++k) {
+        R dkk = ST<S>::re(SM(Sg, k * m + k));
+        for (int j = 0; j < k; ++j) dkk -= ST<S>::norm(SM(Sg, k * m + j));
+        if (!(dkk > 0.0)) {
+            bad = true;
+            dkk = 1.0;
         }
-        // M = L^-1 A (column c per lane), stored in sV
-        for (int c = lane; c < m; c += 32)
-            for (int i = 0; i < m; ++i) {
-                cx<double> s = sA(i, c);
-                for (int j = 0; j < i; ++j) s = csub(s, cmul(sS(i, j), sV(j, c)));
-                sV(i, c) = cscale(s, 1.0 / sS(i, i).x);
-            }
-        __syncwarp();
-        // C = L^-1 M^H (C is Hermitian), stored in sA
-        for (int c = lane; c < m; c += 32)
-            for (int i = 0; i < m; ++i) {
-                cx<double> s = cconj(sV(c, i));
-                for (int j = 0; j < i; ++j) s = csub(s, cmul(sS(i, j), sA(j, c)));
-                sA(i, c) = cscale(s, 1.0 / sS(i, i).x);
-            }
-        __syncwarp();
-        // symmetrise, V = I
-        for (int q = lane; q < m * m; q += 32) {
-            const int i = q / m, c = q - i * m;
+        const R lkk = sqrt(dkk), il = 1.0 / lkk;
+        SM(Sg, k * m + k) = ST<S>::make(lkk, 0.0);
+        for (int i = k + 1; i < m; ++i) {
+            S s = SM(Sg, i * m + k);
+            for (int j = 0; j < k; ++j) s = cfms_conjb(SM(Sg, i * m + j), SM(Sg, k * m + j), s);
+            SM(Sg, i * m + k) = cscale(s, il);
+        }
+    }
+    // M = L^-1 A
+    for (int c = 0; c < m; ++c)
+        for (int i = 0; i < m; ++i) {
+            S s = SM(Ag, i * m + c);
+            for (int j = 0; j < i; ++j) s = cfma(ST<S>::neg(SM(Sg, i * m + j)), SM(Mg, j * m + c), s);
+            SM(Mg, i * m + c) = cscale(s, 1.0 / ST<S>::re(SM(Sg, i * m + i)));
+        }
+    // C = L^-1 M^H (Hermitian)
+    for (int c = 0; c < m; ++c)
+        for (int i = 0; i < m; ++i) {
+            S s = ST<S>::conj(SM(Mg, c * m + i));
+            for (int j = 0; j < i; ++j) s = cfma(ST<S>::neg(SM(Sg, i * m + j)), SM(Cg, j * m + c), s);
+            SM(Cg, i * m + c) = cscale(s, 1.0 / ST<S>::re(SM(Sg, i * m + i)));
+        }
+    // symmetrise C into Ag; V = I into Mg
+    for (int i = 0; i < m; ++i)
+        for (int c = 0; c < m; ++c) {
             if (i < c) {
-                const cx<double> u = sA(i, c), l = sA(c, i);
-                const cx<double> h = mk(0.5 * (u.x + l.x), 0.5 * (u.y - l.y));
-                sA(i, c)           = h;
-                sA(c, i)           = cconj(h);
+                const S u = SM(Cg, i * m + c), l = SM(Cg, c * m + i);
+                const S h = ST<S>::make(0.5 * (ST<S>::re(u) + ST<S>::re(l)), 0.5 * (ST<S>::im(u) - ST<S>::im(l)));
+                SM(Ag, i * m + c) = h;
+                SM(Ag, c * m + i) = ST<S>::conj(h);
             } else if (i == c) {
-                sA(i, i).y = 0.0;
+                SM(Ag, i * m + i) = ST<S>::make(ST<S>::re(SM(Cg, i * m + i)), 0.0);
             }
-            sV(i, c) = mk(i == c ? 1.0 : 0.0, 0.0);
+            SM(Mg, i * m + c) = (i == c) ? ST<S>::one() : ST<S>::zero();
         }
-        __syncwarp();
-        // cyclic complex Jacobi: at most 12 sweeps, stop once every off-diagonal is negligible
-        for (int sweep = 0; sweep < 12; ++sweep) {
-            double off = 0.0, dia = 0.0;
-            for (int q = lane; q < m * m; q += 32) {
-                const int i = q / m, c = q - i * m;
-                if (i < c) off = fmax(off, fabs(sA(i, c).x) + fabs(sA(i, c).y));
-                if (i == c) dia = fmax(dia, fabs(sA(i, i).x));
-            }
-            off = warp_max(off);
-            dia = warp_max(dia);
-            if (off <= 1e-17 * dia || off == 0.0) break;
-            for (int p = 0; p < m - 1; ++p)
-                for (int q = p + 1; q < m; ++q) {
-                    const cx<double> bpq = sA(p, q);
-                    const double     ab  = sqrt(bpq.x * bpq.x + bpq.y * bpq.y);
-                    if (ab <= 1e-300) continue;
-                    const double     a = sA(p, p).x, d = sA(q, q).x;
-                    const double     tau = (d - a) / (2.0 * ab);
-                    const double     t   = (tau >= 0.0 ? 1.0 : -1.0) / (fabs(tau) + sqrt(1.0 + tau * tau));
-                    const double     c   = 1.0 / sqrt(1.0 + t * t), s = t * c;
-                    const cx<double> e   = mk(bpq.x / ab, bpq.y / ab);  // b = |b| e
-                    // J = [[c, s], [-s conj(e), c conj(e)]] on columns p, q; C <- J^H C J; V <- V J
-                    const cx<double> jqp = mk(-s * e.x, s * e.y);   // -s conj(e)
-                    const cx<double> jqq = mk(c * e.x, -c * e.y);   //  c conj(e)
-                    for (int r = lane; r < m; r += 32) {
-                        const cx<double> cp = sA(r, p), cq = sA(r, q);
-                        sA(r, p) = cfma(cq, jqp, cscale(cp, c));
-                        sA(r, q) = cfma(cq, jqq, cscale(cp, s));
-                        const cx<double> vp = sV(r, p), vq = sV(r, q);
-                        sV(r, p) = cfma(vq, jqp, cscale(vp, c));
-                        sV(r, q) = cfma(vq, jqq, cscale(vp, s));
-                    }
-                    __syncwarp();
-                    for (int r = lane; r < m; r += 32) {
-                        // rows: (J^H C)_p = c C_p + conj(jqp) C_q ; (J^H C)_q = s C_p + conj(jqq) C_q
-                        const cx<double> cp = sA(p, r), cq = sA(q, r);
-                        sA(p, r) = cfma(cconj(jqp), cq, cscale(cp, c));
-                        sA(q, r) = cfma(cconj(jqq), cq, cscale(cp, s));
-                    }
-                    __syncwarp();
-                    if (lane == 0) {
-                        sA(p, q)   = mk(0.0, 0.0);
-                        sA(q, p)   = mk(0.0, 0.0);
-                        sA(p, p).y = 0.0;
-                        sA(q, q).y = 0.0;
-                    }
-                    __syncwarp();
+    // cyclic Jacobi; a sweep without any rotation ends it (at most 12 sweeps)
+    for (int sweep = 0; sweep < 12; ++sweep) {
+        int rot = 0;
+        for (int p = 0; p < m - 1; ++p)
+            for (int q = p + 1; q < m; ++q) {
+                const S bpq = SM(Ag, p * m + q);
+                const R a = ST<S>::re(SM(Ag, p * m + p)), d = ST<S>::re(SM(Ag, q * m + q));
+                const R ab = sqrt(ST<S>::norm(bpq));
+                if (ab <= 1e-18 * (fabs(a) + fabs(d)) || ab == 0.0) continue;
+                ++rot;
+                const R tau = (d - a) / (2.0 * ab);
+                const R t   = (tau >= 0.0 ? 1.0 : -1.0) / (fabs(tau) + sqrt(1.0 + tau * tau));
+                const R c   = 1.0 / sqrt(1.0 + t * t), s = t * c;
+                const R ex = ST<S>::re(bpq) / ab, ey = ST<S>::im(bpq) / ab;  // b = |b| e
+                // J = [[c, s], [-s conj(e), c conj(e)]] on columns p, q: C <- J^H C J, V <- V J
+                const S jqp = ST<S>::make(-s * ex, s * ey);
+                const S jqq = ST<S>::make(c * ex, -c * ey);
+                for (int r = 0; r < m; ++r) {
+                    const S cp = SM(Ag, r * m + p), cq = SM(Ag, r * m + q);
+                    SM(Ag, r * m + p) = cfma(cq, jqp, cscale(cp, c));
+                    SM(Ag, r * m + q) = cfma(cq, jqq, cscale(cp, s));
+                    const S vp = SM(Mg, r * m + p), vq = SM(Mg, r * m + q);
+                    SM(Mg, r * m + p) = cfma(vq, jqp, cscale(vp, c));
+                    SM(Mg, r * m + q) = cfma(vq, jqq, cscale(vp, s));
                 }
-        }
-        // ascending order of the Ritz values
-        if (lane == 0) {
-            for (int i = 0; i < m; ++i) {
-                sE[i]   = sA(i, i).x;
-                sOrd[i] = i;
-            }
-            for (int i = 1; i < m; ++i) {
-                const double ev = sE[i];
-                const int    o  = sOrd[i];
-                int          k  = i - 1;
-                while (k >= 0 && sE[k] > ev) {
-                    sE[k + 1]   = sE[k];
-                    sOrd[k + 1] = sOrd[k];
-                    --k;
+                for (int r = 0; r < m; ++r) {
+                    const S cp = SM(Ag, p * m + r), cq = SM(Ag, q * m + r);
+                    SM(Ag, p * m + r) = cfma(ST<S>::conj(jqp), cq, cscale(cp, c));
+                    SM(Ag, q * m + r) = cfma(ST<S>::conj(jqq), cq, cscale(cp, s));
                 }
-                sE[k + 1]   = ev;
-                sOrd[k + 1] = o;
+                SM(Ag, p * m + q) = ST<S>::zero();
+                SM(Ag, q * m + p) = ST<S>::zero();
+                SM(Ag, p * m + p) = ST<S>::make(ST<S>::re(SM(Ag, p * m + p)), 0.0);
+                SM(Ag, q * m + q) = ST<S>::make(ST<S>::re(SM(Ag, q * m + q)), 0.0);
             }
-        }
-        __syncwarp();
-        for (int j = lane; j < nb; j += 32) {
-            const double ev = sE[j];
-            Eout[(size_t)b * nb + j] = ev;
-            if (!isfinite(ev)) sBad = 1;
-        }
-        // W = L^-H V (back substitution with the upper factor L^H), into sA
-        if (Xout || grad) {
-            for (int c = lane; c < m; c += 32)
-                for (int i = m - 1; i >= 0; --i) {
-                    cx<double> s = sV(i, c);
-                    for (int j = i + 1; j < m; ++j) s = cfms_conjb(sA(j, c), sS(j, i), s);
-                    sA(i, c) = cscale(s, 1.0 / sS(i, i).x);
-                }
-        }
+        if (rot == 0) break;
     }
-    __syncthreads();
-    if (tid == 0 && sBad && status) status[b] |= 2;
-    if (!(Xout || grad)) return;
+    // the nb smallest Ritz values in ascending order (selection), with their columns of V
+    for (int j = 0; j < nb; ++j) {
+        int kmin = j;
+        R   emin = ST<S>::re(SM(Ag, j * m + j));
+        for (int q = j + 1; q < m; ++q) {
+            const R eq = ST<S>::re(SM(Ag, q * m + q));
+            if (eq < emin) {
+                emin = eq;
+                kmin = q;
+            }
+        }
+        if (kmin != j) {
+            const S t = SM(Ag, j * m + j);
+            SM(Ag, j * m + j) = SM(Ag, kmin * m + kmin);
+            SM(Ag, kmin * m + kmin) = t;
+            for (int r = 0; r < m; ++r) {
+                const S v = SM(Mg, r * m + j);
+                SM(Mg, r * m + j) = SM(Mg, r * m + kmin);
+                SM(Mg, r * m + kmin) = v;
+            }
+        }
+        Eout[(size_t)b * nb + j] = emin;
+        if (!isfinite(emin)) bad = true;
+    }
+    // W = L^-H V[:, :nb] (back substitution with L^H)
+    if (Wout) {
+        for (int c = 0; c < nb; ++c)
+            for (int i = m - 1; i >= 0; --i) {
+                S s = SM(Mg, i * m + c);
+                for (int j = i + 1; j < m; ++j) s = cfms_conjb(SM(Wout, j * nb + c), SM(Sg, j * m + i), s);
+                SM(Wout, i * nb + c) = cscale(s, 1.0 / ST<S>::re(SM(Sg, i * m + i)));
+            }
+    }
+    if (bad && status) atomicOr(status + b, 2);
+}
 
-    // Ritz vectors x_j = X W[:, ord(j)] for the nb kept bands, one warp per band
-    for (int j = warp; j < nb; j += kRefineNT / 32) {
-        const int c  = sOrd[j];
-        double    sx = 0, sy = 0, sz = 0;
+// Ritz vectors x_j = X W[:, j] and gradients; one CTA per matrix, one warp per band.
+template <typename S>
+__global__ void k_refine_vectors(int n, int m, int nb, const S* __restrict__ work, const S* __restrict__ Wg,
+                                 cx<double>* __restrict__ Xout, double* __restrict__ grad, const DevParams P,
+                                 const double* __restrict__ kpts, const int* __restrict__ G, int batch) {
+    const int b = blockIdx.x;
+    if (b >= batch) return;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const S*  X    = work + (size_t)b * refine_work_elems(n, m);
+    for (int j = warp; j < nb; j += nw) {
+        double sx = 0, sy = 0, sz = 0;
         for (int r = lane; r < n; r += 32) {
-            cx<double> x = mk(0.0, 0.0);
-            for (int q = 0; q < m; ++q) x = cfma(X[(size_t)r * m + q], sA(q, c), x);
-            if (Xout) stc(Xout + ((size_t)b * nb + j) * n + r, x);
+            S x = ST<S>::zero();
+            for (int q = 0; q < m; ++q) x = cfma(X[(size_t)r * m + q], SM(Wg, q * nb + j), x);
+            if (Xout) stc(Xout + ((size_t)b * nb + j) * n + r, mk<double>(ST<S>::re(x), ST<S>::im(x)));
             if (grad) {
                 const double* k  = kpts + 3 * (size_t)b;
                 const int     bi = (r < P.N) ? r : r - P.N;
-                const double  w  = x.x * x.x + x.y * x.y;
+                const double  w  = ST<S>::norm(x);
                 sx += (k[0] + G[3 * bi]) * w;
                 sy += (k[1] + G[3 * bi + 1]) * w;
                 sz += (k[2] + G[3 * bi + 2]) * w;
@@ -259,18 +254,36 @@ __global__ void __launch_bounds__(kRefineNT) k_refine(const cx<double>* __restri
             }
         }
     }
-#undef sS
-#undef sA
-#undef sV
 }
+#undef SM
 
-void launch_refine(const cx<double>* H, int n, int ld, size_t mstride, const cx<float>* X32, int m, int nb, double* Eout,
-                   cx<double>* Xout, double* grad, const DevParams& P, const double* d_k, const int* d_G, cx<double>* work,
-                   int* status, int batch, cudaStream_t s) {
-    const size_t smem = sizeof(cx<double>) * 3 * (size_t)m * (m + 1) + sizeof(double) * kRefineMax + sizeof(int) * kRefineMax;
-    if (smem > 48 * 1024) cudaFuncSetAttribute(k_refine, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    k_refine<<<batch, kRefineNT, smem, s>>>(H, n, ld, mstride, X32, m, nb, Eout, Xout, grad, P, d_k, d_G, work, status, batch);
+template <typename S>
+void launch_refine_project(const S* H, int n, int ld, size_t mstride, const cx<float>* X32, int m, S* work, S* small,
+                           int batch, cudaStream_t s) {
+    k_refine_project<S><<<batch, kProjNT, 0, s>>>(H, n, ld, mstride, X32, m, work, small, batch);
     count_launch();
 }
+
+template <typename S>
+void launch_small_eigh(S* small, int m, int nb, double* Eout, S* W, int* status, int batch, cudaStream_t s) {
+    k_small_eigh<S><<<(batch + 63) / 64, 64, 0, s>>>(small, m, nb, Eout, W, status, batch);
+    count_launch();
+}
+
+template <typename S>
+void launch_refine_vectors(int n, int m, int nb, const S* work, const S* W, cx<double>* Xout, double* grad,
+                           const DevParams& P, const double* d_k, const int* d_G, int batch, cudaStream_t s) {
+    k_refine_vectors<S><<<batch, 256, 0, s>>>(n, m, nb, work, W, Xout, grad, P, d_k, d_G, batch);
+    count_launch();
+}
+
+#define UEPM_RF_INST(S)                                                                                             \
+    template void launch_refine_project<S>(const S*, int, int, size_t, const cx<float>*, int, S*, S*, int, cudaStream_t); \
+    template void launch_small_eigh<S>(S*, int, int, double*, S*, int*, int, cudaStream_t);                        \
+    template void launch_refine_vectors<S>(int, int, int, const S*, const S*, cx<double>*, double*, const DevParams&,   \
+                                           const double*, const int*, int, cudaStream_t);
+UEPM_RF_INST(double)
+UEPM_RF_INST(cx<double>)
+#undef UEPM_RF_INST
 
 }  // namespace uepm

@@ -1,198 +1,212 @@
-// tridiag.cu -- batched Householder reduction of complex Hermitian matrices to real symmetric
-// tridiagonal form, one CTA per matrix (the first half of Eigen's SelfAdjointEigenSolver, called by
-// Hamiltonian::Diagonalize, src/EPP/Hamiltonian.cpp:125-134).
+// tridiag.cu -- batched Householder reduction of Hermitian (or real symmetric) matrices to real
+// symmetric tridiagonal form, one CTA per matrix (the first half of Eigen's SelfAdjointEigenSolver,
+// called by Hamiltonian::Diagonalize, src/EPP/Hamiltonian.cpp:125-134).
 //
-// Algorithm (LAPACK zhetd2 / Eigen tridiagonalization_inplace, lower storage): for i = 0..n-2
+// Algorithm (LAPACK zhetd2 / Eigen tridiagonalization_inplace): for i = 0..n-2
 //   v = house(A[i+1:, i])               beta real, tau = (beta - alpha) / beta
-//   p = tau * A22 v                     Hermitian product from the lower triangle
+//   p = tau * A22 v
 //   w = p - (tau/2)(p^H v) v
-//   A22 -= v w^H + w v^H                lower triangle only
+//   A22 -= v w^H + w v^H
 // so that A = Q T Q^H with Q = H_0 ... H_{n-2}, H_i = I - tau_i v_i v_i^H. The reflector tails stay
-// in A below the subdiagonal and the tau_i go to `tq`, for the back-transformation.
+// in column i below the subdiagonal and the tau_i go to `tq`, for the back-transformation.
 //
-// GB300 mapping. The matrix lives in a per-k HBM workspace (L2-resident while the CTA works on
-// it). Each step streams the trailing triangle twice (product, then rank-2 update). Warps own
-// columns round-robin, lanes own rows r = lane + 32 t (fixed alignment), so the Hermitian product
-// keeps per-lane row accumulators in registers and needs one cross-warp sum in shared memory per
-// step. Each stored element costs exactly 8 FMAs in the product and 8 in the update, which is the
-// 16/3 n^3 algorithmic flop count; in FP64 this kernel is bound by GB300's FP64 pipe.
+// GB300 mapping. GB300's FP64 pipe issues one warp instruction per ~16 cycles per SM whatever the
+// lane mask, so the kernel is organised to issue FP64 instructions only with full lanes and only for
+// algorithmic work:
+//   * the matrix is kept in FULL storage (both triangles): the rank-2 update computes the lower
+//     triangle and mirrors each element into the upper one (a store, no arithmetic), so the product
+//     p = A22 v is a plain row-by-lane product with per-lane accumulators and no cross-lane
+//     reductions (4 FMA per element, complex);
+//   * chunk loops have warp-uniform bounds, so fully masked chunks are skipped, not issued;
+//   * the Householder scalars (sqrt, reciprocals) are computed once per CTA by one thread.
+// Per step: 4 m^2 FMA for the product + 4 m^2 for the lower-triangle update (complex), i.e. the
+// 16/3 n^3 algorithmic flops (4/3 n^3 for real symmetric matrices). The matrix lives in a per-k HBM
+// workspace; the 129 MB L2 holds the working set of the resident CTAs.
 #include "uepm_common.cuh"
 #include "uepm_kernels.h"
 
 namespace uepm {
 
-template <typename T, int NT, int MAXT>
-__global__ void __launch_bounds__(NT) k_tridiag(cx<T>* __restrict__ H, int n, int ld, size_t mstride, T* __restrict__ dOut,
-                                                T* __restrict__ eOut, cx<T>* __restrict__ tqOut, int* __restrict__ status,
-                                                int batch) {
+template <typename S, int NT, int MAXT>
+__global__ void __launch_bounds__(NT) k_tridiag(S* __restrict__ H, int n, int ld, size_t mstride,
+                                                typename ST<S>::R* __restrict__ dOut, typename ST<S>::R* __restrict__ eOut,
+                                                S* __restrict__ tqOut, int* __restrict__ status, int batch) {
+    using R       = typename ST<S>::R;
     constexpr int NW = NT / 32;
     const int     b  = blockIdx.x;
     if (b >= batch) return;
-    cx<T>* A = H + (size_t)b * mstride;
+    S* A = H + (size_t)b * mstride;
     extern __shared__ __align__(16) unsigned char smraw[];
-    cx<T>*    v    = reinterpret_cast<cx<T>*>(smraw);  // n
-    cx<T>*    w    = v + n;                            // n
-    cx<T>*    pdot = w + n;                            // n
-    cx<T>*    pacc = pdot + n;                         // NW * n
-    T*        red  = reinterpret_cast<T*>(pacc + NW * n);  // 3 * NW
+    S*        v    = reinterpret_cast<S*>(smraw);  // n
+    S*        w    = v + n;                        // n
+    S*        pacc = w + n;                        // NW * n
+    R*        red  = reinterpret_cast<R*>(pacc + NW * n);  // 3 * NW
+    __shared__ S   s_th, s_sc;
+    __shared__ int s_skip;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     bool      bad = false;
 
     for (int i = 0; i < n - 1; ++i) {
         const int o = i + 1, m = n - o;
-        cx<T>*    col = A + (size_t)i * ld + o;
+        S*        col = A + (size_t)i * ld + o;
 
         // ---- Householder vector of A[o:, i] -------------------------------------------------
-        T part = 0;
-        for (int r = 1 + tid; r < m; r += NT) {
-            const cx<T> x = ldc(col + r);
-            part          = fma(x.x, x.x, fma(x.y, x.y, part));
-        }
+        R part = 0;
+        for (int r = 1 + tid; r < m; r += NT) part += ST<S>::norm(ldc(col + r));
         part = warp_sum(part);
         if (lane == 0) red[warp] = part;
-        const cx<T> c0 = ldc(col);
         __syncthreads();
-        T tail2 = 0;
+        if (tid == 0) {
+            R tail2 = 0;
 #pragma unroll
-        for (int q = 0; q < NW; ++q) tail2 += red[q];
-        T     beta;
-        cx<T> th, sc;
-        if (tail2 <= num<T>::tiny() && c0.y * c0.y <= num<T>::tiny()) {
-            th   = mk<T>(0, 0);
-            sc   = mk<T>(0, 0);
-            beta = c0.x;
-        } else {
-            beta = sqrt(fma(c0.x, c0.x, fma(c0.y, c0.y, tail2)));
-            if (c0.x >= 0) beta = -beta;
-            const T ib = T(1) / beta;
-            th         = mk<T>((beta - c0.x) * ib, -c0.y * ib);
-            // sc = 1 / (c0 - beta)
-            const T ar = c0.x - beta, ai = c0.y;
-            const T den = T(1) / fma(ar, ar, ai * ai);
-            sc          = mk<T>(ar * den, -ai * den);
+            for (int q = 0; q < NW; ++q) tail2 += red[q];
+            const S c0 = ldc(col);
+            const R c0r = ST<S>::re(c0), c0i = ST<S>::im(c0);
+            R       beta;
+            S       th, sc;
+            if (tail2 <= num<R>::tiny() && c0i * c0i <= num<R>::tiny()) {
+                th   = ST<S>::zero();
+                sc   = ST<S>::zero();
+                beta = c0r;
+            } else {
+                beta = sqrt(fma(c0r, c0r, fma(c0i, c0i, tail2)));
+                if (c0r >= 0) beta = -beta;
+                const R ib = R(1) / beta;
+                th         = ST<S>::make((beta - c0r) * ib, -c0i * ib);
+                // sc = 1 / (c0 - beta)
+                const R ar = c0r - beta, ai = c0i;
+                const R den = R(1) / fma(ar, ar, ai * ai);
+                sc          = ST<S>::make(ar * den, -ai * den);
+            }
+            s_th   = th;
+            s_sc   = sc;
+            s_skip = (ST<S>::re(th) == R(0) && ST<S>::im(th) == R(0));
+            const R di = ST<S>::re(A[(size_t)i * ld + i]);
+            dOut[(size_t)b * n + i]  = di;
+            eOut[(size_t)b * n + i]  = beta;
+            tqOut[(size_t)b * n + i] = th;
+            stc(col, ST<S>::make(beta, R(0)));
+            if (!isfinite(beta) || !isfinite(di)) bad = true;
         }
-        const bool skip = (th.x == T(0) && th.y == T(0));
+        __syncthreads();
+        const S th = s_th, sc = s_sc;
         for (int r = tid; r < m; r += NT) {
-            cx<T> vr;
+            S vr;
             if (r == 0) {
-                vr = mk<T>(1, 0);
+                vr = ST<S>::one();
             } else {
                 vr = cmul(ldc(col + r), sc);
                 stc(col + r, vr);
             }
             v[r] = vr;
         }
-        if (tid == 0) {
-            const T di = A[(size_t)i * ld + i].x;
-            dOut[(size_t)b * n + i]  = di;
-            eOut[(size_t)b * n + i]  = beta;
-            tqOut[(size_t)b * n + i] = th;
-            stc(col, mk<T>(beta, 0));
-            if (!isfinite(beta) || !isfinite(di)) bad = true;
-        }
         __syncthreads();
-        if (skip) continue;
+        if (s_skip) continue;
 
-        // ---- p = A22 v (Hermitian, lower storage) ---------------------------------------------
-        cx<T> acc[MAXT];
+        // ---- p = A22 v (full storage): warps own columns, lanes own rows ----------------------
+        S acc[MAXT];
 #pragma unroll
-        for (int t = 0; t < MAXT; ++t) acc[t] = mk<T>(0, 0);
+        for (int t = 0; t < MAXT; ++t) acc[t] = ST<S>::zero();
+        const int tn = (m + 31) >> 5;
         for (int c = warp; c < m; c += NW) {
-            const cx<T>* ac  = A + (size_t)(o + c) * ld + o;
-            const cx<T>  vc  = v[c];
-            cx<T>        dot = mk<T>(0, 0);
+            const S* ac = A + (size_t)(o + c) * ld + o;
+            const S  vc = v[c];
 #pragma unroll
             for (int t = 0; t < MAXT; ++t) {
-                const int r = lane + 32 * t;
-                if (r > c && r < m) {
-                    const cx<T> a = ldc(ac + r);
-                    acc[t]        = cfma(a, vc, acc[t]);
-                    dot           = cfmac(a, v[r], dot);
+                if (t < tn) {  // warp-uniform
+                    const int r = lane + 32 * t;
+                    const S   a = (r < m) ? ldc(ac + r) : ST<S>::zero();
+                    acc[t]      = cfma(a, vc, acc[t]);
                 }
-            }
-            dot = warp_sum(dot);
-            if (lane == 0) {
-                const T acc_d = ac[c].x;
-                pdot[c]       = mk<T>(fma(acc_d, vc.x, dot.x), fma(acc_d, vc.y, dot.y));
             }
         }
 #pragma unroll
         for (int t = 0; t < MAXT; ++t) {
             const int r = lane + 32 * t;
-            if (r < m) pacc[warp * n + r] = acc[t];
+            if (t < tn && r < m) pacc[warp * n + r] = acc[t];
         }
         __syncthreads();
 
         // ---- w = tau p; alpha = -tau/2 (w^H v) -------------------------------------------------
-        cx<T> part2 = mk<T>(0, 0);
+        S part2 = ST<S>::zero();
         for (int r = tid; r < m; r += NT) {
-            cx<T> p = pdot[r];
+            S p = pacc[r];
 #pragma unroll
-            for (int q = 0; q < NW; ++q) p = cadd(p, pacc[q * n + r]);
-            const cx<T> wr = cmul(th, p);
-            w[r]           = wr;
-            part2          = cfmac(wr, v[r], part2);
+            for (int q = 1; q < NW; ++q) p = cadd(p, pacc[q * n + r]);
+            const S wr = cmul(th, p);
+            w[r]       = wr;
+            part2      = cfmac(wr, v[r], part2);
         }
         part2 = warp_sum(part2);
         if (lane == 0) {
-            red[NW + warp]     = part2.x;
-            red[2 * NW + warp] = part2.y;
+            red[NW + warp]     = ST<S>::re(part2);
+            red[2 * NW + warp] = ST<S>::im(part2);
         }
         __syncthreads();
-        cx<T> wv = mk<T>(0, 0);
+        R wvr = 0, wvi = 0;
 #pragma unroll
         for (int q = 0; q < NW; ++q) {
-            wv.x += red[NW + q];
-            wv.y += red[2 * NW + q];
+            wvr += red[NW + q];
+            wvi += red[2 * NW + q];
         }
-        const cx<T> alpha = cscale(cmul(th, wv), T(-0.5));
+        const S alpha = cscale(cmul(th, ST<S>::make(wvr, wvi)), R(-0.5));
         for (int r = tid; r < m; r += NT) w[r] = cfma(alpha, v[r], w[r]);
         __syncthreads();
 
-        // ---- A22 -= v w^H + w v^H (lower) ------------------------------------------------------
+        // ---- A22 -= v w^H + w v^H: lower triangle computed, upper mirrored -------------------
         for (int c = warp; c < m; c += NW) {
-            cx<T>*      ac = A + (size_t)(o + c) * ld + o;
-            const cx<T> vc = v[c], wc = w[c];
+            S*      ac = A + (size_t)(o + c) * ld + o;
+            const S vc = v[c], wc = w[c];
             for (int r = c + lane; r < m; r += 32) {
-                cx<T> a = ldc(ac + r);
-                a       = cfms_conjb(v[r], wc, a);
-                a       = cfms_conjb(w[r], vc, a);
+                S a = ldc(ac + r);
+                a   = cfms_conjb(v[r], wc, a);
+                a   = cfms_conjb(w[r], vc, a);
+                if (r == c) {
+                    a = ST<S>::make(ST<S>::re(a), R(0));
+                } else {
+                    stc(A + (size_t)(o + r) * ld + (o + c), ST<S>::conj(a));
+                }
                 stc(ac + r, a);
             }
         }
         __syncthreads();
     }
     if (tid == 0) {
-        const T dl = A[(size_t)(n - 1) * ld + (n - 1)].x;
+        const R dl = ST<S>::re(A[(size_t)(n - 1) * ld + (n - 1)]);
         dOut[(size_t)b * n + n - 1] = dl;
-        eOut[(size_t)b * n + n - 1] = T(0);
-        tqOut[(size_t)b * n + n - 1] = mk<T>(0, 0);
+        eOut[(size_t)b * n + n - 1] = R(0);
+        tqOut[(size_t)b * n + n - 1] = ST<S>::zero();
         if (!isfinite(dl)) bad = true;
-        if (bad && status) status[b] |= 2;  // UEPM_K_NONFINITE
+        if (bad && status) atomicOr(status + b, 2);  // UEPM_K_NONFINITE
     }
 }
 
-template <typename T, int NT, int MAXT>
-static void tridiag_launch_t(cx<T>* H, int n, int ld, size_t mstride, T* d, T* e, cx<T>* tq, int* status, int batch,
-                             cudaStream_t s) {
-    const size_t smem = sizeof(cx<T>) * (size_t)(3 + NT / 32) * n + sizeof(T) * 3 * (NT / 32);
-    auto         kern = k_tridiag<T, NT, MAXT>;
+template <typename S, int NT, int MAXT>
+static void tridiag_launch_t(S* H, int n, int ld, size_t mstride, typename ST<S>::R* d, typename ST<S>::R* e, S* tq,
+                             int* status, int batch, cudaStream_t s) {
+    using R           = typename ST<S>::R;
+    const size_t smem = sizeof(S) * (size_t)(2 + NT / 32) * n + sizeof(R) * 3 * (NT / 32);
+    auto         kern = k_tridiag<S, NT, MAXT>;
     if (smem > 48 * 1024) cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     kern<<<batch, NT, smem, s>>>(H, n, ld, mstride, d, e, tq, status, batch);
     count_launch();
 }
 
-template <typename T>
-void launch_tridiag(cx<T>* H, int n, int ld, size_t mstride, T* d, T* e, cx<T>* tq, int* status, int batch, cudaStream_t s) {
-    // rows of the trailing matrix are at most n - 1 = 32 * MAXT
-    if (n <= 129) tridiag_launch_t<T, 256, 4>(H, n, ld, mstride, d, e, tq, status, batch, s);
-    else if (n <= 161) tridiag_launch_t<T, 256, 5>(H, n, ld, mstride, d, e, tq, status, batch, s);
-    else if (n <= 257) tridiag_launch_t<T, 256, 8>(H, n, ld, mstride, d, e, tq, status, batch, s);
-    else if (n <= 385) tridiag_launch_t<T, 256, 12>(H, n, ld, mstride, d, e, tq, status, batch, s);
-    else tridiag_launch_t<T, 256, 16>(H, n, ld, mstride, d, e, tq, status, batch, s);
+template <typename S>
+void launch_tridiag(S* H, int n, int ld, size_t mstride, typename ST<S>::R* d, typename ST<S>::R* e, S* tq, int* status,
+                    int batch, cudaStream_t s) {
+    // rows of the trailing matrix are at most n - 1 <= 32 * MAXT
+    constexpr int NT = 128;
+    if (n <= 129) tridiag_launch_t<S, NT, 4>(H, n, ld, mstride, d, e, tq, status, batch, s);
+    else if (n <= 161) tridiag_launch_t<S, NT, 5>(H, n, ld, mstride, d, e, tq, status, batch, s);
+    else if (n <= 257) tridiag_launch_t<S, NT, 8>(H, n, ld, mstride, d, e, tq, status, batch, s);
+    else if (n <= 385) tridiag_launch_t<S, NT, 12>(H, n, ld, mstride, d, e, tq, status, batch, s);
+    else tridiag_launch_t<S, NT, 16>(H, n, ld, mstride, d, e, tq, status, batch, s);
 }
 
-template void launch_tridiag<double>(cx<double>*, int, int, size_t, double*, double*, cx<double>*, int*, int, cudaStream_t);
-template void launch_tridiag<float>(cx<float>*, int, int, size_t, float*, float*, cx<float>*, int*, int, cudaStream_t);
+template void launch_tridiag<cx<double>>(cx<double>*, int, int, size_t, double*, double*, cx<double>*, int*, int, cudaStream_t);
+template void launch_tridiag<cx<float>>(cx<float>*, int, int, size_t, float*, float*, cx<float>*, int*, int, cudaStream_t);
+template void launch_tridiag<double>(double*, int, int, size_t, double*, double*, double*, int*, int, cudaStream_t);
+template void launch_tridiag<float>(float*, int, int, size_t, float*, float*, float*, int*, int, cudaStream_t);
 
 }  // namespace uepm

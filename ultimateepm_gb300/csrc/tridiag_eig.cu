@@ -12,6 +12,8 @@
 //             Gram-Schmidt inside clusters (consecutive gaps <= 1e-3 ||T||_1), so degenerate
 //             bands (Kramers pairs with SOC, the Gamma-point triplets) get an orthonormal basis of
 //             their eigenspace. Iteration counts are fixed: nothing here can spin.
+#include <algorithm>
+
 #include "uepm_common.cuh"
 #include "uepm_kernels.h"
 
@@ -21,47 +23,82 @@ constexpr int kBisectWarpsPerBlock = 4;
 constexpr int kInvitWarpsPerBlock  = 2;
 constexpr int kInvitIters          = 3;
 
-template <typename T>
-__device__ __forceinline__ int sturm_count(const T* __restrict__ d, const T* __restrict__ e2, int n, T x, T pivmin) {
-    T   q   = d[0] - x;
-    if (fabs(q) <= pivmin) q = -pivmin;
-    int cnt = (q < T(0));
+// Sturm count: the number of eigenvalues of T below x, from the LDL^T pivots
+// q_0 = d_0 - x, q_i = (d_i - x) - e_{i-1}^2 / q_{i-1} (pivots within pivmin replaced by -pivmin).
+// FP64: 1 / q comes from the hardware reciprocal approximation refined by two Newton steps (relative
+// error far below 1e-20, i.e. a backward perturbation of e^2 well under the tolerance), and the
+// pivot guard and sign test use integer compares on the high word, so a step issues 6 FP64
+// instructions instead of a full IEEE division sequence.
+__device__ __forceinline__ int sturm_count(const double* __restrict__ d, const double* __restrict__ e2, int n, double x,
+                                           double pivmin) {
+    const int piv_hi = __double2hiint(pivmin);
+    double    q      = d[0] - x;
+    if ((__double2hiint(q) & 0x7fffffff) <= piv_hi) q = -pivmin;
+    int cnt = (int)((unsigned)__double2hiint(q) >> 31);
     for (int i = 1; i < n; ++i) {
-        q = (d[i] - x) - e2[i - 1] / q;
-        if (fabs(q) <= pivmin) q = -pivmin;
-        cnt += (q < T(0));
+        double r;
+        asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(r) : "d"(q));
+        double er = fma(-q, r, 1.0);
+        r         = fma(r, er, r);
+        er        = fma(-q, r, 1.0);
+        r         = fma(r, er, r);
+        q         = fma(-e2[i - 1], r, d[i] - x);
+        if ((__double2hiint(q) & 0x7fffffff) <= piv_hi) q = -pivmin;
+        cnt += (int)((unsigned)__double2hiint(q) >> 31);
+    }
+    return cnt;
+}
+__device__ __forceinline__ int sturm_count(const float* __restrict__ d, const float* __restrict__ e2, int n, float x,
+                                           float pivmin) {
+    float q = d[0] - x;
+    if (fabsf(q) <= pivmin) q = -pivmin;
+    int cnt = (q < 0.f);
+    for (int i = 1; i < n; ++i) {
+        q = (d[i] - x) - __fdividef(e2[i - 1], q);
+        if (fabsf(q) <= pivmin) q = -pivmin;
+        cnt += (q < 0.f);
     }
     return cnt;
 }
 
+// One group of LPM lanes per matrix (LPM = smallest power of two >= nb, at most 32), so a warp
+// bisects 32 / LPM matrices at once and every lane carries an eigenvalue.
 template <typename T>
-__global__ void k_bisect(const T* __restrict__ dIn, const T* __restrict__ eIn, int n, int nb, T* __restrict__ evOut, int ev_ld,
-                         int batch) {
+__global__ void k_bisect(const T* __restrict__ dIn, const T* __restrict__ eIn, int n, int nb, int lpm, T* __restrict__ evOut,
+                         int ev_ld, int batch) {
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int b    = blockIdx.x * kBisectWarpsPerBlock + warp;
+    const int mpw  = 32 / lpm;
+    const int g    = lane / lpm, gl = lane - g * lpm;
+    const int b    = (blockIdx.x * kBisectWarpsPerBlock + warp) * mpw + g;
     extern __shared__ __align__(16) unsigned char smraw[];
-    T* d  = reinterpret_cast<T*>(smraw) + (size_t)warp * 2 * n;
-    T* e2 = d + n;
-    if (b >= batch) return;
-    const T* dg = dIn + (size_t)b * n;
-    const T* eg = eIn + (size_t)b * n;
-    T        lo = T(3.0e38), hi = T(-3.0e38), emax2 = T(0);
-    for (int i = lane; i < n; i += 32) {
-        const T di = dg[i];
-        const T em = (i > 0) ? fabs(eg[i - 1]) : T(0);
-        const T ep = (i < n - 1) ? fabs(eg[i]) : T(0);
-        d[i]       = di;
-        if (i < n - 1) {
-            e2[i] = eg[i] * eg[i];
-            emax2 = max(emax2, e2[i]);
+    T*         d     = reinterpret_cast<T*>(smraw) + ((size_t)warp * mpw + g) * 2 * n;
+    T*         e2    = d + n;
+    const bool valid = b < batch;
+    T          lo = T(3.0e38), hi = T(-3.0e38), emax2 = T(0);
+    if (valid) {
+        const T* dg = dIn + (size_t)b * n;
+        const T* eg = eIn + (size_t)b * n;
+        for (int i = gl; i < n; i += lpm) {
+            const T di = dg[i];
+            const T em = (i > 0) ? fabs(eg[i - 1]) : T(0);
+            const T ep = (i < n - 1) ? fabs(eg[i]) : T(0);
+            d[i]       = di;
+            if (i < n - 1) {
+                e2[i] = eg[i] * eg[i];
+                emax2 = max(emax2, e2[i]);
+            }
+            lo = min(lo, di - em - ep);
+            hi = max(hi, di + em + ep);
         }
-        lo = min(lo, di - em - ep);
-        hi = max(hi, di + em + ep);
     }
-    lo    = warp_min(lo);
-    hi    = warp_max(hi);
-    emax2 = warp_max(emax2);
+    // reductions within each lane group
+    for (int o = lpm / 2; o > 0; o >>= 1) {
+        lo    = min(lo, __shfl_xor_sync(0xffffffffu, lo, o));
+        hi    = max(hi, __shfl_xor_sync(0xffffffffu, hi, o));
+        emax2 = max(emax2, __shfl_xor_sync(0xffffffffu, emax2, o));
+    }
     __syncwarp();
+    if (!valid) return;
     const T eps    = num<T>::eps();
     const T pivmin = num<T>::tiny() * max(T(1), emax2);
     const T tnorm  = max(fabs(lo), fabs(hi));
@@ -69,7 +106,7 @@ __global__ void k_bisect(const T* __restrict__ dIn, const T* __restrict__ eIn, i
     lo -= widen;
     hi += widen;
     const T atol = eps * tnorm;
-    for (int j = lane; j < nb; j += 32) {
+    for (int j = gl; j < nb; j += lpm) {
         T a = lo, c = hi;
         // count(a) <= j < count(c) holds throughout; at most ~log2(range / atol) < 200 steps.
         for (int it = 0; it < 200; ++it) {
@@ -85,9 +122,18 @@ __global__ void k_bisect(const T* __restrict__ dIn, const T* __restrict__ eIn, i
 
 template <typename T>
 void launch_bisect(const T* d, const T* e, int n, int nb, T* ev, int ev_ld, int batch, cudaStream_t s) {
-    const int    blocks = (batch + kBisectWarpsPerBlock - 1) / kBisectWarpsPerBlock;
-    const size_t smem   = sizeof(T) * 2 * (size_t)n * kBisectWarpsPerBlock;
-    k_bisect<T><<<blocks, 32 * kBisectWarpsPerBlock, smem, s>>>(d, e, n, nb, ev, ev_ld, batch);
+    // lanes per matrix: >= nb (one lane per eigenvalue) and large enough that the d / e^2 copies
+    // of the warp's matrices fit in 96 KB of shared memory per block
+    const int max_mpw = (int)std::max<size_t>(1, (96 * 1024) / (sizeof(T) * 2 * (size_t)n * kBisectWarpsPerBlock));
+    int       lpm     = 1;
+    while ((lpm < nb || 32 / lpm > max_mpw) && lpm < 32) lpm <<= 1;
+    const int    mpw    = 32 / lpm;
+    const int    warps  = (batch + mpw - 1) / mpw;
+    const int    blocks = (warps + kBisectWarpsPerBlock - 1) / kBisectWarpsPerBlock;
+    const size_t smem   = sizeof(T) * 2 * (size_t)n * 32 * kBisectWarpsPerBlock / lpm;
+    auto         kern   = k_bisect<T>;
+    if (smem > 48 * 1024) cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    kern<<<blocks, 32 * kBisectWarpsPerBlock, smem, s>>>(d, e, n, nb, lpm, ev, ev_ld, batch);
     count_launch();
 }
 

@@ -68,6 +68,80 @@ __device__ __forceinline__ cx<float> ldc(const cx<float>* p) {
 __device__ __forceinline__ void stc(cx<double>* p, cx<double> a) { *reinterpret_cast<double2*>(p) = make_double2(a.x, a.y); }
 __device__ __forceinline__ void stc(cx<float>* p, cx<float> a) { *reinterpret_cast<float2*>(p) = make_float2(a.x, a.y); }
 
+// Real-scalar counterparts of the complex helpers: the same kernel templates serve real symmetric
+// matrices (H(k) is exactly real for diamond-structure local / symmetric-nonlocal EPM without SOC).
+__device__ __forceinline__ double cadd(double a, double b) { return a + b; }
+__device__ __forceinline__ float cadd(float a, float b) { return a + b; }
+__device__ __forceinline__ double cmul(double a, double b) { return a * b; }
+__device__ __forceinline__ float cmul(float a, float b) { return a * b; }
+__device__ __forceinline__ double cfma(double a, double b, double c) { return fma(a, b, c); }
+__device__ __forceinline__ float cfma(float a, float b, float c) { return fmaf(a, b, c); }
+__device__ __forceinline__ double cfmac(double a, double b, double c) { return fma(a, b, c); }
+__device__ __forceinline__ float cfmac(float a, float b, float c) { return fmaf(a, b, c); }
+__device__ __forceinline__ double cfms_conjb(double a, double b, double c) { return fma(-a, b, c); }
+__device__ __forceinline__ float cfms_conjb(float a, float b, float c) { return fmaf(-a, b, c); }
+__device__ __forceinline__ double cscale(double a, double s) { return a * s; }
+__device__ __forceinline__ float cscale(float a, float s) { return a * s; }
+__device__ __forceinline__ double ldc(const double* p) { return *p; }
+__device__ __forceinline__ float ldc(const float* p) { return *p; }
+__device__ __forceinline__ void stc(double* p, double a) { *p = a; }
+__device__ __forceinline__ void stc(float* p, float a) { *p = a; }
+
+// Scalar traits: R = the real type, and the few operations that differ between real and complex.
+template <typename S>
+struct ST;
+template <>
+struct ST<double> {
+    using R = double;
+    static constexpr bool cplx = false;
+    static __device__ __forceinline__ double zero() { return 0.0; }
+    static __device__ __forceinline__ double one() { return 1.0; }
+    static __device__ __forceinline__ double re(double a) { return a; }
+    static __device__ __forceinline__ double im(double) { return 0.0; }
+    static __device__ __forceinline__ double make(double r, double) { return r; }
+    static __device__ __forceinline__ double conj(double a) { return a; }
+    static __device__ __forceinline__ double norm(double a) { return a * a; }
+    static __device__ __forceinline__ double neg(double a) { return -a; }
+};
+template <>
+struct ST<float> {
+    using R = float;
+    static constexpr bool cplx = false;
+    static __device__ __forceinline__ float zero() { return 0.f; }
+    static __device__ __forceinline__ float one() { return 1.f; }
+    static __device__ __forceinline__ float re(float a) { return a; }
+    static __device__ __forceinline__ float im(float) { return 0.f; }
+    static __device__ __forceinline__ float make(float r, float) { return r; }
+    static __device__ __forceinline__ float conj(float a) { return a; }
+    static __device__ __forceinline__ float norm(float a) { return a * a; }
+    static __device__ __forceinline__ float neg(float a) { return -a; }
+};
+template <typename T>
+struct ST<cx<T>> {
+    using R = T;
+    static constexpr bool cplx = true;
+    static __device__ __forceinline__ cx<T> zero() { return mk<T>(0, 0); }
+    static __device__ __forceinline__ cx<T> one() { return mk<T>(1, 0); }
+    static __device__ __forceinline__ T re(cx<T> a) { return a.x; }
+    static __device__ __forceinline__ T im(cx<T> a) { return a.y; }
+    static __device__ __forceinline__ cx<T> make(T r, T i) { return mk<T>(r, i); }
+    static __device__ __forceinline__ cx<T> conj(cx<T> a) { return mk<T>(a.x, -a.y); }
+    static __device__ __forceinline__ T norm(cx<T> a) { return fma(a.x, a.x, a.y * a.y); }
+    static __device__ __forceinline__ cx<T> neg(cx<T> a) { return mk<T>(-a.x, -a.y); }
+};
+
+// Lower-precision counterpart of a scalar type (FP64 -> FP32), for the mixed path.
+template <typename S>
+struct Lower;
+template <>
+struct Lower<double> {
+    using type = float;
+};
+template <>
+struct Lower<cx<double>> {
+    using type = cx<float>;
+};
+
 template <typename T>
 __device__ __forceinline__ T warp_sum(T v) {
 #pragma unroll

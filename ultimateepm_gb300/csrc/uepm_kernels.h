@@ -1,4 +1,5 @@
 // uepm_kernels.h -- host-side launch wrappers of the device kernels (one declaration per kernel).
+// Scalar type S is double / float (real symmetric H) or cx<double> / cx<float> (complex Hermitian H).
 #pragma once
 
 #include <cuda_runtime.h>
@@ -10,16 +11,19 @@ namespace uepm {
 
 void count_launch(int n = 1);
 
-// assemble.cu
+// assemble.cu: H(k) in FULL column-major storage (both triangles). SO = double (real H) or
+// cx<double>; H32 (optional) receives the FP32 copy for the mixed path (float or cx<float>).
 void launch_rows(const DevParams& P, const double* d_k, const int* d_G, double* d_rows, int batch, cudaStream_t s);
+template <typename SO>
 void launch_assemble(const DevParams& P, const cx<double>* Vloc, const double2* phNL, const double2* phSO, const double* rows,
-                     cx<double>* H, int ld, size_t mstride, cx<float>* H32, size_t mstride32, int batch, cudaStream_t s);
-void launch_mirror_upper(cx<double>* H, int n, int ld, size_t mstride, int batch, cudaStream_t s);
+                     SO* H, int ld, size_t mstride, typename Lower<SO>::type* H32, size_t mstride32, int batch,
+                     cudaStream_t s);
 
-// tridiag.cu: Householder reduction of the lower triangle, in place. d, e: [batch][n];
-// tq: [batch][n] reflector scalars; status: [batch] (ORed with UEPM_K_NONFINITE on NaN/Inf).
-template <typename T>
-void launch_tridiag(cx<T>* H, int n, int ld, size_t mstride, T* d, T* e, cx<T>* tq, int* status, int batch, cudaStream_t s);
+// tridiag.cu: Householder reduction in place. d, e: [batch][n]; tq: [batch][n] reflector scalars;
+// status: [batch] (ORed with UEPM_K_NONFINITE on NaN/Inf).
+template <typename S>
+void launch_tridiag(S* H, int n, int ld, size_t mstride, typename ST<S>::R* d, typename ST<S>::R* e, S* tq, int* status,
+                    int batch, cudaStream_t s);
 
 // tridiag_eig.cu
 template <typename T>
@@ -33,18 +37,26 @@ __host__ __device__ inline size_t invit_work_elems(int n) {
     return (size_t)5 * n * 32;
 }
 
-// backtransform.cu: X = Q Z for the nb vectors, optional gradient and complex-vector output.
-template <typename T>
-void launch_backtransform(const cx<T>* H, int n, int ld, size_t mstride, const cx<T>* tq, const T* z, int nb,
-                          cx<T>* Xout, const DevParams& P, const double* d_k, const int* d_G, double* grad,
-                          const T* ev, double* Eout, int batch, cudaStream_t s);
+// backtransform.cu: X = Q Z for nb real tridiagonal eigenvectors z ([batch][nb][n]); X is written as
+// complex ([batch][nb][n]) when Xout is given; optional Hellmann-Feynman gradients ([batch][nb][3]).
+template <typename S>
+void launch_backtransform(const S* H, int n, int ld, size_t mstride, const S* tq, const typename ST<S>::R* z, int nb,
+                          cx<typename ST<S>::R>* Xout, const DevParams& P, const double* d_k, const int* d_G, double* grad,
+                          int batch, cudaStream_t s);
 
-// refine.cu: FP64 residual + Rayleigh-Ritz in the nb-dimensional subspace of FP32 vectors.
-// X32 holds m >= nb FP32 vectors ([batch][m][n]); the nb lowest Ritz pairs are returned.
+// refine.cu: FP64 Rayleigh-Ritz in the m-dimensional subspace of FP32 vectors X32 ([batch][m][n]);
+// the nb lowest Ritz values go to Eout, optionally vectors / gradients.
 constexpr int kRefineMaxSubspace = 40;
-void launch_refine(const cx<double>* H, int n, int ld, size_t mstride, const cx<float>* X32, int m, int nb, double* Eout,
-                   cx<double>* Xout, double* grad, const DevParams& P, const double* d_k, const int* d_G, cx<double>* work,
-                   int* status, int batch, cudaStream_t s);
 __host__ __device__ inline size_t refine_work_elems(int n, int m) { return (size_t)2 * n * m; }
+// small-solve scratch per matrix: 4 m x m blocks plus the m x nb Ritz coefficients
+__host__ __device__ inline size_t refine_small_elems(int m, int nb) { return (size_t)4 * m * m + (size_t)m * nb; }
+template <typename S>
+void launch_refine_project(const S* H, int n, int ld, size_t mstride, const cx<float>* X32, int m, S* work, S* small,
+                           int batch, cudaStream_t s);
+template <typename S>
+void launch_small_eigh(S* small, int m, int nb, double* Eout, S* W, int* status, int batch, cudaStream_t s);
+template <typename S>
+void launch_refine_vectors(int n, int m, int nb, const S* work, const S* W, cx<double>* Xout, double* grad,
+                           const DevParams& P, const double* d_k, const int* d_G, int batch, cudaStream_t s);
 
 }  // namespace uepm
