@@ -271,7 +271,7 @@ def test_real_kernels_are_chosen_exactly_when_h_is_real(gpu, oracle, mats):
     G = oracle.generate_basis(8)
     assert _ctx(mats["Si-CB"], G, False, False).real
     assert _ctx(mats["Si-d"], G, True, False).real
-    assert not _ctx(mats["Si-CB"], G, False, True).real  # SOC blocks are complex
+    assert not _ctx(mats["Si"], G, False, True).real  # SOC blocks are complex
     assert not _ctx(mats["GaAs"], G, False, False).real  # antisymmetric form factors
     assert not _ctx(mats["InP"], G, True, False).real
     assert not _ctx(mats["Si-CB"], G, False, False, force_complex=True).real

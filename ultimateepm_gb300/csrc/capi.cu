@@ -301,7 +301,7 @@ void run_chunk(uepm_ctx* ctx, const Layout& L, char* ws, const double* kk, int c
         ProfScope p(ctx, s, KK_REFINE_PROJECT);
         launch_refine_project<S>(H, n, n, mstride, X32, m, rw, small, c, s);
     }
-    S* W = small + (size_t)4 * m * m * c;
+    S* W = small + (size_t)2 * m * m;  // W block of the first matrix; matrices are refine_small_elems apart
     {
         ProfScope p(ctx, s, KK_SMALL_EIGH);
         launch_small_eigh<S>(small, m, nb, E, vec ? W : nullptr, st, c, s);

@@ -5,10 +5,8 @@
 // in FP64
 //   k_refine_project   Y = H X, S = X^H X, A = X^H Y            (one CTA per matrix)
 //   k_small_eigh       the m x m pencil A c = lambda S c: Cholesky S = L L^H, C = L^-1 A L^-H,
-//                      cyclic Jacobi on C, ascending sort, W = L^-H V   (one THREAD per matrix:
-//                      GB300's FP64 pipe costs the same per warp instruction whatever the lane mask,
-//                      so the small dense solve runs 32 matrices per warp instead of one matrix per
-//                      warp)
+//                      parallel cyclic Jacobi on C (m/2 disjoint rotations at a time), ascending
+//                      sort, W = L^-H V   (one warp per matrix, all in shared memory)
 //   k_refine_vectors   Ritz vectors X W and their Hellmann-Feynman gradients (on request)
 // Ritz values err by about ||H x - lambda x||^2 / gap, where the gap is to the first eigenvalue
 // outside the subspace; the guard bands keep that gap open.
@@ -22,8 +20,6 @@ namespace uepm {
 
 constexpr int kProjNT = 256;
 
-// interleaved small-matrix storage: element e of matrix b at base[e * batch + b]
-#define SM(base, e) (base)[(size_t)(e) * batch + b]
 
 template <typename S>
 __global__ void __launch_bounds__(kProjNT) k_refine_project(const S* __restrict__ H, int n, int ld, size_t mstride,
@@ -67,8 +63,8 @@ __global__ void __launch_bounds__(kProjNT) k_refine_project(const S* __restrict_
     }
     __syncthreads();
     // S = X^H X and A = X^H Y, upper triangles (p <= q) only
-    S*        Sg = small;
-    S*        Ag = small + (size_t)m * m * batch;
+    S*        Sg = small + (size_t)b * refine_small_elems(m, 0);
+    S*        Ag = Sg + (size_t)m * m;
     const int np = m * (m + 1) / 2;
     for (int k = tid; k < np; k += kProjNT) {
         int p = 0, rest = k;
@@ -83,139 +79,223 @@ __global__ void __launch_bounds__(kProjNT) k_refine_project(const S* __restrict_
             s          = cfmac(xp, X[(size_t)r * m + q], s);
             a          = cfmac(xp, Y[(size_t)r * m + q], a);
         }
-        SM(Sg, p * m + q) = s;
-        SM(Ag, p * m + q) = a;
-        SM(Sg, q * m + p) = ST<S>::conj(s);
-        SM(Ag, q * m + p) = ST<S>::conj(a);
+        Sg[p * m + q] = s;
+        Ag[p * m + q] = a;
+        Sg[q * m + p] = ST<S>::conj(s);
+        Ag[q * m + p] = ST<S>::conj(a);
     }
 }
 
-// One thread per matrix. small = [S | A | M | C] (m x m each, interleaved), W = m x nb (interleaved).
+// One WARP per matrix; L, C and V live in shared memory. small = [S | A | W] per matrix, contiguous.
+// The Jacobi sweeps rotate m/2 disjoint pairs at once (round-robin tournament order), the lanes of
+// the warp computing the pairs' rotations and then sharing the row/column updates, so FP64
+// instructions are issued with most lanes busy.
+constexpr int kSmallWarps = 2;
+
 template <typename S>
-__global__ void k_small_eigh(S* __restrict__ small, int m, int nb, double* __restrict__ Eout, S* __restrict__ Wout,
-                             int* __restrict__ status, int batch) {
-    using R     = double;
-    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+__global__ void __launch_bounds__(32 * kSmallWarps) k_small_eigh(S* __restrict__ small, int m, int nb, double* __restrict__ Eout,
+                                                                 int want_w, int* __restrict__ status, int batch) {
+    using R         = double;
+    const int warp  = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int b     = blockIdx.x * kSmallWarps + warp;
+    const int mp    = m + 1;                       // padded row length
+    const int me    = (m + 1) & ~1;                // m rounded up to even (tournament size)
+    extern __shared__ __align__(16) unsigned char smraw[];
+    const size_t per = (size_t)3 * m * mp;
+    S*  L    = reinterpret_cast<S*>(smraw) + (size_t)warp * (per + 2 * me);
+    S*  Cm   = L + (size_t)m * mp;
+    S*  V    = Cm + (size_t)m * mp;
+    S*  rotc = V + (size_t)m * mp;  // per pair: (c, s) packed as re parts
+    S*  rote = rotc + me;           // per pair: the unit phase e (or +-1)
     if (b >= batch) return;
-    S*   Sg  = small;                              // S, then L (lower)
-    S*   Ag  = small + (size_t)m * m * batch;      // A, then the Jacobi matrix C
-    S*   Mg  = small + (size_t)2 * m * m * batch;  // M = L^-1 A, then V
-    S*   Cg  = small + (size_t)3 * m * m * batch;  // C before symmetrisation
-    bool bad = false;
-    // Cholesky S = L L^H
+    S*       Sg  = small + (size_t)b * refine_small_elems(m, nb);
+    const S* Ag  = Sg + (size_t)m * m;
+    S*       Wg  = Sg + (size_t)2 * m * m;
+    bool     bad = false;
+#define LL(i, j) L[(size_t)(i) * mp + (j)]
+#define CC(i, j) Cm[(size_t)(i) * mp + (j)]
+#define VV(i, j) V[(size_t)(i) * mp + (j)]
+    for (int q = lane; q < m * m; q += 32) {
+        const int i = q / m, j = q - i * m;
+        LL(i, j)    = Sg[q];
+        VV(i, j)    = Ag[q];  // A, overwritten below
+    }
+    __syncwarp();
+    // Cholesky S = L L^H (lanes over rows)
     for (int k = 0; k < m; ++k) {
-        R dkk = ST<S>::re(SM(Sg, k * m + k));
-        for (int j = 0; j < k; ++j) dkk -= ST<S>::norm(SM(Sg, k * m + j));
+        R dkk = ST<S>::re(LL(k, k));
+        for (int j = 0; j < k; ++j) dkk -= ST<S>::norm(LL(k, j));
         if (!(dkk > 0.0)) {
             bad = true;
             dkk = 1.0;
         }
         const R lkk = sqrt(dkk), il = 1.0 / lkk;
-        SM(Sg, k * m + k) = ST<S>::make(lkk, 0.0);
-        for (int i = k + 1; i < m; ++i) {
-            S s = SM(Sg, i * m + k);
-            for (int j = 0; j < k; ++j) s = cfms_conjb(SM(Sg, i * m + j), SM(Sg, k * m + j), s);
-            SM(Sg, i * m + k) = cscale(s, il);
+        __syncwarp();
+        for (int i = k + 1 + lane; i < m; i += 32) {
+            S s = LL(i, k);
+            for (int j = 0; j < k; ++j) s = cfms_conjb(LL(i, j), LL(k, j), s);
+            LL(i, k) = cscale(s, il);
+        }
+        __syncwarp();
+        if (lane == 0) LL(k, k) = ST<S>::make(lkk, 0.0);
+        __syncwarp();
+    }
+    // M = L^-1 A into C (lanes over columns), then C = L^-1 M^H into V's place... keep M in C,
+    // write L^-1 M^H into V, then copy back to C after symmetrising.
+    for (int c = lane; c < m; c += 32)
+        for (int i = 0; i < m; ++i) {
+            S s = VV(i, c);
+            for (int j = 0; j < i; ++j) s = cfma(ST<S>::neg(LL(i, j)), CC(j, c), s);
+            CC(i, c) = cscale(s, 1.0 / ST<S>::re(LL(i, i)));
+        }
+    __syncwarp();
+    for (int c = lane; c < m; c += 32)
+        for (int i = 0; i < m; ++i) {
+            S s = ST<S>::conj(CC(c, i));
+            for (int j = 0; j < i; ++j) s = cfma(ST<S>::neg(LL(i, j)), VV(j, c), s);
+            VV(i, c) = cscale(s, 1.0 / ST<S>::re(LL(i, i)));
+        }
+    __syncwarp();
+    // C = (V + V^H) / 2, V = I
+    for (int q = lane; q < m * m; q += 32) {
+        const int i = q / m, c = q - i * m;
+        if (i <= c) {
+            const S u = VV(i, c), l = VV(c, i);
+            const S h = ST<S>::make(0.5 * (ST<S>::re(u) + ST<S>::re(l)), i == c ? 0.0 : 0.5 * (ST<S>::im(u) - ST<S>::im(l)));
+            CC(i, c)  = h;
+            CC(c, i)  = ST<S>::conj(h);
         }
     }
-    // M = L^-1 A
-    for (int c = 0; c < m; ++c)
-        for (int i = 0; i < m; ++i) {
-            S s = SM(Ag, i * m + c);
-            for (int j = 0; j < i; ++j) s = cfma(ST<S>::neg(SM(Sg, i * m + j)), SM(Mg, j * m + c), s);
-            SM(Mg, i * m + c) = cscale(s, 1.0 / ST<S>::re(SM(Sg, i * m + i)));
+    __syncwarp();
+    for (int q = lane; q < m * m; q += 32) {
+        const int i = q / m, c = q - i * m;
+        VV(i, c)    = (i == c) ? ST<S>::one() : ST<S>::zero();
+    }
+    __syncwarp();
+    // parallel cyclic Jacobi: me - 1 rounds of me / 2 disjoint pairs per sweep
+    const int npair = me / 2;
+    for (int sweep = 0; sweep < 10; ++sweep) {
+        R off = 0, dia = 0;
+        for (int q = lane; q < m * m; q += 32) {
+            const int i = q / m, c = q - i * m;
+            if (i < c) off = fmax(off, sqrt(ST<S>::norm(CC(i, c))));
+            if (i == c) dia = fmax(dia, fabs(ST<S>::re(CC(i, i))));
         }
-    // C = L^-1 M^H (Hermitian)
-    for (int c = 0; c < m; ++c)
-        for (int i = 0; i < m; ++i) {
-            S s = ST<S>::conj(SM(Mg, c * m + i));
-            for (int j = 0; j < i; ++j) s = cfma(ST<S>::neg(SM(Sg, i * m + j)), SM(Cg, j * m + c), s);
-            SM(Cg, i * m + c) = cscale(s, 1.0 / ST<S>::re(SM(Sg, i * m + i)));
-        }
-    // symmetrise C into Ag; V = I into Mg
-    for (int i = 0; i < m; ++i)
-        for (int c = 0; c < m; ++c) {
-            if (i < c) {
-                const S u = SM(Cg, i * m + c), l = SM(Cg, c * m + i);
-                const S h = ST<S>::make(0.5 * (ST<S>::re(u) + ST<S>::re(l)), 0.5 * (ST<S>::im(u) - ST<S>::im(l)));
-                SM(Ag, i * m + c) = h;
-                SM(Ag, c * m + i) = ST<S>::conj(h);
-            } else if (i == c) {
-                SM(Ag, i * m + i) = ST<S>::make(ST<S>::re(SM(Cg, i * m + i)), 0.0);
+        off = warp_max(off);
+        dia = warp_max(dia);
+        if (off <= 1e-17 * dia || off == 0.0) break;
+        for (int round = 0; round < me - 1; ++round) {
+            // tournament pairing: slot 0 fixed, slots 1..me-1 rotate
+            if (lane < npair) {
+                const int a0 = (lane == 0) ? 0 : ((lane - 1 + round) % (me - 1)) + 1;
+                const int a1 = ((me - 2 - lane + round) % (me - 1)) + 1;
+                const int p = min(a0, a1), q = max(a0, a1);
+                R         cc = 1.0, ss = 0.0, ex = 1.0, ey = 0.0;
+                if (q < m) {
+                    const S bpq = CC(p, q);
+                    const R ab  = sqrt(ST<S>::norm(bpq));
+                    const R a = ST<S>::re(CC(p, p)), d = ST<S>::re(CC(q, q));
+                    if (ab > 1e-18 * (fabs(a) + fabs(d)) && ab != 0.0) {
+                        const R tau = (d - a) / (2.0 * ab);
+                        const R t   = (tau >= 0.0 ? 1.0 : -1.0) / (fabs(tau) + sqrt(1.0 + tau * tau));
+                        cc          = 1.0 / sqrt(1.0 + t * t);
+                        ss          = t * cc;
+                        ex          = ST<S>::re(bpq) / ab;
+                        ey          = ST<S>::im(bpq) / ab;
+                    }
+                }
+                rotc[lane] = ST<S>::make(cc, ss);
+                rote[lane] = ST<S>::make(ex, ey);
             }
-            SM(Mg, i * m + c) = (i == c) ? ST<S>::one() : ST<S>::zero();
-        }
-    // cyclic Jacobi; a sweep without any rotation ends it (at most 12 sweeps)
-    for (int sweep = 0; sweep < 12; ++sweep) {
-        int rot = 0;
-        for (int p = 0; p < m - 1; ++p)
-            for (int q = p + 1; q < m; ++q) {
-                const S bpq = SM(Ag, p * m + q);
-                const R a = ST<S>::re(SM(Ag, p * m + p)), d = ST<S>::re(SM(Ag, q * m + q));
-                const R ab = sqrt(ST<S>::norm(bpq));
-                if (ab <= 1e-18 * (fabs(a) + fabs(d)) || ab == 0.0) continue;
-                ++rot;
-                const R tau = (d - a) / (2.0 * ab);
-                const R t   = (tau >= 0.0 ? 1.0 : -1.0) / (fabs(tau) + sqrt(1.0 + tau * tau));
-                const R c   = 1.0 / sqrt(1.0 + t * t), s = t * c;
-                const R ex = ST<S>::re(bpq) / ab, ey = ST<S>::im(bpq) / ab;  // b = |b| e
-                // J = [[c, s], [-s conj(e), c conj(e)]] on columns p, q: C <- J^H C J, V <- V J
+            __syncwarp();
+            // columns: C <- C J, V <- V J  (work items: pair x row)
+            for (int it = lane; it < npair * m; it += 32) {
+                const int k = it / m, r = it - k * m;
+                const int a0 = (k == 0) ? 0 : ((k - 1 + round) % (me - 1)) + 1;
+                const int a1 = ((me - 2 - k + round) % (me - 1)) + 1;
+                const int p = min(a0, a1), q = max(a0, a1);
+                if (q >= m) continue;
+                const R c = ST<S>::re(rotc[k]), s = ST<S>::im(rotc[k]);
+                if (s == 0.0 && c == 1.0) continue;
+                const R ex = ST<S>::re(rote[k]), ey = ST<S>::im(rote[k]);
                 const S jqp = ST<S>::make(-s * ex, s * ey);
                 const S jqq = ST<S>::make(c * ex, -c * ey);
-                for (int r = 0; r < m; ++r) {
-                    const S cp = SM(Ag, r * m + p), cq = SM(Ag, r * m + q);
-                    SM(Ag, r * m + p) = cfma(cq, jqp, cscale(cp, c));
-                    SM(Ag, r * m + q) = cfma(cq, jqq, cscale(cp, s));
-                    const S vp = SM(Mg, r * m + p), vq = SM(Mg, r * m + q);
-                    SM(Mg, r * m + p) = cfma(vq, jqp, cscale(vp, c));
-                    SM(Mg, r * m + q) = cfma(vq, jqq, cscale(vp, s));
+                const S cp = CC(r, p), cq = CC(r, q);
+                CC(r, p) = cfma(cq, jqp, cscale(cp, c));
+                CC(r, q) = cfma(cq, jqq, cscale(cp, s));
+                const S vp = VV(r, p), vq = VV(r, q);
+                VV(r, p) = cfma(vq, jqp, cscale(vp, c));
+                VV(r, q) = cfma(vq, jqq, cscale(vp, s));
+            }
+            __syncwarp();
+            // rows: C <- J^H C
+            for (int it = lane; it < npair * m; it += 32) {
+                const int k = it / m, r = it - k * m;
+                const int a0 = (k == 0) ? 0 : ((k - 1 + round) % (me - 1)) + 1;
+                const int a1 = ((me - 2 - k + round) % (me - 1)) + 1;
+                const int p = min(a0, a1), q = max(a0, a1);
+                if (q >= m) continue;
+                const R c = ST<S>::re(rotc[k]), s = ST<S>::im(rotc[k]);
+                if (s == 0.0 && c == 1.0) continue;
+                const R ex = ST<S>::re(rote[k]), ey = ST<S>::im(rote[k]);
+                const S jqp = ST<S>::make(-s * ex, s * ey);
+                const S jqq = ST<S>::make(c * ex, -c * ey);
+                const S cp = CC(p, r), cq = CC(q, r);
+                CC(p, r) = cfma(ST<S>::conj(jqp), cq, cscale(cp, c));
+                CC(q, r) = cfma(ST<S>::conj(jqq), cq, cscale(cp, s));
+            }
+            __syncwarp();
+            if (lane < npair) {
+                const int a0 = (lane == 0) ? 0 : ((lane - 1 + round) % (me - 1)) + 1;
+                const int a1 = ((me - 2 - lane + round) % (me - 1)) + 1;
+                const int p = min(a0, a1), q = max(a0, a1);
+                if (q < m && !(ST<S>::im(rotc[lane]) == 0.0 && ST<S>::re(rotc[lane]) == 1.0)) {
+                    CC(p, q) = ST<S>::zero();
+                    CC(q, p) = ST<S>::zero();
+                    CC(p, p) = ST<S>::make(ST<S>::re(CC(p, p)), 0.0);
+                    CC(q, q) = ST<S>::make(ST<S>::re(CC(q, q)), 0.0);
                 }
-                for (int r = 0; r < m; ++r) {
-                    const S cp = SM(Ag, p * m + r), cq = SM(Ag, q * m + r);
-                    SM(Ag, p * m + r) = cfma(ST<S>::conj(jqp), cq, cscale(cp, c));
-                    SM(Ag, q * m + r) = cfma(ST<S>::conj(jqq), cq, cscale(cp, s));
-                }
-                SM(Ag, p * m + q) = ST<S>::zero();
-                SM(Ag, q * m + p) = ST<S>::zero();
-                SM(Ag, p * m + p) = ST<S>::make(ST<S>::re(SM(Ag, p * m + p)), 0.0);
-                SM(Ag, q * m + q) = ST<S>::make(ST<S>::re(SM(Ag, q * m + q)), 0.0);
             }
-        if (rot == 0) break;
-    }
-    // the nb smallest Ritz values in ascending order (selection), with their columns of V
-    for (int j = 0; j < nb; ++j) {
-        int kmin = j;
-        R   emin = ST<S>::re(SM(Ag, j * m + j));
-        for (int q = j + 1; q < m; ++q) {
-            const R eq = ST<S>::re(SM(Ag, q * m + q));
-            if (eq < emin) {
-                emin = eq;
-                kmin = q;
-            }
+            __syncwarp();
         }
-        if (kmin != j) {
-            const S t = SM(Ag, j * m + j);
-            SM(Ag, j * m + j) = SM(Ag, kmin * m + kmin);
-            SM(Ag, kmin * m + kmin) = t;
-            for (int r = 0; r < m; ++r) {
-                const S v = SM(Mg, r * m + j);
-                SM(Mg, r * m + j) = SM(Mg, r * m + kmin);
-                SM(Mg, r * m + kmin) = v;
-            }
-        }
-        Eout[(size_t)b * nb + j] = emin;
-        if (!isfinite(emin)) bad = true;
     }
-    // W = L^-H V[:, :nb] (back substitution with L^H)
-    if (Wout) {
-        for (int c = 0; c < nb; ++c)
+    // ascending order of the Ritz values (lane 0), nb smallest out
+    int* ord = reinterpret_cast<int*>(rotc);  // reuse: me >= m ints fit in me scalars
+    if (lane == 0) {
+        for (int i = 0; i < m; ++i) ord[i] = i;
+        for (int i = 1; i < m; ++i) {
+            const int o = ord[i];
+            const R   ev = ST<S>::re(CC(o, o));
+            int       k  = i - 1;
+            while (k >= 0 && ST<S>::re(CC(ord[k], ord[k])) > ev) {
+                ord[k + 1] = ord[k];
+                --k;
+            }
+            ord[k + 1] = o;
+        }
+    }
+    __syncwarp();
+    for (int j = lane; j < nb; j += 32) {
+        const R ev = ST<S>::re(CC(ord[j], ord[j]));
+        Eout[(size_t)b * nb + j] = ev;
+        if (!isfinite(ev)) bad = true;
+    }
+    // W = L^-H V[:, ord[:nb]] (back substitution with L^H), lanes over columns
+    if (want_w) {
+        for (int c = lane; c < nb; c += 32) {
+            const int oc = ord[c];
             for (int i = m - 1; i >= 0; --i) {
-                S s = SM(Mg, i * m + c);
-                for (int j = i + 1; j < m; ++j) s = cfms_conjb(SM(Wout, j * nb + c), SM(Sg, j * m + i), s);
-                SM(Wout, i * nb + c) = cscale(s, 1.0 / ST<S>::re(SM(Sg, i * m + i)));
+                S s = VV(i, oc);
+                for (int j = i + 1; j < m; ++j) s = cfms_conjb(Wg[(size_t)j * nb + c], LL(j, i), s);
+                Wg[(size_t)i * nb + c] = cscale(s, 1.0 / ST<S>::re(LL(i, i)));
             }
+        }
     }
-    if (bad && status) atomicOr(status + b, 2);
+    bad = __any_sync(0xffffffffu, bad);
+    if (bad && lane == 0 && status) atomicOr(status + b, 2);
+#undef LL
+#undef CC
+#undef VV
 }
 
 // Ritz vectors x_j = X W[:, j] and gradients; one CTA per matrix, one warp per band.
@@ -227,11 +307,12 @@ __global__ void k_refine_vectors(int n, int m, int nb, const S* __restrict__ wor
     if (b >= batch) return;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
     const S*  X    = work + (size_t)b * refine_work_elems(n, m);
+    const S*  Wb   = Wg + (size_t)b * refine_small_elems(m, nb);
     for (int j = warp; j < nb; j += nw) {
         double sx = 0, sy = 0, sz = 0;
         for (int r = lane; r < n; r += 32) {
             S x = ST<S>::zero();
-            for (int q = 0; q < m; ++q) x = cfma(X[(size_t)r * m + q], SM(Wg, q * nb + j), x);
+            for (int q = 0; q < m; ++q) x = cfma(X[(size_t)r * m + q], Wb[(size_t)q * nb + j], x);
             if (Xout) stc(Xout + ((size_t)b * nb + j) * n + r, mk<double>(ST<S>::re(x), ST<S>::im(x)));
             if (grad) {
                 const double* k  = kpts + 3 * (size_t)b;
@@ -255,7 +336,6 @@ __global__ void k_refine_vectors(int n, int m, int nb, const S* __restrict__ wor
         }
     }
 }
-#undef SM
 
 template <typename S>
 void launch_refine_project(const S* H, int n, int ld, size_t mstride, const cx<float>* X32, int m, S* work, S* small,
@@ -266,7 +346,12 @@ void launch_refine_project(const S* H, int n, int ld, size_t mstride, const cx<f
 
 template <typename S>
 void launch_small_eigh(S* small, int m, int nb, double* Eout, S* W, int* status, int batch, cudaStream_t s) {
-    k_small_eigh<S><<<(batch + 63) / 64, 64, 0, s>>>(small, m, nb, Eout, W, status, batch);
+    const int    me   = (m + 1) & ~1;
+    const size_t smem = sizeof(S) * ((size_t)3 * m * (m + 1) + 2 * me) * kSmallWarps;
+    auto         kern = k_small_eigh<S>;
+    if (smem > 48 * 1024) cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    kern<<<(batch + kSmallWarps - 1) / kSmallWarps, 32 * kSmallWarps, smem, s>>>(small, m, nb, Eout, W != nullptr, status,
+                                                                              batch);
     count_launch();
 }
 

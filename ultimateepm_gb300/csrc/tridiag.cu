@@ -27,17 +27,23 @@
 
 namespace uepm {
 
-template <typename S, int NT, int MAXT>
-__global__ void __launch_bounds__(NT) k_tridiag(S* __restrict__ H, int n, int ld, size_t mstride,
+// SMEM = true: the matrix is copied into shared memory (leading dimension n | 1, odd, so that the
+// mirrored row-wise stores do not collide on banks), reduced there, and its reflector columns are
+// written back. Used where n x n fits (the FP32 reductions of the mixed path), because those are
+// bound by memory latency rather than by arithmetic.
+template <typename S, int NT, int MAXT, bool SMEM>
+__global__ void __launch_bounds__(NT) k_tridiag(S* __restrict__ H, int n, int ldg, size_t mstride,
                                                 typename ST<S>::R* __restrict__ dOut, typename ST<S>::R* __restrict__ eOut,
                                                 S* __restrict__ tqOut, int* __restrict__ status, int batch) {
     using R       = typename ST<S>::R;
     constexpr int NW = NT / 32;
     const int     b  = blockIdx.x;
     if (b >= batch) return;
-    S* A = H + (size_t)b * mstride;
+    S*        Ag  = H + (size_t)b * mstride;
+    const int lds = n | 1;
     extern __shared__ __align__(16) unsigned char smraw[];
-    S*        v    = reinterpret_cast<S*>(smraw);  // n
+    S*        As   = reinterpret_cast<S*>(smraw);  // SMEM: n x lds
+    S*        v    = SMEM ? As + (size_t)n * lds : As;  // n
     S*        w    = v + n;                        // n
     S*        pacc = w + n;                        // NW * n
     R*        red  = reinterpret_cast<R*>(pacc + NW * n);  // 3 * NW
@@ -45,6 +51,15 @@ __global__ void __launch_bounds__(NT) k_tridiag(S* __restrict__ H, int n, int ld
     __shared__ int s_skip;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     bool      bad = false;
+    S*        A   = SMEM ? As : Ag;
+    const int ld  = SMEM ? lds : ldg;
+    if (SMEM) {
+        for (int q = tid; q < n * n; q += NT) {
+            const int c = q / n, r = q - c * n;
+            As[(size_t)c * lds + r] = Ag[(size_t)c * ldg + r];
+        }
+        __syncthreads();
+    }
 
     for (int i = 0; i < n - 1; ++i) {
         const int o = i + 1, m = n - o;
@@ -179,29 +194,50 @@ __global__ void __launch_bounds__(NT) k_tridiag(S* __restrict__ H, int n, int ld
         if (!isfinite(dl)) bad = true;
         if (bad && status) atomicOr(status + b, 2);  // UEPM_K_NONFINITE
     }
+    if (SMEM) {
+        // reflector tails (column i, rows i+2..n-1) for the back-transformation
+        __syncthreads();
+        for (int q = tid; q < n * n; q += NT) {
+            const int c = q / n, r = q - c * n;
+            if (r > c + 1) Ag[(size_t)c * ldg + r] = As[(size_t)c * lds + r];
+        }
+    }
 }
 
-template <typename S, int NT, int MAXT>
+template <typename S, int NT, int MAXT, bool SMEM>
 static void tridiag_launch_t(S* H, int n, int ld, size_t mstride, typename ST<S>::R* d, typename ST<S>::R* e, S* tq,
                              int* status, int batch, cudaStream_t s) {
     using R           = typename ST<S>::R;
-    const size_t smem = sizeof(S) * (size_t)(2 + NT / 32) * n + sizeof(R) * 3 * (NT / 32);
-    auto         kern = k_tridiag<S, NT, MAXT>;
+    const size_t smem = sizeof(S) * ((SMEM ? (size_t)n * (n | 1) : 0) + (size_t)(2 + NT / 32) * n) + sizeof(R) * 3 * (NT / 32);
+    auto         kern = k_tridiag<S, NT, MAXT, SMEM>;
     if (smem > 48 * 1024) cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     kern<<<batch, NT, smem, s>>>(H, n, ld, mstride, d, e, tq, status, batch);
     count_launch();
+}
+
+// Shared-memory residency: FP32 matrices whose n x n copy (plus vectors) fits in 200 KB.
+template <typename S>
+static bool use_smem(int n) {
+    using R = typename ST<S>::R;
+    return sizeof(R) == 4 && sizeof(S) * ((size_t)n * (n | 1) + (size_t)10 * n) <= 200 * 1024;
+}
+
+template <typename S, int MAXT>
+static void tridiag_pick(S* H, int n, int ld, size_t mstride, typename ST<S>::R* d, typename ST<S>::R* e, S* tq,
+                         int* status, int batch, cudaStream_t s) {
+    if (use_smem<S>(n)) tridiag_launch_t<S, 256, MAXT, true>(H, n, ld, mstride, d, e, tq, status, batch, s);
+    else tridiag_launch_t<S, 128, MAXT, false>(H, n, ld, mstride, d, e, tq, status, batch, s);
 }
 
 template <typename S>
 void launch_tridiag(S* H, int n, int ld, size_t mstride, typename ST<S>::R* d, typename ST<S>::R* e, S* tq, int* status,
                     int batch, cudaStream_t s) {
     // rows of the trailing matrix are at most n - 1 <= 32 * MAXT
-    constexpr int NT = 128;
-    if (n <= 129) tridiag_launch_t<S, NT, 4>(H, n, ld, mstride, d, e, tq, status, batch, s);
-    else if (n <= 161) tridiag_launch_t<S, NT, 5>(H, n, ld, mstride, d, e, tq, status, batch, s);
-    else if (n <= 257) tridiag_launch_t<S, NT, 8>(H, n, ld, mstride, d, e, tq, status, batch, s);
-    else if (n <= 385) tridiag_launch_t<S, NT, 12>(H, n, ld, mstride, d, e, tq, status, batch, s);
-    else tridiag_launch_t<S, NT, 16>(H, n, ld, mstride, d, e, tq, status, batch, s);
+    if (n <= 129) tridiag_pick<S, 4>(H, n, ld, mstride, d, e, tq, status, batch, s);
+    else if (n <= 161) tridiag_pick<S, 5>(H, n, ld, mstride, d, e, tq, status, batch, s);
+    else if (n <= 257) tridiag_pick<S, 8>(H, n, ld, mstride, d, e, tq, status, batch, s);
+    else if (n <= 385) tridiag_pick<S, 12>(H, n, ld, mstride, d, e, tq, status, batch, s);
+    else tridiag_pick<S, 16>(H, n, ld, mstride, d, e, tq, status, batch, s);
 }
 
 template void launch_tridiag<cx<double>>(cx<double>*, int, int, size_t, double*, double*, cx<double>*, int*, int, cudaStream_t);

@@ -48,8 +48,9 @@ void launch_backtransform(const S* H, int n, int ld, size_t mstride, const S* tq
 // the nb lowest Ritz values go to Eout, optionally vectors / gradients.
 constexpr int kRefineMaxSubspace = 40;
 __host__ __device__ inline size_t refine_work_elems(int n, int m) { return (size_t)2 * n * m; }
-// small-solve scratch per matrix: 4 m x m blocks plus the m x nb Ritz coefficients
-__host__ __device__ inline size_t refine_small_elems(int m, int nb) { return (size_t)4 * m * m + (size_t)m * nb; }
+// small-solve scratch per matrix, contiguous: S (m x m), A (m x m), then the m x nb (<= m x m) Ritz
+// coefficients W at offset 2 m^2
+__host__ __device__ inline size_t refine_small_elems(int m, int) { return (size_t)3 * m * m; }
 template <typename S>
 void launch_refine_project(const S* H, int n, int ld, size_t mstride, const cx<float>* X32, int m, S* work, S* small,
                            int batch, cudaStream_t s);
