@@ -92,6 +92,13 @@ __global__ void __launch_bounds__(kProjNT) k_refine_project(const S* __restrict_
 // instructions are issued with most lanes busy.
 constexpr int kSmallWarps = 2;
 
+// shared memory of one warp's matrix: L, C, V (m x (m+1) scalars each) and 4 rotation arrays
+template <typename S>
+__host__ __device__ inline size_t small_eigh_warp_bytes(int m) {
+    const int me = (m + 1) & ~1;
+    return (sizeof(S) * 3 * (size_t)m * (m + 1) + sizeof(double) * 4 * (size_t)me + 15) & ~(size_t)15;
+}
+
 template <typename S>
 __global__ void __launch_bounds__(32 * kSmallWarps) k_small_eigh(S* __restrict__ small, int m, int nb, double* __restrict__ Eout,
                                                                  int want_w, int* __restrict__ status, int batch) {
@@ -101,12 +108,13 @@ __global__ void __launch_bounds__(32 * kSmallWarps) k_small_eigh(S* __restrict__
     const int mp    = m + 1;                       // padded row length
     const int me    = (m + 1) & ~1;                // m rounded up to even (tournament size)
     extern __shared__ __align__(16) unsigned char smraw[];
-    const size_t per = (size_t)3 * m * mp;
-    S*  L    = reinterpret_cast<S*>(smraw) + (size_t)warp * (per + 2 * me);
+    S*  L    = reinterpret_cast<S*>(smraw + (size_t)warp * small_eigh_warp_bytes<S>(m));
     S*  Cm   = L + (size_t)m * mp;
     S*  V    = Cm + (size_t)m * mp;
-    S*  rotc = V + (size_t)m * mp;  // per pair: (c, s) packed as re parts
-    S*  rote = rotc + me;           // per pair: the unit phase e (or +-1)
+    R*  rc   = reinterpret_cast<R*>(V + (size_t)m * mp);  // per pair: cosine
+    R*  rs   = rc + me;                                   // sine
+    R*  rex  = rs + me;                                   // unit phase e of the off-diagonal (re, im)
+    R*  rey  = rex + me;
     if (b >= batch) return;
     S*       Sg  = small + (size_t)b * refine_small_elems(m, nb);
     const S* Ag  = Sg + (size_t)m * m;
@@ -204,8 +212,10 @@ __global__ void __launch_bounds__(32 * kSmallWarps) k_small_eigh(S* __restrict__
                         ey          = ST<S>::im(bpq) / ab;
                     }
                 }
-                rotc[lane] = ST<S>::make(cc, ss);
-                rote[lane] = ST<S>::make(ex, ey);
+                rc[lane]  = cc;
+                rs[lane]  = ss;
+                rex[lane] = ex;
+                rey[lane] = ey;
             }
             __syncwarp();
             // columns: C <- C J, V <- V J  (work items: pair x row)
@@ -215,9 +225,9 @@ __global__ void __launch_bounds__(32 * kSmallWarps) k_small_eigh(S* __restrict__
                 const int a1 = ((me - 2 - k + round) % (me - 1)) + 1;
                 const int p = min(a0, a1), q = max(a0, a1);
                 if (q >= m) continue;
-                const R c = ST<S>::re(rotc[k]), s = ST<S>::im(rotc[k]);
+                const R c = rc[k], s = rs[k];
                 if (s == 0.0 && c == 1.0) continue;
-                const R ex = ST<S>::re(rote[k]), ey = ST<S>::im(rote[k]);
+                const R ex = rex[k], ey = rey[k];
                 const S jqp = ST<S>::make(-s * ex, s * ey);
                 const S jqq = ST<S>::make(c * ex, -c * ey);
                 const S cp = CC(r, p), cq = CC(r, q);
@@ -235,9 +245,9 @@ __global__ void __launch_bounds__(32 * kSmallWarps) k_small_eigh(S* __restrict__
                 const int a1 = ((me - 2 - k + round) % (me - 1)) + 1;
                 const int p = min(a0, a1), q = max(a0, a1);
                 if (q >= m) continue;
-                const R c = ST<S>::re(rotc[k]), s = ST<S>::im(rotc[k]);
+                const R c = rc[k], s = rs[k];
                 if (s == 0.0 && c == 1.0) continue;
-                const R ex = ST<S>::re(rote[k]), ey = ST<S>::im(rote[k]);
+                const R ex = rex[k], ey = rey[k];
                 const S jqp = ST<S>::make(-s * ex, s * ey);
                 const S jqq = ST<S>::make(c * ex, -c * ey);
                 const S cp = CC(p, r), cq = CC(q, r);
@@ -249,7 +259,7 @@ __global__ void __launch_bounds__(32 * kSmallWarps) k_small_eigh(S* __restrict__
                 const int a0 = (lane == 0) ? 0 : ((lane - 1 + round) % (me - 1)) + 1;
                 const int a1 = ((me - 2 - lane + round) % (me - 1)) + 1;
                 const int p = min(a0, a1), q = max(a0, a1);
-                if (q < m && !(ST<S>::im(rotc[lane]) == 0.0 && ST<S>::re(rotc[lane]) == 1.0)) {
+                if (q < m && !(rs[lane] == 0.0 && rc[lane] == 1.0)) {
                     CC(p, q) = ST<S>::zero();
                     CC(q, p) = ST<S>::zero();
                     CC(p, p) = ST<S>::make(ST<S>::re(CC(p, p)), 0.0);
@@ -260,7 +270,7 @@ __global__ void __launch_bounds__(32 * kSmallWarps) k_small_eigh(S* __restrict__
         }
     }
     // ascending order of the Ritz values (lane 0), nb smallest out
-    int* ord = reinterpret_cast<int*>(rotc);  // reuse: me >= m ints fit in me scalars
+    int* ord = reinterpret_cast<int*>(rc);  // reuse: 4 me doubles hold m ints
     if (lane == 0) {
         for (int i = 0; i < m; ++i) ord[i] = i;
         for (int i = 1; i < m; ++i) {
@@ -346,8 +356,7 @@ void launch_refine_project(const S* H, int n, int ld, size_t mstride, const cx<f
 
 template <typename S>
 void launch_small_eigh(S* small, int m, int nb, double* Eout, S* W, int* status, int batch, cudaStream_t s) {
-    const int    me   = (m + 1) & ~1;
-    const size_t smem = sizeof(S) * ((size_t)3 * m * (m + 1) + 2 * me) * kSmallWarps;
+    const size_t smem = small_eigh_warp_bytes<S>(m) * kSmallWarps;
     auto         kern = k_small_eigh<S>;
     if (smem > 48 * 1024) cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     kern<<<(batch + kSmallWarps - 1) / kSmallWarps, 32 * kSmallWarps, smem, s>>>(small, m, nb, Eout, W != nullptr, status,
