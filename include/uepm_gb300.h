@@ -139,6 +139,19 @@ int uepm_solve_device(uepm_ctx* ctx, const double* d_k, size_t nk, int nb, uint3
  * complex128, column-major per k, both triangles filled. Device buffers, enqueued on `stream`. */
 int uepm_assemble_device(uepm_ctx* ctx, const double* d_k, size_t nk, double* d_H, void* stream);
 
+/* H(k) assembly that allocates nothing (no counterpart in the reference). Same inputs, output and
+ * results as uepm_assemble_device, for callers that must not allocate device memory when they call
+ * (a serving loop with memory reserved at start-up, a host program whose device memory belongs to its
+ * own allocator): the per-plane-wave row table lives in a fixed 16 MiB device array of the library,
+ * present on every GPU that loads it until exit, instead of a workspace grown on demand. Limit:
+ * nk * N * 24 * 8 bytes <= UEPM_NOALLOC_SCRATCH_BYTES (e.g. 637 k-points per call for basis 137);
+ * larger requests fail with UEPM_ERR_INVALID. The first call on a device looks up the array's
+ * device address (with that device current) and should come before any stream capture. All calls
+ * share the array: calls that overlap on the GPU race. The context must have been created (which
+ * allocates) beforehand, with the same device current. */
+#define UEPM_NOALLOC_SCRATCH_BYTES (16u << 20)
+int uepm_assemble_device_noalloc(uepm_ctx* ctx, const double* d_k, size_t nk, double* d_H, void* stream);
+
 /* BandStructure::AdjustValues (FindBandGap + shift) on host E (nk x nb). Returns the gap via *gap
  * and whether FindBandGap succeeded via *found. soc selects 8 instead of 4 valence bands. */
 int uepm_adjust_values(double* E, size_t nk, int nb, int soc, int min_cond_zero, double* gap, int* found);

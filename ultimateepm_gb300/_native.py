@@ -34,8 +34,9 @@ EXPORTED = [
     "uepm_materials_load", "uepm_ctx_create", "uepm_ctx_destroy", "uepm_ctx_set_precision", "uepm_ctx_order",
     "uepm_ctx_set_workspace_limit", "uepm_solve", "uepm_solve_device", "uepm_assemble_device",
     "uepm_adjust_values", "uepm_kernel_launches", "uepm_ctx_set_profiling", "uepm_ctx_read_profile",
-    "uepm_kernel_name", "uepm_measure_peak", "uepm_ctx_force_complex",
+    "uepm_kernel_name", "uepm_measure_peak", "uepm_ctx_force_complex", "uepm_assemble_device_noalloc",
 ]
+NOALLOC_SCRATCH_BYTES = 16 << 20
 KERNEL_KINDS = 10
 
 
@@ -106,6 +107,7 @@ def load():
             "uepm_kernel_name": (C.c_char_p, [C.c_int]),
             "uepm_measure_peak": (C.c_int, [C.c_int, dp]),
             "uepm_ctx_force_complex": (C.c_int, [vp, C.c_int]),
+            "uepm_assemble_device_noalloc": (C.c_int, [vp, vp, C.c_size_t, vp, vp]),
         }
         for name, (res, args) in sig.items():
             f = getattr(L, name)

@@ -16,6 +16,7 @@
 #include <string>
 #include <vector>
 
+#include "ctx_view.h"
 #include "uepm_common.cuh"
 #include "uepm_gb300.h"
 #include "uepm_kernels.h"
@@ -79,6 +80,20 @@ struct uepm_ctx {
     double                   prof_ms[UEPM_KERNEL_KINDS] = {0};
     uint64_t                 prof_n[UEPM_KERNEL_KINDS]  = {0};
 };
+
+namespace uepm {
+bool ctx_tables(const uepm_ctx* ctx, CtxTables* out) {
+    if (!ctx || !out) return false;
+    out->P    = ctx->P;
+    out->d_G  = ctx->d_G;
+    out->Vloc = ctx->d_Vloc;
+    out->phNL = ctx->d_phNL;
+    out->phSO = ctx->d_phSO;
+    out->N    = ctx->N;
+    out->n    = ctx->n;
+    return true;
+}
+}  // namespace uepm
 
 namespace {
 
