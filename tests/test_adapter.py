@@ -1,0 +1,80 @@
+"""The C++ adapter (include/uepm/*.h, libuepm_epp.so): the reference's uepm::pseudopotential classes
+over the C ABI. CPU: it compiles and links, and the reference's own apps/EmpiricalPseudoPotentialMain.cpp
+compiles unchanged against it (where the reference tree exists). GPU: the driver's results match the
+oracle."""
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+from conftest import PARAMS, ROOT
+
+LIB = os.path.join(ROOT, "ultimateepm_gb300", "lib")
+INC = [f"-I{os.path.join(ROOT, 'include')}", f"-I{os.path.join(ROOT, 'include', 'uepm')}"]
+REF = "/root/reference"
+
+
+def _compile_driver(tmp_path):
+    exe = str(tmp_path / "adapter_driver")
+    cmd = ["g++", "-O2", "-std=c++20", *INC, os.path.join(ROOT, "tests", "cpp", "adapter_driver.cpp"), "-o", exe,
+           f"-L{LIB}", "-luepm_epp", "-luepm_gb300", f"-Wl,-rpath,{LIB}"]
+    subprocess.run(cmd, check=True, capture_output=True, text=True)
+    return exe
+
+
+def test_adapter_driver_compiles_and_links(native, tmp_path):
+    assert os.path.exists(_compile_driver(tmp_path))
+
+
+@pytest.mark.skipif(not os.path.isdir(os.path.join(REF, "apps")), reason="reference tree not present")
+def test_reference_app_compiles_unchanged_against_the_adapter(native, tmp_path):
+    """apps/EmpiricalPseudoPotentialMain.cpp, untouched, against include/uepm (TCLAP from the reference
+    tree, a minimal fmt stand-in), linked with libuepm_epp.so."""
+    exe = str(tmp_path / "epm_main")
+    cmd = ["g++", "-O1", "-std=c++20", *INC, f"-I{os.path.join(ROOT, 'tests', 'cpp', 'fmt_stub')}",
+           f"-I{os.path.join(REF, 'external', 'tclap-1.4.0', 'include')}", f'-DPROJECT_SRC_DIR="{ROOT}"',
+           os.path.join(REF, "apps", "EmpiricalPseudoPotentialMain.cpp"), "-o", exe,
+           f"-L{LIB}", "-luepm_epp", "-luepm_gb300", f"-Wl,-rpath,{LIB}"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr[-4000:]
+
+
+def _read_raw(path, nb):
+    a = np.loadtxt(path)
+    nk = int(a[:, 0].max()) + 1
+    return a[:, 2].reshape(nk, nb), a[:, 3:6].reshape(nk, nb, 3)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("yaml,mat,key,nl,soc,shells,nbands", [
+    ("si-cohen-bergstresser.yaml", "Si", "Si-CB", 0, 0, 10, 16),
+    ("materials.yaml", "Ge", "Ge", 1, 1, 8, 6),
+])
+def test_adapter_matches_oracle(gpu, oracle, mats, tmp_path, yaml, mat, key, nl, soc, shells, nbands):
+    exe = _compile_driver(tmp_path)
+    out = str(tmp_path / "run")
+    r = subprocess.run([exe, os.path.join(PARAMS, yaml), mat, "LGXWKULWXKG", "120", str(nbands), str(shells), str(nl),
+                        str(soc), "fp64", out], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr[-2000:]
+    nb = nbands * (2 if soc else 1)
+    E, g = _read_raw(out + "_raw.txt", nb)
+    G = oracle.generate_basis(shells)
+    k, _ = oracle.generate_path("LGXWKULWXKG", 120)
+    ref = oracle.band_structure(mats[key], G, k, nb, nl=bool(nl), soc=bool(soc), grad=True, vectors=True)
+    assert np.abs(E - ref["E"]).max() <= 1e-10
+    Eo = ref["E"].copy()
+    gap_o, _ = oracle.adjust_values(Eo, soc=bool(soc))
+    gap = float([l for l in r.stdout.splitlines() if l.startswith("gap")][0].split()[1])
+    assert abs(gap - gap_o) <= 1e-10
+    # the band file: the reference's header and CSV layout, values after AdjustValues
+    lines = open(out + "_bands.txt").read().splitlines()
+    assert lines[0] == f"# Material {mat}" and lines[1] == f"# NBands {nb}"
+    assert lines[3] == "# Path LGXWKULWXKG" and lines[5].startswith("band_0,band_1")
+    vals = np.array([[float(x) for x in l.split(",")] for l in lines[6:]])
+    np.testing.assert_allclose(vals, Eo, atol=1e-5)  # 6 significant digits, like the reference's stream output
+    # Hamiltonian path: all eigenvalues at one k
+    ham = open(out + "_ham.txt").read().split("\n")
+    Eh = np.array([float(l.split()[1]) for l in ham if l.startswith("E ")])
+    H = oracle.assemble(mats[key], G, [0.11, 0.27, -0.05], nl=bool(nl), soc=bool(soc))
+    assert np.abs(Eh - oracle.eigh(H)).max() <= 1e-10
