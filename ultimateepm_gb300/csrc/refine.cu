@@ -129,8 +129,38 @@ __global__ void __launch_bounds__(32 * kSmallWarps) k_small_eigh(S* __restrict__
         VV(i, j)    = Ag[q];  // A, overwritten below
     }
     __syncwarp();
+    // FP32 eigenvectors are orthonormal to ~1e-6, so S = I + E with a small E and, to first order,
+    // S^-1/2 = I - E/2 (Loewdin): C = A - (E A + A E)/2 and W = (I - E/2) V, with an O(|E|^2 |A|)
+    // error (~1e-11 eV at |E| = 1e-6). When some |E_ij| exceeds 1e-4 the Cholesky route runs instead.
+    R emax = 0;
+    for (int q = lane; q < m * m; q += 32) {
+        const int i = q / m, j = q - i * m;
+        const S   e = (i == j) ? ST<S>::make(ST<S>::re(LL(i, j)) - 1.0, ST<S>::im(LL(i, j))) : LL(i, j);
+        emax        = fmax(emax, sqrt(ST<S>::norm(e)));
+    }
+    emax             = warp_max(emax);
+    const bool lowdin = emax <= 1e-4;
+    if (lowdin) {
+        for (int q = lane; q < m * m; q += 32) {
+            const int i = q / m, c = q - i * m;
+            S         acc = ST<S>::zero();
+            for (int j = 0; j < m; ++j) {
+                const S eij = (i == j) ? ST<S>::make(ST<S>::re(LL(i, j)) - 1.0, ST<S>::im(LL(i, j))) : LL(i, j);
+                const S ejc = (j == c) ? ST<S>::make(ST<S>::re(LL(j, c)) - 1.0, ST<S>::im(LL(j, c))) : LL(j, c);
+                acc         = cfma(eij, VV(j, c), acc);
+                acc         = cfma(VV(i, j), ejc, acc);
+            }
+            CC(i, c) = cfma(acc, ST<S>::make(-0.5, 0.0), VV(i, c));
+        }
+        __syncwarp();
+        for (int q = lane; q < m * m; q += 32) {
+            const int i = q / m, c = q - i * m;
+            VV(i, c)    = CC(i, c);
+        }
+        __syncwarp();
+    }
     // Cholesky S = L L^H (lanes over rows)
-    for (int k = 0; k < m; ++k) {
+    for (int k = 0; k < m && !lowdin; ++k) {
         R dkk = ST<S>::re(LL(k, k));
         for (int j = 0; j < k; ++j) dkk -= ST<S>::norm(LL(k, j));
         if (!(dkk > 0.0)) {
@@ -148,22 +178,23 @@ __global__ void __launch_bounds__(32 * kSmallWarps) k_small_eigh(S* __restrict__
         if (lane == 0) LL(k, k) = ST<S>::make(lkk, 0.0);
         __syncwarp();
     }
-    // M = L^-1 A into C (lanes over columns), then C = L^-1 M^H into V's place... keep M in C,
-    // write L^-1 M^H into V, then copy back to C after symmetrising.
-    for (int c = lane; c < m; c += 32)
-        for (int i = 0; i < m; ++i) {
-            S s = VV(i, c);
-            for (int j = 0; j < i; ++j) s = cfma(ST<S>::neg(LL(i, j)), CC(j, c), s);
-            CC(i, c) = cscale(s, 1.0 / ST<S>::re(LL(i, i)));
-        }
-    __syncwarp();
-    for (int c = lane; c < m; c += 32)
-        for (int i = 0; i < m; ++i) {
-            S s = ST<S>::conj(CC(c, i));
-            for (int j = 0; j < i; ++j) s = cfma(ST<S>::neg(LL(i, j)), VV(j, c), s);
-            VV(i, c) = cscale(s, 1.0 / ST<S>::re(LL(i, i)));
-        }
-    __syncwarp();
+    // M = L^-1 A into C (lanes over columns), then L^-1 M^H into V; symmetrised into C below.
+    if (!lowdin) {
+        for (int c = lane; c < m; c += 32)
+            for (int i = 0; i < m; ++i) {
+                S s = VV(i, c);
+                for (int j = 0; j < i; ++j) s = cfma(ST<S>::neg(LL(i, j)), CC(j, c), s);
+                CC(i, c) = cscale(s, 1.0 / ST<S>::re(LL(i, i)));
+            }
+        __syncwarp();
+        for (int c = lane; c < m; c += 32)
+            for (int i = 0; i < m; ++i) {
+                S s = ST<S>::conj(CC(c, i));
+                for (int j = 0; j < i; ++j) s = cfma(ST<S>::neg(LL(i, j)), VV(j, c), s);
+                VV(i, c) = cscale(s, 1.0 / ST<S>::re(LL(i, i)));
+            }
+        __syncwarp();
+    }
     // C = (V + V^H) / 2, V = I
     for (int q = lane; q < m * m; q += 32) {
         const int i = q / m, c = q - i * m;
@@ -191,7 +222,9 @@ __global__ void __launch_bounds__(32 * kSmallWarps) k_small_eigh(S* __restrict__
         }
         off = warp_max(off);
         dia = warp_max(dia);
-        if (off <= 1e-17 * dia || off == 0.0) break;
+        // remaining off-diagonals move the Ritz values by at most ~off (degenerate pairs) or
+        // off^2 / gap: 1e-10 of the largest diagonal is ~2e-9 eV here
+        if (off <= 1e-10 * dia || off == 0.0) break;
         for (int round = 0; round < me - 1; ++round) {
             // tournament pairing: slot 0 fixed, slots 1..me-1 rotate
             if (lane < npair) {
@@ -290,8 +323,20 @@ __global__ void __launch_bounds__(32 * kSmallWarps) k_small_eigh(S* __restrict__
         Eout[(size_t)b * nb + j] = ev;
         if (!isfinite(ev)) bad = true;
     }
-    // W = L^-H V[:, ord[:nb]] (back substitution with L^H), lanes over columns
-    if (want_w) {
+    // W = (I - E/2) V[:, ord[:nb]] (Loewdin) or L^-H V[:, ord[:nb]] (Cholesky)
+    if (want_w && lowdin) {
+        for (int q = lane; q < m * nb; q += 32) {
+            const int i = q / nb, c = q - i * nb;
+            const int oc = ord[c];
+            S         acc = ST<S>::zero();
+            for (int j = 0; j < m; ++j) {
+                const S eij = (i == j) ? ST<S>::make(ST<S>::re(LL(i, j)) - 1.0, ST<S>::im(LL(i, j))) : LL(i, j);
+                acc         = cfma(eij, VV(j, oc), acc);
+            }
+            Wg[(size_t)i * nb + c] = cfma(acc, ST<S>::make(-0.5, 0.0), VV(i, oc));
+        }
+    }
+    if (want_w && !lowdin) {
         for (int c = lane; c < nb; c += 32) {
             const int oc = ord[c];
             for (int i = m - 1; i >= 0; --i) {

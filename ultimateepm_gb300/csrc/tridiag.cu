@@ -22,6 +22,8 @@
 // Per step: 4 m^2 FMA for the product + 4 m^2 for the lower-triangle update (complex), i.e. the
 // 16/3 n^3 algorithmic flops (4/3 n^3 for real symmetric matrices). The matrix lives in a per-k HBM
 // workspace; the 129 MB L2 holds the working set of the resident CTAs.
+#include <algorithm>
+
 #include "uepm_common.cuh"
 #include "uepm_kernels.h"
 
@@ -37,9 +39,6 @@ __global__ void __launch_bounds__(NT) k_tridiag(S* __restrict__ H, int n, int ld
                                                 S* __restrict__ tqOut, int* __restrict__ status, int batch) {
     using R       = typename ST<S>::R;
     constexpr int NW = NT / 32;
-    const int     b  = blockIdx.x;
-    if (b >= batch) return;
-    S*        Ag  = H + (size_t)b * mstride;
     const int lds = n | 1;
     extern __shared__ __align__(16) unsigned char smraw[];
     S*        As   = reinterpret_cast<S*>(smraw);  // SMEM: n x lds
@@ -50,6 +49,10 @@ __global__ void __launch_bounds__(NT) k_tridiag(S* __restrict__ H, int n, int ld
     __shared__ S   s_th, s_sc;
     __shared__ int s_skip;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    // The grid may be smaller than the batch: each CTA reduces matrices b, b + gridDim.x, ... so the
+    // number of matrices in flight (and their L2 working set) is set by the launch, not the batch.
+    for (int b = blockIdx.x; b < batch; b += gridDim.x) {
+    S*        Ag  = H + (size_t)b * mstride;
     bool      bad = false;
     S*        A   = SMEM ? As : Ag;
     const int ld  = SMEM ? lds : ldg;
@@ -202,6 +205,19 @@ __global__ void __launch_bounds__(NT) k_tridiag(S* __restrict__ H, int n, int ld
             if (r > c + 1) Ag[(size_t)c * ldg + r] = As[(size_t)c * lds + r];
         }
     }
+    __syncthreads();  // shared memory is reused by the CTA's next matrix
+    }
+}
+
+static int sm_count() {
+    static int sms = 0;
+    if (!sms) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        if (sms <= 0) sms = 1;
+    }
+    return sms;
 }
 
 template <typename S, int NT, int MAXT, bool SMEM>
@@ -211,7 +227,15 @@ static void tridiag_launch_t(S* H, int n, int ld, size_t mstride, typename ST<S>
     const size_t smem = sizeof(S) * ((SMEM ? (size_t)n * (n | 1) : 0) + (size_t)(2 + NT / 32) * n) + sizeof(R) * 3 * (NT / 32);
     auto         kern = k_tridiag<S, NT, MAXT, SMEM>;
     if (smem > 48 * 1024) cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    kern<<<batch, NT, smem, s>>>(H, n, ld, mstride, d, e, tq, status, batch);
+    int grid = batch;
+    if (!SMEM) {
+        // keep the matrices in flight within ~96 MB so that they stay resident in the 129 MB L2:
+        // each step re-reads the whole trailing matrix
+        const size_t bytes = sizeof(S) * (size_t)n * n;
+        const int    per_sm = (int)std::max<size_t>(1, std::min<size_t>(8, (96u << 20) / (bytes * (size_t)sm_count())));
+        grid                = std::min(batch, per_sm * sm_count());
+    }
+    kern<<<grid, NT, smem, s>>>(H, n, ld, mstride, d, e, tq, status, batch);
     count_launch();
 }
 
@@ -226,7 +250,7 @@ template <typename S, int MAXT>
 static void tridiag_pick(S* H, int n, int ld, size_t mstride, typename ST<S>::R* d, typename ST<S>::R* e, S* tq,
                          int* status, int batch, cudaStream_t s) {
     if (use_smem<S>(n)) tridiag_launch_t<S, 256, MAXT, true>(H, n, ld, mstride, d, e, tq, status, batch, s);
-    else tridiag_launch_t<S, 128, MAXT, false>(H, n, ld, mstride, d, e, tq, status, batch, s);
+    else tridiag_launch_t<S, 256, MAXT, false>(H, n, ld, mstride, d, e, tq, status, batch, s);
 }
 
 template <typename S>

@@ -63,6 +63,14 @@ __device__ __forceinline__ int sturm_count(const float* __restrict__ d, const fl
 
 // One group of LPM lanes per matrix (LPM = smallest power of two >= nb, at most 32), so a warp
 // bisects 32 / LPM matrices at once and every lane carries an eigenvalue.
+// Shared memory of one matrix in k_bisect: d and e^2 in T, plus FP32 copies for the FP64 kernel's
+// FP32 pre-bracketing.
+template <typename T>
+__host__ __device__ inline size_t bisect_matrix_bytes(int n) {
+    const size_t b = sizeof(T) * 2 * (size_t)n + (sizeof(T) == 8 ? sizeof(float) * 2 * (size_t)n : 0);
+    return (b + 15) & ~(size_t)15;
+}
+
 template <typename T>
 __global__ void k_bisect(const T* __restrict__ dIn, const T* __restrict__ eIn, int n, int nb, int lpm, T* __restrict__ evOut,
                          int ev_ld, int batch) {
@@ -71,8 +79,11 @@ __global__ void k_bisect(const T* __restrict__ dIn, const T* __restrict__ eIn, i
     const int g    = lane / lpm, gl = lane - g * lpm;
     const int b    = (blockIdx.x * kBisectWarpsPerBlock + warp) * mpw + g;
     extern __shared__ __align__(16) unsigned char smraw[];
-    T*         d     = reinterpret_cast<T*>(smraw) + ((size_t)warp * mpw + g) * 2 * n;
-    T*         e2    = d + n;
+    unsigned char* mine = smraw + ((size_t)warp * mpw + g) * bisect_matrix_bytes<T>(n);
+    T*             d    = reinterpret_cast<T*>(mine);
+    T*             e2   = d + n;
+    float*         df   = reinterpret_cast<float*>(e2 + n);  // FP64 kernel only
+    float*         e2f  = df + n;
     const bool valid = b < batch;
     T          lo = T(3.0e38), hi = T(-3.0e38), emax2 = T(0);
     if (valid) {
@@ -83,9 +94,11 @@ __global__ void k_bisect(const T* __restrict__ dIn, const T* __restrict__ eIn, i
             const T em = (i > 0) ? fabs(eg[i - 1]) : T(0);
             const T ep = (i < n - 1) ? fabs(eg[i]) : T(0);
             d[i]       = di;
+            if (sizeof(T) == 8) df[i] = (float)di;
             if (i < n - 1) {
                 e2[i] = eg[i] * eg[i];
                 emax2 = max(emax2, e2[i]);
+                if (sizeof(T) == 8) e2f[i] = (float)e2[i];
             }
             lo = min(lo, di - em - ep);
             hi = max(hi, di + em + ep);
@@ -108,6 +121,26 @@ __global__ void k_bisect(const T* __restrict__ dIn, const T* __restrict__ eIn, i
     const T atol = eps * tnorm;
     for (int j = gl; j < nb; j += lpm) {
         T a = lo, c = hi;
+        if (sizeof(T) == 8) {
+            // FP32 pre-bracketing: bisect in FP32 (the FP32 pipe is 64x wider on GB300) to ~1e-6
+            // relative, widen by 16 eps32 ||T|| (the backward error of an FP32 Sturm count is a few
+            // eps32 ||T||) and keep the bracket only if two FP64 counts confirm it.
+            const float pivf = FLT_MIN * fmaxf(1.f, (float)emax2);
+            const float tolf = 4.f * FLT_EPSILON * (float)tnorm;
+            float       af = (float)a, cf = (float)c;
+            for (int it = 0; it < 64; ++it) {
+                const float mf = 0.5f * (af + cf);
+                if (cf - af <= tolf || mf <= af || mf >= cf) break;
+                if (sturm_count(df, e2f, n, mf, pivf) > j) cf = mf;
+                else af = mf;
+            }
+            const T w   = T(16) * T(FLT_EPSILON) * tnorm;
+            const T lo2 = max(a, T(af) - w), hi2 = min(c, T(cf) + w);
+            if (lo2 < hi2 && sturm_count(d, e2, n, lo2, pivmin) <= j && sturm_count(d, e2, n, hi2, pivmin) > j) {
+                a = lo2;
+                c = hi2;
+            }
+        }
         // count(a) <= j < count(c) holds throughout; at most ~log2(range / atol) < 200 steps.
         for (int it = 0; it < 200; ++it) {
             const T mid = T(0.5) * (a + c);
@@ -124,13 +157,13 @@ template <typename T>
 void launch_bisect(const T* d, const T* e, int n, int nb, T* ev, int ev_ld, int batch, cudaStream_t s) {
     // lanes per matrix: >= nb (one lane per eigenvalue) and large enough that the d / e^2 copies
     // of the warp's matrices fit in 96 KB of shared memory per block
-    const int max_mpw = (int)std::max<size_t>(1, (96 * 1024) / (sizeof(T) * 2 * (size_t)n * kBisectWarpsPerBlock));
+    const int max_mpw = (int)std::max<size_t>(1, (96 * 1024) / (bisect_matrix_bytes<T>(n) * kBisectWarpsPerBlock));
     int       lpm     = 1;
     while ((lpm < nb || 32 / lpm > max_mpw) && lpm < 32) lpm <<= 1;
     const int    mpw    = 32 / lpm;
     const int    warps  = (batch + mpw - 1) / mpw;
     const int    blocks = (warps + kBisectWarpsPerBlock - 1) / kBisectWarpsPerBlock;
-    const size_t smem   = sizeof(T) * 2 * (size_t)n * 32 * kBisectWarpsPerBlock / lpm;
+    const size_t smem   = bisect_matrix_bytes<T>(n) * mpw * kBisectWarpsPerBlock;
     auto         kern   = k_bisect<T>;
     if (smem > 48 * 1024) cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     kern<<<blocks, 32 * kBisectWarpsPerBlock, smem, s>>>(d, e, n, nb, lpm, ev, ev_ld, batch);
