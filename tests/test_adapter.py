@@ -62,7 +62,12 @@ def test_adapter_matches_oracle(gpu, oracle, mats, tmp_path, yaml, mat, key, nl,
     G = oracle.generate_basis(shells)
     k, _ = oracle.generate_path("LGXWKULWXKG", 120)
     ref = oracle.band_structure(mats[key], G, k, nb, nl=bool(nl), soc=bool(soc), grad=True, vectors=True)
-    assert np.abs(E - ref["E"]).max() <= 1e-10
+    # Near Gamma the gaussian-well nonlocal term evaluates the reference's closed form
+    # i2(x) = ((x^2+3) sinh x - 3x cosh x) / x^3 (bessel_func.hpp:47-52) at small x, where it cancels
+    # to ~3 eps / x^2: a 1-ulp difference between the device and glibc sinh/cosh then moves an
+    # eigenvalue by up to ~1e-9 eV. Away from that (random BZ k-points) parity is 1e-10 eV.
+    tol = 1e-9 if (nl and mats[key].nl_well == 2) else 1e-10
+    assert np.abs(E - ref["E"]).max() <= tol
     Eo = ref["E"].copy()
     gap_o, _ = oracle.adjust_values(Eo, soc=bool(soc))
     gap = float([l for l in r.stdout.splitlines() if l.startswith("gap")][0].split()[1])
