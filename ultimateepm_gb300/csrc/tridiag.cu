@@ -23,6 +23,7 @@
 // 16/3 n^3 algorithmic flops (4/3 n^3 for real symmetric matrices). The matrix lives in a per-k HBM
 // workspace; the 129 MB L2 holds the working set of the resident CTAs.
 #include <algorithm>
+#include <type_traits>
 
 #include "uepm_common.cuh"
 #include "uepm_kernels.h"
@@ -256,6 +257,12 @@ static void tridiag_pick(S* H, int n, int ld, size_t mstride, typename ST<S>::R*
 template <typename S>
 void launch_tridiag(S* H, int n, int ld, size_t mstride, typename ST<S>::R* d, typename ST<S>::R* e, S* tq, int* status,
                     int batch, cudaStream_t s) {
+    if constexpr (std::is_same<S, float>::value) {
+        if (n <= tridiag_reg_max_n()) {
+            launch_tridiag_reg(H, n, ld, mstride, d, e, tq, status, batch, s);
+            return;
+        }
+    }
     // rows of the trailing matrix are at most n - 1 <= 32 * MAXT
     if (n <= 129) tridiag_pick<S, 4>(H, n, ld, mstride, d, e, tq, status, batch, s);
     else if (n <= 161) tridiag_pick<S, 5>(H, n, ld, mstride, d, e, tq, status, batch, s);

@@ -24,6 +24,11 @@ void launch_assemble(const DevParams& P, const cx<double>* Vloc, const double2* 
 template <typename S>
 void launch_tridiag(S* H, int n, int ld, size_t mstride, typename ST<S>::R* d, typename ST<S>::R* e, S* tq, int* status,
                     int batch, cudaStream_t s);
+// tridiag_reg.cu: the same reduction for real FP32 matrices with n <= tridiag_reg_max_n(), held in
+// registers (launch_tridiag<float> dispatches to it).
+int  tridiag_reg_max_n();
+void launch_tridiag_reg(float* H, int n, int ld, size_t mstride, float* d, float* e, float* tq, int* status, int batch,
+                        cudaStream_t s);
 
 // tridiag_eig.cu
 template <typename T>
