@@ -160,6 +160,18 @@ def test_mixed_precision_eigenvalues_within_1e6(gpu, oracle, mats, case, nb, nk)
     assert err <= MIXED_TOL, f"{case}: mixed max |dE| = {err:.3e} eV"
 
 
+def test_mixed_precision_on_the_2000_point_path(gpu, oracle, mats):
+    """The benchmark workload itself (Si Cohen-Bergstresser, basis 137, 16 bands, 2000 k along
+    LGXWKULWXKG): its high-symmetry lines carry many (near-)degenerate clusters."""
+    G = oracle.generate_basis(10)
+    ks, _ = oracle.generate_path("LGXWKULWXKG", 2000)
+    E, _, _, st = _ctx(mats["Si-CB"], G, False, False, N.UEPM_PREC_MIXED).solve(ks, 16)
+    Eo = oracle.band_structure(mats["Si-CB"], G, ks, 16)["E"]
+    assert not st.any()
+    err = np.abs(E - Eo).max()
+    assert err <= MIXED_TOL, f"mixed max |dE| = {err:.3e} eV"
+
+
 def test_mixed_precision_vectors_and_gradients(gpu, oracle, mats):
     G = oracle.generate_basis(10)
     ks = _kset(oracle, 41, 4)
