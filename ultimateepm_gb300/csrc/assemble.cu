@@ -224,6 +224,15 @@ __device__ __forceinline__ void put(double* p, cx<double> h) { *p = h.x; }
 __device__ __forceinline__ void put(cx<double>* p, cx<double> h) { *p = h; }
 __device__ __forceinline__ void put(float* p, cx<double> h) { *p = (float)h.x; }
 __device__ __forceinline__ void put(cx<float>* p, cx<double> h) { *p = mk((float)h.x, (float)h.y); }
+__device__ __forceinline__ ds2 split_fp32(double v) {
+    const float hi = __double2float_rn(v);
+    return ds2{hi, __double2float_rn(v - (double)hi)};
+}
+__device__ __forceinline__ void put(ds2* p, cx<double> h) { *p = split_fp32(h.x); }
+__device__ __forceinline__ void put(ds4* p, cx<double> h) {
+    const ds2 r = split_fp32(h.x), i = split_fp32(h.y);
+    *p = ds4{r.hi, r.lo, i.hi, i.lo};
+}
 __device__ __forceinline__ cx<double> conjd(cx<double> a) { return mk(a.x, -a.y); }
 
 // Writes element (r, c) of the full matrix and, when r != c, its Hermitian mirror (c, r).
@@ -298,5 +307,9 @@ template void launch_assemble<double>(const DevParams&, const cx<double>*, const
                                       double*, int, size_t, float*, size_t, int, cudaStream_t);
 template void launch_assemble<cx<double>>(const DevParams&, const cx<double>*, const double2*, const double2*, const double*,
                                           cx<double>*, int, size_t, cx<float>*, size_t, int, cudaStream_t);
+template void launch_assemble<ds2>(const DevParams&, const cx<double>*, const double2*, const double2*, const double*, ds2*,
+                                   int, size_t, float*, size_t, int, cudaStream_t);
+template void launch_assemble<ds4>(const DevParams&, const cx<double>*, const double2*, const double2*, const double*, ds4*,
+                                   int, size_t, cx<float>*, size_t, int, cudaStream_t);
 
 }  // namespace uepm

@@ -282,10 +282,13 @@ void run_chunk(uepm_ctx* ctx, const Layout& L, char* ws, const double* kk, int c
         }
         return;
     }
+    using SP  = typename Split<S>::type;
     auto* H32 = reinterpret_cast<S32*>(ws + L.H32);
+    auto* Hs  = reinterpret_cast<SP*>(ws + L.H);
     {
         ProfScope p(ctx, s, KK_ASSEMBLE);
-        launch_assemble<S>(ctx->P, ctx->d_Vloc, ctx->d_phNL, ctx->d_phSO, rows, H, n, mstride, H32, mstride, c, s);
+        // the FP64 matrix is kept only for the Rayleigh-Ritz products: stored as FP32 pairs in place
+        launch_assemble<SP>(ctx->P, ctx->d_Vloc, ctx->d_phNL, ctx->d_phSO, rows, Hs, n, mstride, H32, mstride, c, s);
     }
     auto* d     = reinterpret_cast<float*>(ws + L.d);
     auto* e     = reinterpret_cast<float*>(ws + L.e);
@@ -314,7 +317,7 @@ void run_chunk(uepm_ctx* ctx, const Layout& L, char* ws, const double* kk, int c
     }
     {
         ProfScope p(ctx, s, KK_REFINE_PROJECT);
-        launch_refine_project<S>(H, n, n, mstride, X32, m, rw, small, c, s);
+        launch_refine_project<S>(Hs, n, n, mstride, X32, m, rw, small, c, s);
     }
     S* W = small + (size_t)2 * m * m;  // W block of the first matrix; matrices are refine_small_elems apart
     {
@@ -323,7 +326,7 @@ void run_chunk(uepm_ctx* ctx, const Layout& L, char* ws, const double* kk, int c
     }
     if (vec) {
         ProfScope p(ctx, s, KK_REFINE_VECTORS);
-        launch_refine_vectors<S>(n, m, nb, rw, W, Xo, gr, ctx->P, kk, ctx->d_G, c, s);
+        launch_refine_vectors<S>(n, m, nb, X32, W, Xo, gr, ctx->P, kk, ctx->d_G, c, s);
     }
 }
 

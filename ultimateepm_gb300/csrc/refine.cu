@@ -1,68 +1,107 @@
-// refine.cu -- FP64 Rayleigh-Ritz refinement of FP32 eigenvectors (mixed-precision path).
+// refine.cu -- FP64-accurate Rayleigh-Ritz refinement of FP32 eigenvectors (mixed-precision path).
 //
 // No reference counterpart: the reference only has the FP64 Eigen solve. Given FP32 approximations
 // X (n x m, m = nb + guard bands) to the lowest eigenvectors of the FP64 Hermitian H, this computes
-// in FP64
 //   k_refine_project   Y = H X, S = X^H X, A = X^H Y            (one CTA per matrix)
 //   k_small_eigh       the m x m pencil A c = lambda S c: Cholesky S = L L^H, C = L^-1 A L^-H,
 //                      parallel cyclic Jacobi on C (m/2 disjoint rotations at a time), ascending
-//                      sort, W = L^-H V   (one warp per matrix, all in shared memory)
+//                      sort, W = L^-H V   (one warp per matrix, all in shared memory, FP64)
 //   k_refine_vectors   Ritz vectors X W and their Hellmann-Feynman gradients (on request)
 // Ritz values err by about ||H x - lambda x||^2 / gap, where the gap is to the first eigenvalue
 // outside the subspace; the guard bands keep that gap open.
 //
-// FP64 work per matrix (complex): 4 n^2 m FMA for Y, 4 n m(m+1) for S and A, O(m^3) for the small
-// solve, 4 n m nb for the refined vectors. Real symmetric matrices need a quarter of that.
+// The products of k_refine_project need FP64-level accuracy (an error dA moves the Ritz values by
+// dA, and |H| reaches ~10^2 eV), but their operands are exact FP32 values (X) and FP64 values split
+// into FP32 pairs (H, written that way by the assembly): they run in double-single arithmetic on the
+// FP32 pipe (exact products, two-sum accumulation, ~48 significant bits), about 10 FP32 operations
+// per real multiply-add instead of one FMA on GB300's ~60x slower FP64 pipe.
+#include <type_traits>
+
 #include "uepm_common.cuh"
 #include "uepm_kernels.h"
 
 namespace uepm {
 
 constexpr int kProjNT = 256;
-
+constexpr int kProjVB = 4;                  // vectors per Y work item
+constexpr size_t kProjStageBytes = 96 << 10;  // X staged in shared memory up to this size
 
 template <typename S>
-__global__ void __launch_bounds__(kProjNT) k_refine_project(const S* __restrict__ H, int n, int ld, size_t mstride,
-                                                            const cx<float>* __restrict__ X32, int m, S* __restrict__ work,
-                                                            S* __restrict__ small, int batch) {
+using XElem = std::conditional_t<std::is_same<S, double>::value, float, float2>;  // FP32 element of X
+template <typename S>
+using YElem = std::conditional_t<std::is_same<S, double>::value, float2, float4>;  // double-single Y
+
+template <typename S>
+__host__ __device__ inline int proj_mp(int m) {
+    return (m + kProjVB - 1) / kProjVB * kProjVB;
+}
+template <typename S>
+inline size_t proj_stage_bytes(int n, int m) {
+    return sizeof(XElem<S>) * (size_t)n * proj_mp<S>(m);
+}
+
+// X(r, j) from the staged copy ([r][mp]) or from X32 ([j][n]); zero for the padding vectors j >= m.
+template <typename S, bool STAGED>
+__device__ __forceinline__ XElem<S> x_at(const XElem<S>* Xs, const cx<float>* Xg, int n, int m, int mp, int r, int j) {
+    if (STAGED) return Xs[(size_t)r * mp + j];
+    cx<float> v = j < m ? Xg[(size_t)j * n + r] : cx<float>{0.f, 0.f};
+    if constexpr (std::is_same<S, double>::value) return v.x;
+    else return make_float2(v.x, v.y);
+}
+
+template <typename S, bool STAGED>
+__global__ void __launch_bounds__(kProjNT) k_refine_project(const typename Split<S>::type* __restrict__ H, int n, int ld,
+                                                            size_t mstride, const cx<float>* __restrict__ X32, int m,
+                                                            void* __restrict__ work, S* __restrict__ small, int batch) {
+    constexpr bool CX = !std::is_same<S, double>::value;
+    using SE          = typename Split<S>::type;
+    using XT          = XElem<S>;
+    using YT          = YElem<S>;
     const int b = blockIdx.x;
     if (b >= batch) return;
-    const int tid = threadIdx.x;
-    const S*  A   = H + (size_t)b * mstride;
-    S*        X   = work + (size_t)b * refine_work_elems(n, m);  // [r][j]
-    S*        Y   = X + (size_t)n * m;                             // [r][j]
-    for (int q = tid; q < n * m; q += kProjNT) {
-        const int       j = q / n, r = q - j * n;
-        const cx<float> x = X32[((size_t)b * m + j) * n + r];
-        X[(size_t)r * m + j] = ST<S>::make((double)x.x, (double)x.y);
+    const int        tid = threadIdx.x, mp = proj_mp<S>(m);
+    const cx<float>* Xg  = X32 + (size_t)b * m * n;
+    extern __shared__ __align__(16) unsigned char smraw[];
+    XT* Xs = reinterpret_cast<XT*>(smraw);  // [r][mp]
+    if (STAGED) {
+        for (int q = tid; q < n * mp; q += kProjNT) {
+            const int j = q / n, r = q - j * n;
+            Xs[(size_t)r * mp + j] = x_at<S, false>(nullptr, Xg, n, m, mp, r, j);
+        }
+        __syncthreads();
     }
-    __syncthreads();
-    // Y = H X (H in full storage): item = (block of 4 vectors, row r); H(r, c) coalesced over r
-    const int nblk = (m + 3) / 4;
+    // ---- Y = H X: item (block of kProjVB vectors, row r); H(r, c) coalesced over r ----------------
+    YT*       Y    = reinterpret_cast<YT*>(work) + (size_t)b * refine_work_elems(n, m) * sizeof(S) / sizeof(YT);  // [r][mp]
+    const SE* A    = H + (size_t)b * mstride;
+    const int nblk = mp / kProjVB;
     for (int item = tid; item < nblk * n; item += kProjNT) {
-        const int jb = item / n, r = item - jb * n;
-        const int j0 = jb * 4;
-        S         acc[4];
+        const int jb = item / n, r = item - jb * n, j0 = jb * kProjVB;
+        dsacc     yr[kProjVB], yi[kProjVB];
 #pragma unroll
-        for (int q = 0; q < 4; ++q) acc[q] = ST<S>::zero();
-        if (j0 + 4 <= m) {
-            for (int c = 0; c < n; ++c) {
-                const S  h  = ldc(A + (size_t)c * ld + r);
-                const S* xr = X + (size_t)c * m + j0;
+        for (int q = 0; q < kProjVB; ++q) yr[q] = yi[q] = dsacc{0.f, 0.f};
+        for (int c = 0; c < n; ++c) {
+            const SE h = A[(size_t)c * ld + r];
 #pragma unroll
-                for (int q = 0; q < 4; ++q) acc[q] = cfma(h, xr[q], acc[q]);
-            }
-        } else {
-            for (int c = 0; c < n; ++c) {
-                const S  h  = ldc(A + (size_t)c * ld + r);
-                const S* xr = X + (size_t)c * m + j0;
-                for (int q = 0; q < m - j0; ++q) acc[q] = cfma(h, xr[q], acc[q]);
+            for (int q = 0; q < kProjVB; ++q) {
+                const XT x = x_at<S, STAGED>(Xs, Xg, n, m, mp, c, j0 + q);
+                if constexpr (CX) {  // (hr + i hi)(xr + i xi)
+                    ds_add_prod(yr[q], h.rhi, h.rlo, x.x);
+                    ds_add_prod(yr[q], -h.ihi, -h.ilo, x.y);
+                    ds_add_prod(yi[q], h.rhi, h.rlo, x.y);
+                    ds_add_prod(yi[q], h.ihi, h.ilo, x.x);
+                } else {
+                    ds_add_prod(yr[q], h.hi, h.lo, x);
+                }
             }
         }
-        for (int q = 0; q < 4 && j0 + q < m; ++q) Y[(size_t)r * m + j0 + q] = acc[q];
+#pragma unroll
+        for (int q = 0; q < kProjVB; ++q) {
+            if constexpr (CX) Y[(size_t)r * mp + j0 + q] = make_float4(yr[q].h, yr[q].l, yi[q].h, yi[q].l);
+            else Y[(size_t)r * mp + j0 + q] = make_float2(yr[q].h, yr[q].l);
+        }
     }
     __syncthreads();
-    // S = X^H X and A = X^H Y, upper triangles (p <= q) only
+    // ---- S = X^H X and A = X^H Y, upper triangles (p <= q) only, FP64 out ---------------------------
     S*        Sg = small + (size_t)b * refine_small_elems(m, 0);
     S*        Ag = Sg + (size_t)m * m;
     const int np = m * (m + 1) / 2;
@@ -73,12 +112,26 @@ __global__ void __launch_bounds__(kProjNT) k_refine_project(const S* __restrict_
             ++p;
         }
         const int q = p + rest;
-        S         s = ST<S>::zero(), a = ST<S>::zero();
+        dsacc     sr{0.f, 0.f}, si{0.f, 0.f}, ar{0.f, 0.f}, ai{0.f, 0.f};
         for (int r = 0; r < n; ++r) {
-            const S xp = X[(size_t)r * m + p];
-            s          = cfmac(xp, X[(size_t)r * m + q], s);
-            a          = cfmac(xp, Y[(size_t)r * m + q], a);
+            const XT xp = x_at<S, STAGED>(Xs, Xg, n, m, mp, r, p);
+            const XT xq = x_at<S, STAGED>(Xs, Xg, n, m, mp, r, q);
+            const YT y  = Y[(size_t)r * mp + q];
+            if constexpr (CX) {  // conj(xp) xq and conj(xp) y
+                ds_add_prod(sr, xp.x, xq.x);
+                ds_add_prod(sr, xp.y, xq.y);
+                ds_add_prod(si, xp.x, xq.y);
+                ds_add_prod(si, -xp.y, xq.x);
+                ds_add_prod(ar, y.x, y.y, xp.x);
+                ds_add_prod(ar, y.z, y.w, xp.y);
+                ds_add_prod(ai, y.z, y.w, xp.x);
+                ds_add_prod(ai, -y.x, -y.y, xp.y);
+            } else {
+                ds_add_prod(sr, xp, xq);
+                ds_add_prod(ar, y.x, y.y, xp);
+            }
         }
+        const S s = ST<S>::make(ds_value(sr), ds_value(si)), a = ST<S>::make(ds_value(ar), ds_value(ai));
         Sg[p * m + q] = s;
         Ag[p * m + q] = a;
         Sg[q * m + p] = ST<S>::conj(s);
@@ -355,19 +408,22 @@ __global__ void __launch_bounds__(32 * kSmallWarps) k_small_eigh(S* __restrict__
 
 // Ritz vectors x_j = X W[:, j] and gradients; one CTA per matrix, one warp per band.
 template <typename S>
-__global__ void k_refine_vectors(int n, int m, int nb, const S* __restrict__ work, const S* __restrict__ Wg,
+__global__ void k_refine_vectors(int n, int m, int nb, const cx<float>* __restrict__ X32, const S* __restrict__ Wg,
                                  cx<double>* __restrict__ Xout, double* __restrict__ grad, const DevParams P,
                                  const double* __restrict__ kpts, const int* __restrict__ G, int batch) {
     const int b = blockIdx.x;
     if (b >= batch) return;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    const S*  X    = work + (size_t)b * refine_work_elems(n, m);
+    const cx<float>* X = X32 + (size_t)b * m * n;  // [q][r]
     const S*  Wb   = Wg + (size_t)b * refine_small_elems(m, nb);
     for (int j = warp; j < nb; j += nw) {
         double sx = 0, sy = 0, sz = 0;
         for (int r = lane; r < n; r += 32) {
             S x = ST<S>::zero();
-            for (int q = 0; q < m; ++q) x = cfma(X[(size_t)r * m + q], Wb[(size_t)q * nb + j], x);
+            for (int q = 0; q < m; ++q) {
+                const cx<float> xv = X[(size_t)q * n + r];
+                x                  = cfma(ST<S>::make((double)xv.x, (double)xv.y), Wb[(size_t)q * nb + j], x);
+            }
             if (Xout) stc(Xout + ((size_t)b * nb + j) * n + r, mk<double>(ST<S>::re(x), ST<S>::im(x)));
             if (grad) {
                 const double* k  = kpts + 3 * (size_t)b;
@@ -393,9 +449,16 @@ __global__ void k_refine_vectors(int n, int m, int nb, const S* __restrict__ wor
 }
 
 template <typename S>
-void launch_refine_project(const S* H, int n, int ld, size_t mstride, const cx<float>* X32, int m, S* work, S* small,
-                           int batch, cudaStream_t s) {
-    k_refine_project<S><<<batch, kProjNT, 0, s>>>(H, n, ld, mstride, X32, m, work, small, batch);
+void launch_refine_project(const typename Split<S>::type* H, int n, int ld, size_t mstride, const cx<float>* X32, int m,
+                           S* work, S* small, int batch, cudaStream_t s) {
+    const size_t stage = proj_stage_bytes<S>(n, m);
+    if (stage <= kProjStageBytes) {
+        auto kern = k_refine_project<S, true>;
+        if (stage > 48 * 1024) cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)stage);
+        kern<<<batch, kProjNT, stage, s>>>(H, n, ld, mstride, X32, m, work, small, batch);
+    } else {
+        k_refine_project<S, false><<<batch, kProjNT, 0, s>>>(H, n, ld, mstride, X32, m, work, small, batch);
+    }
     count_launch();
 }
 
@@ -410,16 +473,17 @@ void launch_small_eigh(S* small, int m, int nb, double* Eout, S* W, int* status,
 }
 
 template <typename S>
-void launch_refine_vectors(int n, int m, int nb, const S* work, const S* W, cx<double>* Xout, double* grad,
+void launch_refine_vectors(int n, int m, int nb, const cx<float>* X32, const S* W, cx<double>* Xout, double* grad,
                            const DevParams& P, const double* d_k, const int* d_G, int batch, cudaStream_t s) {
-    k_refine_vectors<S><<<batch, 256, 0, s>>>(n, m, nb, work, W, Xout, grad, P, d_k, d_G, batch);
+    k_refine_vectors<S><<<batch, 256, 0, s>>>(n, m, nb, X32, W, Xout, grad, P, d_k, d_G, batch);
     count_launch();
 }
 
 #define UEPM_RF_INST(S)                                                                                             \
-    template void launch_refine_project<S>(const S*, int, int, size_t, const cx<float>*, int, S*, S*, int, cudaStream_t); \
+    template void launch_refine_project<S>(const typename Split<S>::type*, int, int, size_t, const cx<float>*, int, S*, S*, \
+                                           int, cudaStream_t);                                                    \
     template void launch_small_eigh<S>(S*, int, int, double*, S*, int*, int, cudaStream_t);                        \
-    template void launch_refine_vectors<S>(int, int, int, const S*, const S*, cx<double>*, double*, const DevParams&,   \
+    template void launch_refine_vectors<S>(int, int, int, const cx<float>*, const S*, cx<double>*, double*, const DevParams&, \
                                            const double*, const int*, int, cudaStream_t);
 UEPM_RF_INST(double)
 UEPM_RF_INST(cx<double>)

@@ -142,6 +142,60 @@ struct Lower<cx<double>> {
     using type = cx<float>;
 };
 
+// An FP64 matrix element carried as the unevaluated sum of two FP32 values, hi = fl32(v) and
+// lo = fl32(v - hi) (about 48 significant bits, same size as the FP64 element): the mixed path's copy
+// of H for the Rayleigh-Ritz products, which then run on the FP32 pipe.
+struct __align__(8) ds2 {
+    float hi, lo;
+};
+struct __align__(16) ds4 {
+    float rhi, rlo, ihi, ilo;
+};
+template <typename S>
+struct Split;
+template <>
+struct Split<double> {
+    using type = ds2;
+};
+template <>
+struct Split<cx<double>> {
+    using type = ds4;
+};
+template <>
+struct Lower<ds2> {
+    using type = float;
+};
+template <>
+struct Lower<ds4> {
+    using type = cx<float>;
+};
+
+// Double-single accumulation (Dekker's exact product, Knuth's two-sum) with operations the compiler
+// does not contract: acc += (xh + xl) * y with xh * y exact, carried as acc.h + acc.l.
+struct dsacc {
+    float h, l;
+};
+__device__ __forceinline__ void ds_add_prod(dsacc& a, float xh, float xl, float y) {
+    const float p  = __fmul_rn(xh, y);
+    const float pe = fmaf(xh, y, -p);
+    const float s  = __fadd_rn(a.h, p);
+    const float z  = __fsub_rn(s, a.h);
+    const float er = __fadd_rn(__fsub_rn(a.h, __fsub_rn(s, z)), __fsub_rn(p, z));
+    a.h            = s;
+    a.l            = fmaf(xl, y, __fadd_rn(a.l, __fadd_rn(er, pe)));
+}
+// acc += x * y for FP32 x, y (the product exactly)
+__device__ __forceinline__ void ds_add_prod(dsacc& a, float x, float y) {
+    const float p  = __fmul_rn(x, y);
+    const float pe = fmaf(x, y, -p);
+    const float s  = __fadd_rn(a.h, p);
+    const float z  = __fsub_rn(s, a.h);
+    const float er = __fadd_rn(__fsub_rn(a.h, __fsub_rn(s, z)), __fsub_rn(p, z));
+    a.h            = s;
+    a.l            = __fadd_rn(a.l, __fadd_rn(er, pe));
+}
+__device__ __forceinline__ double ds_value(dsacc a) { return (double)a.h + (double)a.l; }
+
 template <typename T>
 __device__ __forceinline__ T warp_sum(T v) {
 #pragma unroll

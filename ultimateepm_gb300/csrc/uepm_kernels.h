@@ -56,13 +56,14 @@ __host__ __device__ inline size_t refine_work_elems(int n, int m) { return (size
 // small-solve scratch per matrix, contiguous: S (m x m), A (m x m), then the m x nb (<= m x m) Ritz
 // coefficients W at offset 2 m^2
 __host__ __device__ inline size_t refine_small_elems(int m, int) { return (size_t)3 * m * m; }
+// H is the FP32-pair copy the mixed-path assembly writes (Split<S>); work holds Y = H X.
 template <typename S>
-void launch_refine_project(const S* H, int n, int ld, size_t mstride, const cx<float>* X32, int m, S* work, S* small,
-                           int batch, cudaStream_t s);
+void launch_refine_project(const typename Split<S>::type* H, int n, int ld, size_t mstride, const cx<float>* X32, int m,
+                           S* work, S* small, int batch, cudaStream_t s);
 template <typename S>
 void launch_small_eigh(S* small, int m, int nb, double* Eout, S* W, int* status, int batch, cudaStream_t s);
 template <typename S>
-void launch_refine_vectors(int n, int m, int nb, const S* work, const S* W, cx<double>* Xout, double* grad,
+void launch_refine_vectors(int n, int m, int nb, const cx<float>* X32, const S* W, cx<double>* Xout, double* grad,
                            const DevParams& P, const double* d_k, const int* d_G, int batch, cudaStream_t s);
 
 }  // namespace uepm
