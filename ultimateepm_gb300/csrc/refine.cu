@@ -145,11 +145,13 @@ __global__ void __launch_bounds__(kProjNT) k_refine_project(const typename Split
 // instructions are issued with most lanes busy.
 constexpr int kSmallWarps = 2;
 
-// shared memory of one warp's matrix: L, C, V (m x (m+1) scalars each) and 4 rotation arrays
+// shared memory of one warp's matrix: L, C, V (m x (m+1) scalars each), 4 rotation arrays and the
+// round's pair table
 template <typename S>
 __host__ __device__ inline size_t small_eigh_warp_bytes(int m) {
     const int me = (m + 1) & ~1;
-    return (sizeof(S) * 3 * (size_t)m * (m + 1) + sizeof(double) * 4 * (size_t)me + 15) & ~(size_t)15;
+    return (sizeof(S) * 3 * (size_t)m * (m + 1) + sizeof(double) * 4 * (size_t)me + sizeof(int) * (size_t)me + 15) &
+           ~(size_t)15;
 }
 
 template <typename S>
@@ -264,22 +266,31 @@ __global__ void __launch_bounds__(32 * kSmallWarps) k_small_eigh(S* __restrict__
         VV(i, c)    = (i == c) ? ST<S>::one() : ST<S>::zero();
     }
     __syncwarp();
-    // parallel cyclic Jacobi: me - 1 rounds of me / 2 disjoint pairs per sweep
+    // parallel cyclic Jacobi: me - 1 rounds of me / 2 disjoint pairs per sweep. The rotation angle
+    // comes from FP32 arithmetic and (c, s) and the unit phase e are then renormalised in FP64 by the
+    // series 1/sqrt(1 + x) = 1 - x/2 + 3x^2/8 (|x| ~ 1e-7), so every rotation is orthogonal to FP64
+    // precision; an angle off by ~1e-7 leaves ~1e-7 of |C_pq| behind, which the next sweep removes.
+    // Pairs below the stopping threshold are not rotated, and a round with no pair above it is
+    // skipped: once the nearly diagonal C has converged, the final sweep costs only its checks.
     const int npair = me / 2;
-    for (int sweep = 0; sweep < 10; ++sweep) {
-        R off = 0, dia = 0;
+    int*      pp    = reinterpret_cast<int*>(rey + me);  // pair table of the round: p, q
+    int*      pq    = pp + npair;
+    for (int sweep = 0; sweep < 12; ++sweep) {
+        R off2 = 0, dia = 0;
         for (int q = lane; q < m * m; q += 32) {
             const int i = q / m, c = q - i * m;
-            if (i < c) off = fmax(off, sqrt(ST<S>::norm(CC(i, c))));
+            if (i < c) off2 = fmax(off2, ST<S>::norm(CC(i, c)));
             if (i == c) dia = fmax(dia, fabs(ST<S>::re(CC(i, i))));
         }
-        off = warp_max(off);
-        dia = warp_max(dia);
+        off2 = warp_max(off2);
+        dia  = warp_max(dia);
         // remaining off-diagonals move the Ritz values by at most ~off (degenerate pairs) or
         // off^2 / gap: 1e-10 of the largest diagonal is ~2e-9 eV here
-        if (off <= 1e-10 * dia || off == 0.0) break;
+        const R thr2 = (1e-10 * dia) * (1e-10 * dia);
+        if (off2 <= thr2 || off2 == 0.0) break;
         for (int round = 0; round < me - 1; ++round) {
             // tournament pairing: slot 0 fixed, slots 1..me-1 rotate
+            bool act = false;
             if (lane < npair) {
                 const int a0 = (lane == 0) ? 0 : ((lane - 1 + round) % (me - 1)) + 1;
                 const int a1 = ((me - 2 - lane + round) % (me - 1)) + 1;
@@ -287,36 +298,51 @@ __global__ void __launch_bounds__(32 * kSmallWarps) k_small_eigh(S* __restrict__
                 R         cc = 1.0, ss = 0.0, ex = 1.0, ey = 0.0;
                 if (q < m) {
                     const S bpq = CC(p, q);
-                    const R ab  = sqrt(ST<S>::norm(bpq));
-                    const R a = ST<S>::re(CC(p, p)), d = ST<S>::re(CC(q, q));
-                    if (ab > 1e-18 * (fabs(a) + fabs(d)) && ab != 0.0) {
-                        const R tau = (d - a) / (2.0 * ab);
-                        const R t   = (tau >= 0.0 ? 1.0 : -1.0) / (fabs(tau) + sqrt(1.0 + tau * tau));
-                        cc          = 1.0 / sqrt(1.0 + t * t);
-                        ss          = t * cc;
-                        ex          = ST<S>::re(bpq) / ab;
-                        ey          = ST<S>::im(bpq) / ab;
+                    const R b2  = ST<S>::norm(bpq);
+                    if (b2 > thr2) {
+                        act               = true;
+                        const R     a = ST<S>::re(CC(p, p)), d = ST<S>::re(CC(q, q));
+                        const float ib = rsqrtf((float)b2);  // 1 / |b|
+                        const float t0 = 0.5f * (float)(d - a) * ib;
+                        const float t  = copysignf(1.f, t0) / (fabsf(t0) + sqrtf(fmaf(t0, t0, 1.f)));
+                        const float c0 = rsqrtf(fmaf(t, t, 1.f));
+                        cc             = c0;
+                        ss             = t * c0;
+                        R x            = fma(cc, cc, ss * ss) - 1.0;
+                        R f            = fma(fma(0.375, x, -0.5), x, 1.0);
+                        cc *= f;
+                        ss *= f;
+                        if constexpr (std::is_same<S, double>::value) {
+                            ex = ST<S>::re(bpq) >= 0.0 ? 1.0 : -1.0;
+                        } else {
+                            ex = ST<S>::re(bpq) * (R)ib;
+                            ey = ST<S>::im(bpq) * (R)ib;
+                            x  = fma(ex, ex, ey * ey) - 1.0;
+                            f  = fma(fma(0.375, x, -0.5), x, 1.0);
+                            ex *= f;
+                            ey *= f;
+                        }
                     }
                 }
+                pp[lane]  = p;
+                pq[lane]  = q;
                 rc[lane]  = cc;
                 rs[lane]  = ss;
                 rex[lane] = ex;
                 rey[lane] = ey;
             }
+            if (!__any_sync(0xffffffffu, act)) continue;  // warp-uniform: nothing to rotate
             __syncwarp();
             // columns: C <- C J, V <- V J  (work items: pair x row)
             for (int it = lane; it < npair * m; it += 32) {
                 const int k = it / m, r = it - k * m;
-                const int a0 = (k == 0) ? 0 : ((k - 1 + round) % (me - 1)) + 1;
-                const int a1 = ((me - 2 - k + round) % (me - 1)) + 1;
-                const int p = min(a0, a1), q = max(a0, a1);
-                if (q >= m) continue;
-                const R c = rc[k], s = rs[k];
-                if (s == 0.0 && c == 1.0) continue;
-                const R ex = rex[k], ey = rey[k];
-                const S jqp = ST<S>::make(-s * ex, s * ey);
-                const S jqq = ST<S>::make(c * ex, -c * ey);
-                const S cp = CC(r, p), cq = CC(r, q);
+                const R   c = rc[k], s = rs[k];
+                if (s == 0.0) continue;
+                const int p = pp[k], q = pq[k];
+                const R   ex = rex[k], ey = rey[k];
+                const S   jqp = ST<S>::make(-s * ex, s * ey);
+                const S   jqq = ST<S>::make(c * ex, -c * ey);
+                const S   cp = CC(r, p), cq = CC(r, q);
                 CC(r, p) = cfma(cq, jqp, cscale(cp, c));
                 CC(r, q) = cfma(cq, jqq, cscale(cp, s));
                 const S vp = VV(r, p), vq = VV(r, q);
@@ -327,30 +353,21 @@ __global__ void __launch_bounds__(32 * kSmallWarps) k_small_eigh(S* __restrict__
             // rows: C <- J^H C
             for (int it = lane; it < npair * m; it += 32) {
                 const int k = it / m, r = it - k * m;
-                const int a0 = (k == 0) ? 0 : ((k - 1 + round) % (me - 1)) + 1;
-                const int a1 = ((me - 2 - k + round) % (me - 1)) + 1;
-                const int p = min(a0, a1), q = max(a0, a1);
-                if (q >= m) continue;
-                const R c = rc[k], s = rs[k];
-                if (s == 0.0 && c == 1.0) continue;
-                const R ex = rex[k], ey = rey[k];
-                const S jqp = ST<S>::make(-s * ex, s * ey);
-                const S jqq = ST<S>::make(c * ex, -c * ey);
-                const S cp = CC(p, r), cq = CC(q, r);
+                const R   c = rc[k], s = rs[k];
+                if (s == 0.0) continue;
+                const int p = pp[k], q = pq[k];
+                const R   ex = rex[k], ey = rey[k];
+                const S   jqp = ST<S>::make(-s * ex, s * ey);
+                const S   jqq = ST<S>::make(c * ex, -c * ey);
+                const S   cp = CC(p, r), cq = CC(q, r);
                 CC(p, r) = cfma(ST<S>::conj(jqp), cq, cscale(cp, c));
                 CC(q, r) = cfma(ST<S>::conj(jqq), cq, cscale(cp, s));
             }
             __syncwarp();
-            if (lane < npair) {
-                const int a0 = (lane == 0) ? 0 : ((lane - 1 + round) % (me - 1)) + 1;
-                const int a1 = ((me - 2 - lane + round) % (me - 1)) + 1;
-                const int p = min(a0, a1), q = max(a0, a1);
-                if (q < m && !(rs[lane] == 0.0 && rc[lane] == 1.0)) {
-                    CC(p, q) = ST<S>::zero();
-                    CC(q, p) = ST<S>::zero();
-                    CC(p, p) = ST<S>::make(ST<S>::re(CC(p, p)), 0.0);
-                    CC(q, q) = ST<S>::make(ST<S>::re(CC(q, q)), 0.0);
-                }
+            if (lane < npair && rs[lane] != 0.0) {  // Hermitian diagonal stays real
+                const int p = pp[lane], q = pq[lane];
+                CC(p, p)    = ST<S>::make(ST<S>::re(CC(p, p)), 0.0);
+                CC(q, q)    = ST<S>::make(ST<S>::re(CC(q, q)), 0.0);
             }
             __syncwarp();
         }
