@@ -2,130 +2,164 @@
 // Hellmann-Feynman kinetic gradient of each band (Hamiltonian::compute_gradient_at_level,
 // src/EPP/Hamiltonian.cpp:146-194).
 //
-// One CTA per matrix; each warp carries whole eigenvectors in registers (lane owns rows
-// r = lane + 32 t) through all n-1 reflectors, so warps never synchronise with each other.
-// Per reflector and vector: v^H z and z -= (tau v^H z) v over the reflector's rows, i.e. the
+// One CTA per matrix. The reflectors are staged in shared memory in blocks of KB (coalesced copies
+// of the reflector columns, the implicit unit element written out), so each is read from memory
+// once however many vectors it is applied to. Each vector belongs to a group of LPV lanes (lane gl
+// owns rows gl + LPV t, t < T) and stays in registers through all n-1 reflectors: per reflector and
+// vector, v^H z over the group (a log2(LPV)-level butterfly) and z -= (tau v^H z) v, i.e. the
 // 8 n^2 nb algorithmic flops of the back-transformation (2 n^2 nb for real symmetric matrices).
+// Rows at or above the reflector's first row are skipped in whole chunks (t < (i + 1) / LPV).
 // Output vectors are complex (the C ABI layout) whatever the arithmetic.
+#include <algorithm>
+
 #include "uepm_common.cuh"
 #include "uepm_kernels.h"
 
 namespace uepm {
 
-template <typename S, int NT, int MAXT, int VPW>
-__global__ void __launch_bounds__(NT) k_backtransform(const S* __restrict__ H, int n, int ld, size_t mstride,
-                                                      const S* __restrict__ tq, const typename ST<S>::R* __restrict__ z, int nb,
-                                                      cx<typename ST<S>::R>* __restrict__ Xout, const DevParams P,
-                                                      const double* __restrict__ kpts, const int* __restrict__ G,
-                                                      double* __restrict__ grad, int batch) {
+constexpr int kBtMaxWarps = 8;
+constexpr int kBtStageBytes = 48 << 10;
+
+template <typename S, int LPV, int T>
+__global__ void __launch_bounds__(32 * kBtMaxWarps) k_backtransform(const S* __restrict__ H, int n, int ld, size_t mstride,
+                                                                   const S* __restrict__ tq,
+                                                                   const typename ST<S>::R* __restrict__ z, int nb, int kb,
+                                                                   cx<typename ST<S>::R>* __restrict__ Xout,
+                                                                   const DevParams P, const double* __restrict__ kpts,
+                                                                   const int* __restrict__ G, double* __restrict__ grad,
+                                                                   int batch) {
     using R          = typename ST<S>::R;
-    constexpr int NW = NT / 32;
     const int     b  = blockIdx.x;
     if (b >= batch) return;
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const S*  A    = H + (size_t)b * mstride;
-    const S*  tb   = tq + (size_t)b * n;
-    const int tn   = (n + 31) >> 5;
-    // each warp carries VPW vectors at once: one reflector load serves all of them
-    for (int j0 = warp * VPW; j0 < nb; j0 += NW * VPW) {
-        S zr[VPW][MAXT];
+    extern __shared__ __align__(16) unsigned char smraw[];
+    S*        Vs   = reinterpret_cast<S*>(smraw);  // [kb][n]: reflector i0 + q in row q
+    S*        taus = Vs + (size_t)kb * n;          // [kb]
+    const int tid = threadIdx.x, nthr = blockDim.x;
+    const int lane = tid & 31, gl = lane & (LPV - 1);
+    const int grp = tid / LPV, ngrp = nthr / LPV;
+    const S*  A   = H + (size_t)b * mstride;
+    const S*  tb  = tq + (size_t)b * n;
+    const int nch = (nb + ngrp - 1) / ngrp;  // vector chunks (uniform over the CTA)
+    for (int ch = 0; ch < nch; ++ch) {
+        const int  j   = ch * ngrp + grp;
+        const bool has = j < nb;
+        S          zr[T];
 #pragma unroll
-        for (int q = 0; q < VPW; ++q)
-#pragma unroll
-            for (int t = 0; t < MAXT; ++t) {
-                const int r = lane + 32 * t;
-                zr[q][t]    = ST<S>::make((r < n && j0 + q < nb) ? z[((size_t)b * nb + j0 + q) * n + r] : R(0), R(0));
+        for (int t = 0; t < T; ++t) {
+            const int r = gl + LPV * t;
+            zr[t]       = ST<S>::make((has && r < n) ? z[((size_t)b * nb + j) * n + r] : R(0), R(0));
+        }
+        for (int i1 = n - 2; i1 >= 0; i1 -= kb) {
+            const int i0 = max(0, i1 - kb + 1), cnt = i1 - i0 + 1;
+            __syncthreads();  // previous block consumed
+            for (int q = tid; q < cnt * n; q += nthr) {
+                const int k = q / n, r = q - k * n, i = i0 + k;
+                S         v = ST<S>::zero();
+                if (r == i + 1) v = ST<S>::one();
+                else if (r > i + 1) v = ldc(A + (size_t)i * ld + r);
+                Vs[q] = v;
             }
-        for (int i = n - 2; i >= 0; --i) {
-            const S tau = tb[i];
-            if (ST<S>::re(tau) == R(0) && ST<S>::im(tau) == R(0)) continue;
-            const S*  vc = A + (size_t)i * ld;
-            const int t0 = (i + 1) >> 5;  // first chunk holding a row > i (warp-uniform)
-            S         vr[MAXT];
-            S         dot[VPW];
+            for (int q = tid; q < cnt; q += nthr) taus[q] = tb[i0 + q];
+            __syncthreads();
+            for (int i = i1; i >= i0; --i) {
+                const S tau = taus[i - i0];
+                if (ST<S>::re(tau) == R(0) && ST<S>::im(tau) == R(0)) continue;  // uniform
+                const S*  vrow = Vs + (size_t)(i - i0) * n;
+                const int t0   = (i + 1) / LPV;
+                S         dot  = ST<S>::zero();
 #pragma unroll
-            for (int q = 0; q < VPW; ++q) dot[q] = ST<S>::zero();
-#pragma unroll
-            for (int t = 0; t < MAXT; ++t) {
-                vr[t] = ST<S>::zero();
-                if (t >= t0 && t < tn) {
-                    const int r = lane + 32 * t;
-                    if (r > i && r < n) vr[t] = (r == i + 1) ? ST<S>::one() : ldc(vc + r);
-#pragma unroll
-                    for (int q = 0; q < VPW; ++q) dot[q] = cfmac(vr[t], zr[q][t], dot[q]);
+                for (int t = 0; t < T; ++t) {
+                    const int r = gl + LPV * t;
+                    if (t >= t0 && r < n) dot = cfmac(vrow[r], zr[t], dot);
                 }
-            }
 #pragma unroll
-            for (int q = 0; q < VPW; ++q) dot[q] = warp_sum(dot[q]);
+                for (int o = LPV / 2; o > 0; o >>= 1) {
+                    if constexpr (sizeof(S) == sizeof(R)) {
+                        dot += __shfl_xor_sync(0xffffffffu, dot, o);
+                    } else {
+                        dot = ST<S>::make(ST<S>::re(dot) + __shfl_xor_sync(0xffffffffu, ST<S>::re(dot), o),
+                                          ST<S>::im(dot) + __shfl_xor_sync(0xffffffffu, ST<S>::im(dot), o));
+                    }
+                }
+                const S sdt = ST<S>::neg(cmul(tau, dot));
 #pragma unroll
-            for (int q = 0; q < VPW; ++q) {
-                const S sdt = ST<S>::neg(cmul(tau, dot[q]));
-#pragma unroll
-                for (int t = 0; t < MAXT; ++t)
-                    if (t >= t0 && t < tn) zr[q][t] = cfma(vr[t], sdt, zr[q][t]);
+                for (int t = 0; t < T; ++t) {
+                    const int r = gl + LPV * t;
+                    if (t >= t0 && r < n) zr[t] = cfma(vrow[r], sdt, zr[t]);
+                }
             }
         }
+        if (Xout && has) {
+            cx<R>* xo = Xout + ((size_t)b * nb + j) * n;
 #pragma unroll
-        for (int q = 0; q < VPW; ++q) {
-            const int j = j0 + q;
-            if (j >= nb) break;
-            if (Xout) {
-                cx<R>* xo = Xout + ((size_t)b * nb + j) * n;
-#pragma unroll
-                for (int t = 0; t < MAXT; ++t) {
-                    const int r = lane + 32 * t;
-                    if (r < n) stc(xo + r, mk<R>(ST<S>::re(zr[q][t]), ST<S>::im(zr[q][t])));
-                }
+            for (int t = 0; t < T; ++t) {
+                const int r = gl + LPV * t;
+                if (r < n) stc(xo + r, mk<R>(ST<S>::re(zr[t]), ST<S>::im(zr[t])));
             }
-            if (grad) {
-                const double* k  = kpts + 3 * (size_t)b;
-                double        sx = 0, sy = 0, sz = 0;
+        }
+        if (grad) {
+            double sx = 0, sy = 0, sz = 0;
+            if (has) {
+                const double* k = kpts + 3 * (size_t)b;
 #pragma unroll
-                for (int t = 0; t < MAXT; ++t) {
-                    const int r = lane + 32 * t;
+                for (int t = 0; t < T; ++t) {
+                    const int r = gl + LPV * t;
                     if (r < n) {
                         const int    bi = (r < P.N) ? r : r - P.N;
-                        const double w  = (double)ST<S>::norm(zr[q][t]);
+                        const double w  = (double)ST<S>::norm(zr[t]);
                         sx += (k[0] + G[3 * bi]) * w;
                         sy += (k[1] + G[3 * bi + 1]) * w;
                         sz += (k[2] + G[3 * bi + 2]) * w;
                     }
                 }
-                sx = warp_sum(sx);
-                sy = warp_sum(sy);
-                sz = warp_sum(sz);
-                if (lane == 0) {
-                    double* go = grad + ((size_t)b * nb + j) * 3;
-                    go[0]      = (sx * P.grad_pref) * P.frac_to_phys;
-                    go[1]      = (sy * P.grad_pref) * P.frac_to_phys;
-                    go[2]      = (sz * P.grad_pref) * P.frac_to_phys;
-                }
+            }
+#pragma unroll
+            for (int o = LPV / 2; o > 0; o >>= 1) {
+                sx += __shfl_xor_sync(0xffffffffu, sx, o);
+                sy += __shfl_xor_sync(0xffffffffu, sy, o);
+                sz += __shfl_xor_sync(0xffffffffu, sz, o);
+            }
+            if (has && gl == 0) {
+                double* go = grad + ((size_t)b * nb + j) * 3;
+                go[0]      = (sx * P.grad_pref) * P.frac_to_phys;
+                go[1]      = (sy * P.grad_pref) * P.frac_to_phys;
+                go[2]      = (sz * P.grad_pref) * P.frac_to_phys;
             }
         }
     }
 }
 
-template <typename S, int MAXT>
+template <typename S, int LPV, int T>
 static void bt_launch(const S* H, int n, int ld, size_t mstride, const S* tq, const typename ST<S>::R* z, int nb,
                       cx<typename ST<S>::R>* Xout, const DevParams& P, const double* d_k, const int* d_G, double* grad,
                       int batch, cudaStream_t s) {
-    constexpr int NT    = 128;
-    constexpr int words = (int)(sizeof(S) / 4);
-    // vectors per warp: as many as keep the carried registers near 24 words per lane
-    constexpr int VPW = (MAXT * words * 4 <= 24) ? 4 : (MAXT * words * 2 <= 24) ? 2 : 1;
-    k_backtransform<S, NT, MAXT, VPW><<<batch, NT, 0, s>>>(H, n, ld, mstride, tq, z, nb, Xout, P, d_k, d_G, grad, batch);
+    constexpr int GW    = 32 / LPV;
+    const int     warps = std::min(kBtMaxWarps, (nb + GW - 1) / GW);
+    const int     kb    = std::max(4, std::min(64, (int)(kBtStageBytes / (sizeof(S) * (size_t)(n + 1)))));
+    const size_t  smem  = sizeof(S) * ((size_t)kb * n + kb);
+    auto          kern  = k_backtransform<S, LPV, T>;
+    if (smem > 48 * 1024) cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    kern<<<batch, 32 * warps, smem, s>>>(H, n, ld, mstride, tq, z, nb, kb, Xout, P, d_k, d_G, grad, batch);
     count_launch();
 }
 
+// (lanes per vector, rows per lane): 8 lanes while a lane's rows fit about 40 register words, then
+// 16 and 32
 template <typename S>
 void launch_backtransform(const S* H, int n, int ld, size_t mstride, const S* tq, const typename ST<S>::R* z, int nb,
                           cx<typename ST<S>::R>* Xout, const DevParams& P, const double* d_k, const int* d_G, double* grad,
                           int batch, cudaStream_t s) {
-    if (n <= 128) bt_launch<S, 4>(H, n, ld, mstride, tq, z, nb, Xout, P, d_k, d_G, grad, batch, s);
-    else if (n <= 160) bt_launch<S, 5>(H, n, ld, mstride, tq, z, nb, Xout, P, d_k, d_G, grad, batch, s);
-    else if (n <= 256) bt_launch<S, 8>(H, n, ld, mstride, tq, z, nb, Xout, P, d_k, d_G, grad, batch, s);
-    else if (n <= 384) bt_launch<S, 12>(H, n, ld, mstride, tq, z, nb, Xout, P, d_k, d_G, grad, batch, s);
-    else bt_launch<S, 16>(H, n, ld, mstride, tq, z, nb, Xout, P, d_k, d_G, grad, batch, s);
+    constexpr bool CX = sizeof(S) == 2 * sizeof(typename ST<S>::R);
+#define UEPM_BT(L_, T_) bt_launch<S, L_, T_>(H, n, ld, mstride, tq, z, nb, Xout, P, d_k, d_G, grad, batch, s)
+    if (n <= 96) UEPM_BT(8, 12);
+    else if (n <= 144) UEPM_BT(8, 18);
+    else if (!CX && n <= 192) UEPM_BT(8, 24);
+    else if (!CX && n <= 256) UEPM_BT(8, 32);
+    else if (n <= 192) UEPM_BT(16, 12);
+    else if (n <= 256) UEPM_BT(16, 16);
+    else if (n <= 384) UEPM_BT(16, 24);
+    else UEPM_BT(32, 16);
+#undef UEPM_BT
 }
 
 #define UEPM_BT_INST(S)                                                                                          \
