@@ -185,18 +185,46 @@ __device__ __forceinline__ unsigned hash32(unsigned x) {
     return x;
 }
 
+// Division in the LU of T - lam I: the FP32 kernel uses the fast form (inverse iteration only needs
+// a small backward error in its solves).
+__device__ __forceinline__ float idiv(float a, float b) { return __fdividef(a, b); }
+__device__ __forceinline__ double idiv(double a, double b) { return a / b; }
+
+// Work arrays per matrix: U0, U1, U2 (the LU factors) and Z, each n x 32 interleaved by lane; the
+// forward sweep writes its right-hand side Y into Z (Y[i] lands after Z[i] was consumed) and the
+// back substitution overwrites it in place. SMEM: the arrays live in shared memory (one warp per
+// CTA), else in the global workspace.
 template <typename T>
+__host__ __device__ inline size_t invit_smem_bytes(int n) {
+    return sizeof(T) * (4 * (size_t)n * 32 + 2 * (size_t)n);  // + copies of d and e
+}
+
+template <typename T, bool SMEM>
 __global__ void k_invit(const T* __restrict__ dIn, const T* __restrict__ eIn, const T* __restrict__ ev, int ev_ld, int n,
                         int nb, T* __restrict__ work, T* __restrict__ zOut, int* __restrict__ status, int batch) {
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int b    = blockIdx.x * kInvitWarpsPerBlock + warp;
-    __shared__ T   s_lam[kInvitWarpsPerBlock][33];
-    __shared__ int s_gs[kInvitWarpsPerBlock][33];
+    constexpr int WPB  = SMEM ? 1 : kInvitWarpsPerBlock;
+    const int     warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int     b    = blockIdx.x * WPB + warp;
+    __shared__ T   s_lam[WPB][33];
+    __shared__ int s_gs[WPB][33];
+    extern __shared__ __align__(16) unsigned char smraw[];
     if (b >= batch) return;
     const T* d = dIn + (size_t)b * n;
     const T* e = eIn + (size_t)b * n;
-    T*       W = work + (size_t)b * invit_work_elems<T>(n);
-    T *U0 = W, *U1 = W + (size_t)n * 32, *U2 = W + (size_t)2 * n * 32, *Y = W + (size_t)3 * n * 32, *Z = W + (size_t)4 * n * 32;
+    T*       W = SMEM ? reinterpret_cast<T*>(smraw) : work + (size_t)b * invit_work_elems<T>(n);
+    T *U0 = W, *U1 = W + (size_t)n * 32, *U2 = W + (size_t)2 * n * 32, *Z = W + (size_t)3 * n * 32;
+    T* Y = Z;
+    if (SMEM) {  // the recurrences read d and e at every step: keep them next to the factors
+        T* ds = W + (size_t)4 * n * 32;
+        T* es = ds + n;
+        for (int i = lane; i < n; i += 32) {
+            ds[i] = d[i];
+            es[i] = e[i];
+        }
+        __syncwarp();
+        d = ds;
+        e = es;
+    }
     T* zb = zOut + (size_t)b * nb * n;  // final vectors, [j][i]
 
     // ||T||_1 for the cluster tolerance and the tiny-pivot replacement (dstein / dlagts).
@@ -261,7 +289,7 @@ __global__ void k_invit(const T* __restrict__ dIn, const T* __restrict__ eIn, co
                     T       n0, n1, nr;
                     if (fabs(p0) >= fabs(s0)) {
                         if (p0 == T(0)) p0 = pivtiny;
-                        const T l = s0 / p0;
+                        const T l = idiv(s0, p0);
                         U0[(size_t)i * 32 + lane] = p0;
                         U1[(size_t)i * 32 + lane] = p1;
                         U2[(size_t)i * 32 + lane] = p2;
@@ -270,7 +298,7 @@ __global__ void k_invit(const T* __restrict__ dIn, const T* __restrict__ eIn, co
                         n1 = s2 - l * p2;
                         nr = rs - l * rp;
                     } else {
-                        const T l = p0 / s0;
+                        const T l = idiv(p0, s0);
                         U0[(size_t)i * 32 + lane] = s0;
                         U1[(size_t)i * 32 + lane] = s1;
                         U2[(size_t)i * 32 + lane] = s2;
@@ -286,13 +314,13 @@ __global__ void k_invit(const T* __restrict__ dIn, const T* __restrict__ eIn, co
                 }
                 if (fabs(p0) < pivtiny) p0 = (p0 < T(0)) ? -pivtiny : pivtiny;
                 // back substitution into Z, scaled by the largest entry to stay in range
-                T z2 = T(0), z1 = rp / p0;
+                T z2 = T(0), z1 = idiv(rp, p0);
                 Z[(size_t)(n - 1) * 32 + lane] = z1;
                 T zmax = fabs(z1);
                 for (int i = n - 2; i >= 0; --i) {
                     T u0 = U0[(size_t)i * 32 + lane];
                     if (fabs(u0) < pivtiny) u0 = (u0 < T(0)) ? -pivtiny : pivtiny;
-                    const T zi = (Y[(size_t)i * 32 + lane] - U1[(size_t)i * 32 + lane] * z1 - U2[(size_t)i * 32 + lane] * z2) / u0;
+                    const T zi = idiv(Y[(size_t)i * 32 + lane] - U1[(size_t)i * 32 + lane] * z1 - U2[(size_t)i * 32 + lane] * z2, u0);
                     Z[(size_t)i * 32 + lane] = zi;
                     zmax = max(zmax, fabs(zi));
                     z2   = z1;
@@ -350,8 +378,15 @@ __global__ void k_invit(const T* __restrict__ dIn, const T* __restrict__ eIn, co
 template <typename T>
 void launch_invit(const T* d, const T* e, const T* ev, int ev_ld, int n, int nb, T* work, T* z, int* status, int batch,
                   cudaStream_t s) {
-    const int blocks = (batch + kInvitWarpsPerBlock - 1) / kInvitWarpsPerBlock;
-    k_invit<T><<<blocks, 32 * kInvitWarpsPerBlock, 0, s>>>(d, e, ev, ev_ld, n, nb, work, z, status, batch);
+    const size_t smem = invit_smem_bytes<T>(n);
+    if (smem <= 200 * 1024) {
+        auto kern = k_invit<T, true>;
+        if (smem > 48 * 1024) cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        kern<<<batch, 32, smem, s>>>(d, e, ev, ev_ld, n, nb, work, z, status, batch);
+    } else {
+        const int blocks = (batch + kInvitWarpsPerBlock - 1) / kInvitWarpsPerBlock;
+        k_invit<T, false><<<blocks, 32 * kInvitWarpsPerBlock, 0, s>>>(d, e, ev, ev_ld, n, nb, work, z, status, batch);
+    }
     count_launch();
 }
 
