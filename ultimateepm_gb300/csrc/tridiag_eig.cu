@@ -21,7 +21,6 @@ namespace uepm {
 
 constexpr int kBisectWarpsPerBlock = 4;
 constexpr int kInvitWarpsPerBlock  = 2;
-constexpr int kInvitIters          = 3;
 
 // Sturm count: the number of eigenvalues of T below x, from the LDL^T pivots
 // q_0 = d_0 - x, q_i = (d_i - x) - e_{i-1}^2 / q_{i-1} (pivots within pivmin replaced by -pivmin).
@@ -189,33 +188,50 @@ __device__ __forceinline__ unsigned hash32(unsigned x) {
 // a small backward error in its solves).
 __device__ __forceinline__ float idiv(float a, float b) { return __fdividef(a, b); }
 __device__ __forceinline__ double idiv(double a, double b) { return a / b; }
+__device__ __forceinline__ float isqrt_inv(float a) { return rsqrtf(a); }
+__device__ __forceinline__ double isqrt_inv(double a) { return 1.0 / sqrt(a); }
 
-// Work arrays per matrix: U0, U1, U2 (the LU factors) and Z, each n x 32 interleaved by lane; the
-// forward sweep writes its right-hand side Y into Z (Y[i] lands after Z[i] was consumed) and the
-// back substitution overwrites it in place. SMEM: the arrays live in shared memory (one warp per
-// CTA), else in the global workspace.
+// Iterations per vector: the FP32 vectors of the mixed path only need their components outside the
+// guard-banded subspace small (the FP64 Rayleigh-Ritz resolves mixing inside it), the FP64 vectors
+// of the drop-in path are final.
 template <typename T>
-__host__ __device__ inline size_t invit_smem_bytes(int n) {
-    return sizeof(T) * (4 * (size_t)n * 32 + 2 * (size_t)n);  // + copies of d and e
+struct InvitIters {
+    static constexpr int value = 3;
+};
+template <>
+struct InvitIters<float> {
+    static constexpr int value = 2;
+};
+
+// Work arrays per matrix, each n x LS interleaved by lane (LS = lanes in use, min(nb, 32)): U0, U1
+// (the first two rows of U), Lm (the multipliers), Z (the vector; the forward sweep writes its
+// right-hand side into it, Y[i] landing after Z[i] was consumed, and the back substitution
+// overwrites it in place), then one word of row-interchange bits per 32 rows and lane (the third row
+// of U is e[i+1] where rows were interchanged, else 0), then copies of d and e. SMEM: all in shared
+// memory (one warp per CTA), else in the global workspace.
+template <typename T>
+__host__ __device__ inline size_t invit_smem_bytes(int n, int ls) {
+    return sizeof(T) * (4 * (size_t)n * ls + 2 * (size_t)n) + sizeof(unsigned) * (size_t)((n + 31) / 32) * ls;
 }
 
 template <typename T, bool SMEM>
 __global__ void k_invit(const T* __restrict__ dIn, const T* __restrict__ eIn, const T* __restrict__ ev, int ev_ld, int n,
                         int nb, T* __restrict__ work, T* __restrict__ zOut, int* __restrict__ status, int batch) {
     constexpr int WPB  = SMEM ? 1 : kInvitWarpsPerBlock;
+    constexpr int NIT  = InvitIters<T>::value;
     const int     warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int     b    = blockIdx.x * WPB + warp;
     __shared__ T   s_lam[WPB][33];
     __shared__ int s_gs[WPB][33];
     extern __shared__ __align__(16) unsigned char smraw[];
     if (b >= batch) return;
-    const T* d = dIn + (size_t)b * n;
-    const T* e = eIn + (size_t)b * n;
-    T*       W = SMEM ? reinterpret_cast<T*>(smraw) : work + (size_t)b * invit_work_elems<T>(n);
-    T *U0 = W, *U1 = W + (size_t)n * 32, *U2 = W + (size_t)2 * n * 32, *Z = W + (size_t)3 * n * 32;
-    T* Y = Z;
+    const int LS = min(nb, 32);
+    const T*  d  = dIn + (size_t)b * n;
+    const T*  e  = eIn + (size_t)b * n;
+    T*        W  = SMEM ? reinterpret_cast<T*>(smraw) : work + (size_t)b * invit_work_elems<T>(n);
+    T *U0 = W, *U1 = W + (size_t)n * LS, *Lm = W + (size_t)2 * n * LS, *Z = W + (size_t)3 * n * LS;
     if (SMEM) {  // the recurrences read d and e at every step: keep them next to the factors
-        T* ds = W + (size_t)4 * n * 32;
+        T* ds = W + (size_t)4 * n * LS;
         T* es = ds + n;
         for (int i = lane; i < n; i += 32) {
             ds[i] = d[i];
@@ -225,7 +241,9 @@ __global__ void k_invit(const T* __restrict__ dIn, const T* __restrict__ eIn, co
         d = ds;
         e = es;
     }
-    T* zb = zOut + (size_t)b * nb * n;  // final vectors, [j][i]
+    unsigned* SW = reinterpret_cast<unsigned*>(W + (size_t)4 * n * LS + (SMEM ? 2 * (size_t)n : 0));  // [n/32][LS]
+    T*        zb = zOut + (size_t)b * nb * n;  // final vectors, [j][i]
+#define AT(X, i) X[(size_t)(i) * LS + lane]
 
     // ||T||_1 for the cluster tolerance and the tiny-pivot replacement (dstein / dlagts).
     T onenrm = 0;
@@ -237,7 +255,9 @@ __global__ void k_invit(const T* __restrict__ dIn, const T* __restrict__ eIn, co
     const T eps     = num<T>::eps();
     const T ortol   = T(1e-3) * onenrm;
     const T pivtiny = eps * onenrm;
-    bool    bad     = false;
+    // largest |z| for which sum z^2 stays finite
+    const T zsafe = sizeof(T) == 4 ? T(1e17) : T(1e150);
+    bool    bad   = false;
 
     // carried across groups of 32: the previous (perturbed) shift and cluster start
     T   prev_lam = T(0);
@@ -270,107 +290,145 @@ __global__ void k_invit(const T* __restrict__ dIn, const T* __restrict__ eIn, co
         const bool active = lane < gn;
         const T    lam    = active ? s_lam[warp][lane] : T(0);
         const int  j      = g0 + lane;
+        bool       clus   = false;  // any vector of this group orthogonalised against earlier ones
+        for (int q = 0; q < gn; ++q) clus |= s_gs[warp][q] < g0 + q;
 
         // deterministic start vector in (-1, 1)
         if (active)
             for (int i = 0; i < n; ++i) {
                 const unsigned h = hash32((unsigned)(j * 7919 + 13) ^ hash32((unsigned)i + 0x9e3779b9U));
-                Z[(size_t)i * 32 + lane] = T(2) * T(h & 0xffffff) / T(16777216) - T(1) + T(1e-3);
+                AT(Z, i)         = T(2) * T(h & 0xffffff) / T(16777216) - T(1) + T(1e-3);
             }
         __syncwarp();
 
-        for (int it = 0; it < kInvitIters; ++it) {
+        T sc = T(1);  // pending scale of Z
+        for (int it = 0; it < NIT; ++it) {
             if (active) {
-                // LU with partial pivoting of T - lam I, applied to the right-hand side Z -> Y.
-                T p0 = d[0] - lam, p1 = (n > 1) ? e[0] : T(0), p2 = T(0), rp = Z[lane];
-                for (int i = 0; i < n - 1; ++i) {
-                    const T s0 = e[i], s1 = d[i + 1] - lam, s2 = (i + 1 < n - 1) ? e[i + 1] : T(0);
-                    const T rs = Z[(size_t)(i + 1) * 32 + lane];
-                    T       n0, n1, nr;
-                    if (fabs(p0) >= fabs(s0)) {
-                        if (p0 == T(0)) p0 = pivtiny;
-                        const T l = idiv(s0, p0);
-                        U0[(size_t)i * 32 + lane] = p0;
-                        U1[(size_t)i * 32 + lane] = p1;
-                        U2[(size_t)i * 32 + lane] = p2;
-                        Y[(size_t)i * 32 + lane]  = rp;
-                        n0 = s1 - l * p1;
-                        n1 = s2 - l * p2;
-                        nr = rs - l * rp;
-                    } else {
-                        const T l = idiv(p0, s0);
-                        U0[(size_t)i * 32 + lane] = s0;
-                        U1[(size_t)i * 32 + lane] = s1;
-                        U2[(size_t)i * 32 + lane] = s2;
-                        Y[(size_t)i * 32 + lane]  = rs;
-                        n0 = p1 - l * s1;
-                        n1 = p2 - l * s2;
-                        nr = rp - l * rs;
+                T rp = AT(Z, 0) * sc, ulast;
+                if (it == 0) {
+                    // LU with partial pivoting of T - lam I (factors kept), applied to Z -> Y
+                    T        p0 = d[0] - lam, p1 = (n > 1) ? e[0] : T(0);
+                    unsigned bits = 0;
+                    for (int i = 0; i < n - 1; ++i) {
+                        const T s0 = e[i], s1 = d[i + 1] - lam, s2 = (i + 1 < n - 1) ? e[i + 1] : T(0);
+                        const T rs = AT(Z, i + 1) * sc;
+                        T       l;
+                        if (fabs(p0) >= fabs(s0)) {
+                            if (p0 == T(0)) p0 = pivtiny;
+                            l         = idiv(s0, p0);
+                            AT(U0, i) = p0;
+                            AT(U1, i) = p1;
+                            AT(Z, i)  = rp;
+                            p0        = s1 - l * p1;
+                            p1        = s2;
+                            rp        = rs - l * rp;
+                        } else {
+                            l         = idiv(p0, s0);
+                            AT(U0, i) = s0;
+                            AT(U1, i) = s1;
+                            AT(Z, i)  = rs;
+                            bits |= 1u << (i & 31);
+                            p0 = p1 - l * s1;
+                            p1 = -l * s2;
+                            rp = rp - l * rs;
+                        }
+                        AT(Lm, i) = l;
+                        if ((i & 31) == 31) {
+                            AT(SW, i >> 5) = bits;
+                            bits           = 0;
+                        }
                     }
-                    p0 = n0;
-                    p1 = n1;
-                    p2 = T(0);
-                    rp = nr;
+                    if (((n - 1) & 31) != 0) AT(SW, (n - 2) >> 5) = bits;
+                    ulast         = p0;
+                    AT(U0, n - 1) = p0;
+                } else {
+                    // the same elimination on the new right-hand side
+                    for (int i = 0; i < n - 1; ++i) {
+                        const T  rs = AT(Z, i + 1) * sc;
+                        const T  l  = AT(Lm, i);
+                        const bool sw = (AT(SW, i >> 5) >> (i & 31)) & 1u;
+                        AT(Z, i)      = sw ? rs : rp;
+                        rp            = sw ? rp - l * rs : rs - l * rp;
+                    }
+                    ulast = AT(U0, n - 1);
                 }
-                if (fabs(p0) < pivtiny) p0 = (p0 < T(0)) ? -pivtiny : pivtiny;
-                // back substitution into Z, scaled by the largest entry to stay in range
-                T z2 = T(0), z1 = idiv(rp, p0);
-                Z[(size_t)(n - 1) * 32 + lane] = z1;
-                T zmax = fabs(z1);
+                if (fabs(ulast) < pivtiny) ulast = (ulast < T(0)) ? -pivtiny : pivtiny;
+                // back substitution into Z with the 2-norm and the largest entry
+                T z2 = T(0), z1 = idiv(rp, ulast);
+                AT(Z, n - 1) = z1;
+                T ss = z1 * z1, zmax = fabs(z1);
                 for (int i = n - 2; i >= 0; --i) {
-                    T u0 = U0[(size_t)i * 32 + lane];
+                    T u0 = AT(U0, i);
                     if (fabs(u0) < pivtiny) u0 = (u0 < T(0)) ? -pivtiny : pivtiny;
-                    const T zi = idiv(Y[(size_t)i * 32 + lane] - U1[(size_t)i * 32 + lane] * z1 - U2[(size_t)i * 32 + lane] * z2, u0);
-                    Z[(size_t)i * 32 + lane] = zi;
-                    zmax = max(zmax, fabs(zi));
-                    z2   = z1;
-                    z1   = zi;
+                    const bool sw = (AT(SW, i >> 5) >> (i & 31)) & 1u;
+                    const T    u2 = (sw && i + 1 < n - 1) ? e[i + 1] : T(0);
+                    const T    zi = idiv(AT(Z, i) - AT(U1, i) * z1 - u2 * z2, u0);
+                    AT(Z, i)      = zi;
+                    ss            = fma(zi, zi, ss);
+                    zmax          = max(zmax, fabs(zi));
+                    z2            = z1;
+                    z1            = zi;
                 }
-                // normalise to unit 2-norm (first by the max entry, then exactly)
-                const T inv = (zmax > T(0) && isfinite(zmax)) ? T(1) / zmax : T(0);
-                if (!(zmax > T(0)) || !isfinite(zmax)) bad = true;
-                T ss = T(0);
-                for (int i = 0; i < n; ++i) {
-                    const T zi = Z[(size_t)i * 32 + lane] * inv;
-                    Z[(size_t)i * 32 + lane] = zi;
-                    ss = fma(zi, zi, ss);
+                if (!(zmax > T(0)) || !isfinite(zmax)) {
+                    bad = true;
+                    sc  = T(0);
+                } else if (zmax <= zsafe) {
+                    sc = isqrt_inv(ss);
+                } else {  // rescale by the largest entry before squaring
+                    const T inv = T(1) / zmax;
+                    ss          = T(0);
+                    for (int i = 0; i < n; ++i) {
+                        const T zi = AT(Z, i) * inv;
+                        AT(Z, i)   = zi;
+                        ss         = fma(zi, zi, ss);
+                    }
+                    sc = isqrt_inv(ss);
                 }
-                const T rn = (ss > T(0)) ? T(1) / sqrt(ss) : T(0);
-                for (int i = 0; i < n; ++i) Z[(size_t)i * 32 + lane] *= rn;
             }
-            __syncwarp();
-            // modified Gram-Schmidt inside clusters, in index order (warp-cooperative)
-            for (int q = 0; q < gn; ++q) {
-                const int jq = g0 + q;
-                const int gs = s_gs[warp][q];
-                if (gs >= jq) continue;
-                for (int p = gs; p < jq; ++p) {
-                    // previous vector: this group's Z column, or an earlier group's final output
-                    T dot = T(0);
-                    for (int i = lane; i < n; i += 32) {
-                        const T zp = (p >= g0) ? Z[(size_t)i * 32 + (p - g0)] : zb[(size_t)p * n + i];
-                        dot        = fma(zp, Z[(size_t)i * 32 + q], dot);
+            if (clus) {
+                // modified Gram-Schmidt inside clusters, in index order (warp-cooperative), on
+                // normalised vectors
+                if (active)
+                    for (int i = 0; i < n; ++i) AT(Z, i) *= sc;
+                sc = T(1);
+                __syncwarp();
+                for (int q = 0; q < gn; ++q) {
+                    const int jq = g0 + q;
+                    const int gs = s_gs[warp][q];
+                    if (gs >= jq) continue;
+                    for (int p = gs; p < jq; ++p) {
+                        // previous vector: this group's Z column, or an earlier group's final output
+                        T dot = T(0);
+                        for (int i = lane; i < n; i += 32) {
+                            const T zp = (p >= g0) ? Z[(size_t)i * LS + (p - g0)] : zb[(size_t)p * n + i];
+                            dot        = fma(zp, Z[(size_t)i * LS + q], dot);
+                        }
+                        dot = warp_sum(dot);
+                        for (int i = lane; i < n; i += 32) {
+                            const T zp = (p >= g0) ? Z[(size_t)i * LS + (p - g0)] : zb[(size_t)p * n + i];
+                            Z[(size_t)i * LS + q] -= dot * zp;
+                        }
+                        __syncwarp();
                     }
-                    dot = warp_sum(dot);
-                    for (int i = lane; i < n; i += 32) {
-                        const T zp = (p >= g0) ? Z[(size_t)i * 32 + (p - g0)] : zb[(size_t)p * n + i];
-                        Z[(size_t)i * 32 + q] -= dot * zp;
-                    }
+                    T ss = T(0);
+                    for (int i = lane; i < n; i += 32) ss = fma(Z[(size_t)i * LS + q], Z[(size_t)i * LS + q], ss);
+                    ss        = warp_sum(ss);
+                    const T r = (ss > T(0)) ? T(1) / sqrt(ss) : T(0);
+                    for (int i = lane; i < n; i += 32) Z[(size_t)i * LS + q] *= r;
                     __syncwarp();
                 }
-                T ss = T(0);
-                for (int i = lane; i < n; i += 32) ss = fma(Z[(size_t)i * 32 + q], Z[(size_t)i * 32 + q], ss);
-                ss        = warp_sum(ss);
-                const T r = (ss > T(0)) ? T(1) / sqrt(ss) : T(0);
-                for (int i = lane; i < n; i += 32) Z[(size_t)i * 32 + q] *= r;
-                __syncwarp();
             }
         }
-        // write this group's vectors ([j][i], coalesced over i)
-        for (int q = 0; q < gn; ++q)
-            for (int i = lane; i < n; i += 32) zb[(size_t)(g0 + q) * n + i] = Z[(size_t)i * 32 + q];
+        // write this group's vectors ([j][i], coalesced over i), with the pending scale
+        const T scq = sc;
+        __syncwarp();
+        for (int q = 0; q < gn; ++q) {
+            const T s = __shfl_sync(0xffffffffu, scq, q);
+            for (int i = lane; i < n; i += 32) zb[(size_t)(g0 + q) * n + i] = Z[(size_t)i * LS + q] * s;
+        }
         __syncwarp();
     }
+#undef AT
     bad = __any_sync(0xffffffffu, bad);
     if (bad && lane == 0 && status) status[b] |= 2;  // UEPM_K_NONFINITE
 }
@@ -378,7 +436,7 @@ __global__ void k_invit(const T* __restrict__ dIn, const T* __restrict__ eIn, co
 template <typename T>
 void launch_invit(const T* d, const T* e, const T* ev, int ev_ld, int n, int nb, T* work, T* z, int* status, int batch,
                   cudaStream_t s) {
-    const size_t smem = invit_smem_bytes<T>(n);
+    const size_t smem = invit_smem_bytes<T>(n, std::min(nb, 32));
     if (smem <= 200 * 1024) {
         auto kern = k_invit<T, true>;
         if (smem > 48 * 1024) cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);

@@ -36,7 +36,8 @@ void launch_bisect(const T* d, const T* e, int n, int nb, T* ev, int ev_ld, int 
 template <typename T>
 void launch_invit(const T* d, const T* e, const T* ev, int ev_ld, int n, int nb, T* work, T* z, int* status, int batch,
                   cudaStream_t s);
-// Inverse-iteration workspace per matrix: U0, U1, U2, Y, Z, each n x 32 interleaved by lane.
+// Inverse-iteration workspace per matrix (used where the arrays exceed shared memory): U0, U1, the
+// multipliers and Z, each n x 32 interleaved by lane, and the row-interchange bits.
 template <typename T>
 __host__ __device__ inline size_t invit_work_elems(int n) {
     return (size_t)5 * n * 32;
