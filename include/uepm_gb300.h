@@ -174,6 +174,52 @@ const char* uepm_kernel_name(int kind);
  * pure-FMA kernel. Used as the roofline denominator of the compute-bound kernels. */
 int uepm_measure_peak(int precision, double* tflops);
 
+/* ---- Tuning (no reference counterpart) -------------------------------------------------------
+ * Kernel-shape choices of a context. 0 in a field means "automatic":
+ *   fp32_reduction    1: register-resident FP32 reduction where the matrix fits (real, n <= 176),
+ *                     2: the shared/global-memory kernel
+ *   fp64_ctas_per_sm  CTAs per SM of the FP64 reduction (its L2 working set), 1..8
+ *   vector_lanes      lanes per eigenvector in the back-transformation: 8, 16 or 32
+ *   chunk             k-points per pipeline pass (smaller keeps H(k) resident in L2 between the
+ *                     kernels of a pass), 64..32768
+ * Every choice gives results within the parity tolerances; a given choice is deterministic.
+ * uepm_ctx_autotune times candidate shapes on sample_k seeded random first-zone k-points (coordinate
+ * descent over the four fields, CUDA events on `stream`) and keeps the fastest; results are cached
+ * process-wide per (device, n, real/complex, precision, nb, vectors) so that contexts of the same
+ * shape reuse them. It allocates and synchronises: call it before capturing work into a graph. */
+typedef struct uepm_tuning {
+    int32_t fp32_reduction;
+    int32_t fp64_ctas_per_sm;
+    int32_t vector_lanes;
+    int32_t chunk;
+} uepm_tuning;
+int uepm_ctx_get_tuning(const uepm_ctx* ctx, uepm_tuning* out);
+int uepm_ctx_set_tuning(uepm_ctx* ctx, const uepm_tuning* t);
+int uepm_ctx_autotune(uepm_ctx* ctx, int nb, uint32_t want, size_t sample_k, void* stream);
+
+/* ---- Uneven batches (no reference counterpart; the reference runs one material at a time,
+ * BandStructure::Compute_parallel, BandStructure.cpp:162-201) ---------------------------------
+ * A batch holds groups: (context, device k-points, nb, want, device outputs), each with the meaning
+ * and layout of uepm_solve_device. Contexts may differ in material, basis, SOC and precision.
+ * uepm_batch_run enqueues every group on `stream`: each distinct context gets its own internal
+ * stream (forked from and joined back to `stream`), so groups of different shapes run concurrently
+ * and fill the GPU together; groups of the same context run in order (they share its workspace).
+ * With graphs on (the default), the first run captures the whole fork/join pipeline into a CUDA
+ * graph and later runs replay it with one launch, as long as the groups are unchanged (the k-points
+ * and outputs are read and written through the registered device pointers at every run). Workspaces
+ * are allocated before capture. Adding or clearing groups drops the graph. Not thread-safe per
+ * batch; a context must not be used by another call while a run of the batch is in flight. */
+typedef struct uepm_batch uepm_batch;
+int  uepm_batch_create(uepm_batch** out);
+void uepm_batch_destroy(uepm_batch* b);
+int  uepm_batch_add(uepm_batch* b, uepm_ctx* ctx, const double* d_k, size_t nk, int nb, uint32_t want, double* d_E,
+                    double* d_X, double* d_grad, int32_t* d_status);
+int  uepm_batch_clear(uepm_batch* b);
+int  uepm_batch_set_graph(uepm_batch* b, int on);
+int  uepm_batch_run(uepm_batch* b, void* stream);
+/* Kernels enqueued by one run of the batch (counted while capturing). */
+uint64_t uepm_batch_kernels_per_run(const uepm_batch* b);
+
 #ifdef __cplusplus
 }
 #endif

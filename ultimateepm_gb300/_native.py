@@ -35,6 +35,8 @@ EXPORTED = [
     "uepm_ctx_set_workspace_limit", "uepm_solve", "uepm_solve_device", "uepm_assemble_device",
     "uepm_adjust_values", "uepm_kernel_launches", "uepm_ctx_set_profiling", "uepm_ctx_read_profile",
     "uepm_kernel_name", "uepm_measure_peak", "uepm_ctx_force_complex", "uepm_assemble_device_noalloc",
+    "uepm_ctx_get_tuning", "uepm_ctx_set_tuning", "uepm_ctx_autotune", "uepm_batch_create", "uepm_batch_destroy",
+    "uepm_batch_add", "uepm_batch_clear", "uepm_batch_set_graph", "uepm_batch_run", "uepm_batch_kernels_per_run",
 ]
 NOALLOC_SCRATCH_BYTES = 16 << 20
 KERNEL_KINDS = 10
@@ -56,6 +58,16 @@ class UepmMaterial(C.Structure):
         ("radial_extent_anion", C.c_double), ("radial_extent_cation", C.c_double),
         ("alpha_soc", C.c_double), ("mu_soc", C.c_double),
     ]
+
+
+class UepmTuning(C.Structure):
+    """struct uepm_tuning (include/uepm_gb300.h); 0 in a field means automatic."""
+
+    _fields_ = [("fp32_reduction", C.c_int32), ("fp64_ctas_per_sm", C.c_int32), ("vector_lanes", C.c_int32),
+                ("chunk", C.c_int32)]
+
+    def as_dict(self) -> dict:
+        return {f: getattr(self, f) for f, _ in self._fields_}
 
 
 class UepmError(RuntimeError):
@@ -108,6 +120,16 @@ def load():
             "uepm_measure_peak": (C.c_int, [C.c_int, dp]),
             "uepm_ctx_force_complex": (C.c_int, [vp, C.c_int]),
             "uepm_assemble_device_noalloc": (C.c_int, [vp, vp, C.c_size_t, vp, vp]),
+            "uepm_ctx_get_tuning": (C.c_int, [vp, C.POINTER(UepmTuning)]),
+            "uepm_ctx_set_tuning": (C.c_int, [vp, C.POINTER(UepmTuning)]),
+            "uepm_ctx_autotune": (C.c_int, [vp, C.c_int, C.c_uint32, C.c_size_t, vp]),
+            "uepm_batch_create": (C.c_int, [C.POINTER(vp)]),
+            "uepm_batch_destroy": (None, [vp]),
+            "uepm_batch_add": (C.c_int, [vp, vp, vp, C.c_size_t, C.c_int, C.c_uint32, vp, vp, vp, vp]),
+            "uepm_batch_clear": (C.c_int, [vp]),
+            "uepm_batch_set_graph": (C.c_int, [vp, C.c_int]),
+            "uepm_batch_run": (C.c_int, [vp, vp]),
+            "uepm_batch_kernels_per_run": (C.c_uint64, [vp]),
         }
         for name, (res, args) in sig.items():
             f = getattr(L, name)

@@ -143,28 +143,39 @@ static void bt_launch(const S* H, int n, int ld, size_t mstride, const S* tq, co
     count_launch();
 }
 
-// (lanes per vector, rows per lane): 8 lanes while a lane's rows fit about 40 register words, then
-// 16 and 32
+// (lanes per vector, rows per lane): automatic is 8 lanes while a lane's rows fit about 40 register
+// words, then 16 and 32; a requested lane count is honoured where its rows fit that budget.
 template <typename S>
 void launch_backtransform(const S* H, int n, int ld, size_t mstride, const S* tq, const typename ST<S>::R* z, int nb,
                           cx<typename ST<S>::R>* Xout, const DevParams& P, const double* d_k, const int* d_G, double* grad,
-                          int batch, cudaStream_t s) {
-    constexpr bool CX = sizeof(S) == 2 * sizeof(typename ST<S>::R);
+                          int batch, cudaStream_t s, int lanes) {
+    constexpr bool CX   = sizeof(S) == 2 * sizeof(typename ST<S>::R);
+    const int      tmax = CX ? 24 : 32;  // rows per lane within the register budget
+    if (lanes != 8 && lanes != 16 && lanes != 32) lanes = 0;
+    if (lanes && (n + lanes - 1) / lanes > tmax) lanes = 0;
+    if (!lanes) lanes = (n + 7) / 8 <= tmax ? 8 : (n + 15) / 16 <= tmax ? 16 : 32;
+    const int t = (n + lanes - 1) / lanes;
 #define UEPM_BT(L_, T_) bt_launch<S, L_, T_>(H, n, ld, mstride, tq, z, nb, Xout, P, d_k, d_G, grad, batch, s)
-    if (n <= 96) UEPM_BT(8, 12);
-    else if (n <= 144) UEPM_BT(8, 18);
-    else if (!CX && n <= 192) UEPM_BT(8, 24);
-    else if (!CX && n <= 256) UEPM_BT(8, 32);
-    else if (n <= 192) UEPM_BT(16, 12);
-    else if (n <= 256) UEPM_BT(16, 16);
-    else if (n <= 384) UEPM_BT(16, 24);
-    else UEPM_BT(32, 16);
+    if (lanes == 8) {
+        if (t <= 12) UEPM_BT(8, 12);
+        else if (t <= 18) UEPM_BT(8, 18);
+        else if (t <= 24) UEPM_BT(8, 24);
+        else UEPM_BT(8, 32);
+    } else if (lanes == 16) {
+        if (t <= 12) UEPM_BT(16, 12);
+        else if (t <= 18) UEPM_BT(16, 18);
+        else if (t <= 24) UEPM_BT(16, 24);
+        else UEPM_BT(16, 32);
+    } else {
+        if (t <= 12) UEPM_BT(32, 12);
+        else UEPM_BT(32, 18);
+    }
 #undef UEPM_BT
 }
 
 #define UEPM_BT_INST(S)                                                                                          \
     template void launch_backtransform<S>(const S*, int, int, size_t, const S*, const ST<S>::R*, int, cx<ST<S>::R>*, \
-                                          const DevParams&, const double*, const int*, double*, int, cudaStream_t);
+                                          const DevParams&, const double*, const int*, double*, int, cudaStream_t, int);
 UEPM_BT_INST(double)
 UEPM_BT_INST(float)
 UEPM_BT_INST(cx<double>)

@@ -16,6 +16,7 @@
 #include <string>
 #include <vector>
 
+#include "ctx_internal.h"
 #include "ctx_view.h"
 #include "uepm_common.cuh"
 #include "uepm_gb300.h"
@@ -28,6 +29,8 @@ static std::atomic<uint64_t>    g_launches{0};
 
 void set_error(const std::string& msg) { g_last_error = msg; }
 void count_launch(int n) { g_launches.fetch_add((uint64_t)n, std::memory_order_relaxed); }
+uint64_t launches_total() { return g_launches.load(); }
+void     uncount_launches(uint64_t n) { g_launches.fetch_sub(n, std::memory_order_relaxed); }
 
 // src/Common/physical_constants.hpp:18-44
 namespace pc {
@@ -46,40 +49,6 @@ constexpr size_t kMaxChunk = 32768;  // k-points per launch: the assembly grid's
 }  // namespace uepm
 
 using namespace uepm;
-
-struct uepm_ctx {
-    int           device    = 0;
-    uepm_material mat{};
-    DevParams     P{};
-    int           N = 0, n = 0;
-    uint32_t      flags     = 0;
-    int           precision = UEPM_PREC_FP64;
-    bool          real_h    = false;  // H(k) is exactly real for this material and flags
-    bool          force_cx  = false;  // run the complex kernels even when H(k) is real
-    bool          real      = false;  // real_h && !force_cx
-    size_t        ws_limit  = (size_t)8 << 30;
-    int*          d_G       = nullptr;
-    cx<double>*   d_Vloc    = nullptr;
-    double2*      d_phNL    = nullptr;
-    double2*      d_phSO    = nullptr;
-    void*         d_ws      = nullptr;
-    size_t        ws_bytes  = 0;
-    // buffers of the host-pointer entry point
-    cudaStream_t  stream    = nullptr;
-    void*         d_io      = nullptr;
-    size_t        io_bytes  = 0;
-    std::vector<int32_t> G;
-    // per-kernel timing (uepm_ctx_set_profiling)
-    struct Rec {
-        int         kind;
-        cudaEvent_t a, b;
-    };
-    int                      profiling = 0;
-    std::vector<Rec>         pending;
-    std::vector<cudaEvent_t> pool;
-    double                   prof_ms[UEPM_KERNEL_KINDS] = {0};
-    uint64_t                 prof_n[UEPM_KERNEL_KINDS]  = {0};
-};
 
 namespace uepm {
 bool ctx_tables(const uepm_ctx* ctx, CtxTables* out) {
@@ -264,7 +233,7 @@ void run_chunk(uepm_ctx* ctx, const Layout& L, char* ws, const double* kk, int c
         auto* tq = reinterpret_cast<S*>(ws + L.tq);
         {
             ProfScope p(ctx, s, KK_TRIDIAG64);
-            launch_tridiag<S>(H, n, n, mstride, d, e, tq, st, c, s);
+            launch_tridiag<S>(H, n, n, mstride, d, e, tq, st, c, s, 0, ctx->tune.fp64_ctas_per_sm);
         }
         {
             ProfScope p(ctx, s, KK_BISECT);
@@ -278,7 +247,7 @@ void run_chunk(uepm_ctx* ctx, const Layout& L, char* ws, const double* kk, int c
                 launch_invit<double>(d, e, E, nb, n, nb, work, z, st, c, s);
             }
             ProfScope p(ctx, s, KK_BACKTRANSFORM);
-            launch_backtransform<S>(H, n, n, mstride, tq, z, nb, Xo, ctx->P, kk, ctx->d_G, gr, c, s);
+            launch_backtransform<S>(H, n, n, mstride, tq, z, nb, Xo, ctx->P, kk, ctx->d_G, gr, c, s, ctx->tune.vector_lanes);
         }
         return;
     }
@@ -301,7 +270,7 @@ void run_chunk(uepm_ctx* ctx, const Layout& L, char* ws, const double* kk, int c
     auto* small = reinterpret_cast<S*>(ws + L.small);
     {
         ProfScope p(ctx, s, KK_TRIDIAG32);
-        launch_tridiag<S32>(H32, n, n, mstride, d, e, tq, st, c, s);
+        launch_tridiag<S32>(H32, n, n, mstride, d, e, tq, st, c, s, ctx->tune.fp32_reduction, 0);
     }
     {
         ProfScope p(ctx, s, KK_BISECT);
@@ -313,7 +282,8 @@ void run_chunk(uepm_ctx* ctx, const Layout& L, char* ws, const double* kk, int c
     }
     {
         ProfScope p(ctx, s, KK_BACKTRANSFORM);
-        launch_backtransform<S32>(H32, n, n, mstride, tq, z, m, X32, ctx->P, kk, ctx->d_G, nullptr, c, s);
+        launch_backtransform<S32>(H32, n, n, mstride, tq, z, m, X32, ctx->P, kk, ctx->d_G, nullptr, c, s,
+                                  ctx->tune.vector_lanes);
     }
     {
         ProfScope p(ctx, s, KK_REFINE_PROJECT);
@@ -331,6 +301,64 @@ void run_chunk(uepm_ctx* ctx, const Layout& L, char* ws, const double* kk, int c
 }
 
 }  // namespace
+
+namespace uepm {
+
+int ensure_workspace(uepm_ctx* ctx, size_t bytes) { return ensure_ws(ctx, bytes); }
+
+int plan_solve(uepm_ctx* ctx, size_t nk, int nb, uint32_t want, SolvePlan* out) {
+    if (nb < 1 || nb > ctx->n) {
+        set_error("nb must be in [1, n]");
+        return UEPM_ERR_OUT_OF_RANGE;
+    }
+    const bool mixed = ctx->precision == UEPM_PREC_MIXED;
+    const int  n     = ctx->n;
+    const int  m     = mixed ? std::min(n, nb + kGuardBands) : nb;
+    if (mixed && m > kRefineMaxSubspace) {
+        set_error("mixed precision supports at most " + std::to_string(kRefineMaxSubspace - kGuardBands) + " bands");
+        return UEPM_ERR_INVALID;
+    }
+    // chunk size from the workspace budget and the tuning
+    const size_t per   = plan(ctx, nb, want, 1).total;
+    size_t       chunk = std::max<size_t>(1, ctx->ws_limit / std::max<size_t>(per, 1));
+    const size_t cap   = ctx->tune.chunk > 0 ? std::min<size_t>((size_t)ctx->tune.chunk, kMaxChunk) : kMaxChunk;
+    chunk              = std::max<size_t>(1, std::min(std::min(chunk, nk), cap));
+    out->chunk         = chunk;
+    out->m             = m;
+    out->ws_bytes      = plan(ctx, nb, want, chunk).total;
+    return UEPM_OK;
+}
+
+int enqueue_solve(uepm_ctx* ctx, const SolvePlan& sp, const double* d_k, size_t nk, int nb, uint32_t want, double* d_E,
+                  double* d_X, double* d_grad, int32_t* d_status, cudaStream_t s) {
+    if (nk == 0) return UEPM_OK;
+    if (ctx->ws_bytes < sp.ws_bytes) {
+        set_error("enqueue_solve: workspace smaller than the plan");
+        return UEPM_ERR_RUNTIME;
+    }
+    const int    n     = ctx->n;
+    const size_t chunk = sp.chunk;
+    const Layout L     = plan(ctx, nb, want, chunk);
+    char*        ws    = static_cast<char*>(ctx->d_ws);
+    if (d_status) UEPM_CUDA(cudaMemsetAsync(d_status, 0, sizeof(int32_t) * nk, s));
+    const bool want_vec  = (want & UEPM_WANT_VECTORS) != 0;
+    const bool want_grad = (want & UEPM_WANT_GRADIENT) != 0;
+    int        rc;
+    for (size_t off = 0; off < nk; off += chunk) {
+        const int     c  = (int)std::min(chunk, nk - off);
+        const double* kk = d_k + 3 * off;
+        int*          st = d_status ? d_status + off : nullptr;
+        double*       E  = d_E + off * nb;
+        cx<double>*   Xo = want_vec ? reinterpret_cast<cx<double>*>(d_X) + off * nb * n : nullptr;
+        double*       gr = want_grad ? d_grad + off * nb * 3 : nullptr;
+        if (ctx->real) run_chunk<double>(ctx, L, ws, kk, c, nb, sp.m, want_vec || want_grad, E, Xo, gr, st, s);
+        else run_chunk<cx<double>>(ctx, L, ws, kk, c, nb, sp.m, want_vec || want_grad, E, Xo, gr, st, s);
+        if ((rc = check_launch())) return rc;
+    }
+    return UEPM_OK;
+}
+
+}  // namespace uepm
 
 extern "C" {
 
@@ -524,10 +552,6 @@ int uepm_solve_device(uepm_ctx* ctx, const double* d_k, size_t nk, int nb, uint3
         set_error("uepm_solve_device: null argument");
         return UEPM_ERR_INVALID;
     }
-    if (nb < 1 || nb > ctx->n) {
-        set_error("uepm_solve_device: nb must be in [1, n]");
-        return UEPM_ERR_OUT_OF_RANGE;
-    }
     if ((want & UEPM_WANT_VECTORS) && !d_X) {
         set_error("uepm_solve_device: UEPM_WANT_VECTORS without an X buffer");
         return UEPM_ERR_INVALID;
@@ -536,40 +560,11 @@ int uepm_solve_device(uepm_ctx* ctx, const double* d_k, size_t nk, int nb, uint3
         set_error("uepm_solve_device: UEPM_WANT_GRADIENT without a gradient buffer");
         return UEPM_ERR_INVALID;
     }
-    const bool mixed = ctx->precision == UEPM_PREC_MIXED;
-    const int  n     = ctx->n;
-    const int  m     = mixed ? std::min(n, nb + kGuardBands) : nb;
-    if (mixed && m > kRefineMaxSubspace) {
-        set_error("mixed precision supports at most " + std::to_string(kRefineMaxSubspace - kGuardBands) + " bands");
-        return UEPM_ERR_INVALID;
-    }
-    if (nk == 0) return UEPM_OK;
-    cudaStream_t s = (cudaStream_t)stream;
-
-    // chunk size from the workspace budget
-    const size_t per   = plan(ctx, nb, want, 1).total;
-    size_t       chunk = std::max<size_t>(1, ctx->ws_limit / std::max<size_t>(per, 1));
-    chunk              = std::min(std::min(chunk, nk), kMaxChunk);
-    const Layout L     = plan(ctx, nb, want, chunk);
-    int          rc    = ensure_ws(ctx, L.total);
-    if (rc) return rc;
-    char* ws = static_cast<char*>(ctx->d_ws);
-    if (d_status) UEPM_CUDA(cudaMemsetAsync(d_status, 0, sizeof(int32_t) * nk, s));
-
-    const bool want_vec  = (want & UEPM_WANT_VECTORS) != 0;
-    const bool want_grad = (want & UEPM_WANT_GRADIENT) != 0;
-    for (size_t off = 0; off < nk; off += chunk) {
-        const int     c  = (int)std::min(chunk, nk - off);
-        const double* kk = d_k + 3 * off;
-        int*          st = d_status ? d_status + off : nullptr;
-        double*       E  = d_E + off * nb;
-        cx<double>*   Xo = want_vec ? reinterpret_cast<cx<double>*>(d_X) + off * nb * n : nullptr;
-        double*       gr = want_grad ? d_grad + off * nb * 3 : nullptr;
-        if (ctx->real) run_chunk<double>(ctx, L, ws, kk, c, nb, m, want_vec || want_grad, E, Xo, gr, st, s);
-        else run_chunk<cx<double>>(ctx, L, ws, kk, c, nb, m, want_vec || want_grad, E, Xo, gr, st, s);
-        if ((rc = check_launch())) return rc;
-    }
-    return UEPM_OK;
+    SolvePlan plan;
+    int       rc = plan_solve(ctx, nk, nb, want, &plan);
+    if (rc || nk == 0) return rc;
+    if ((rc = ensure_workspace(ctx, plan.ws_bytes))) return rc;
+    return enqueue_solve(ctx, plan, d_k, nk, nb, want, d_E, d_X, d_grad, d_status, (cudaStream_t)stream);
 }
 
 int uepm_assemble_device(uepm_ctx* ctx, const double* d_k, size_t nk, double* d_H, void* stream) {

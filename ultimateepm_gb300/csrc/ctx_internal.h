@@ -1,0 +1,67 @@
+// ctx_internal.h -- the context behind the C ABI handle, and the solve entry points shared by the
+// C ABI (capi.cu) and the batch / autotuning runtime (batch.cu). Not part of the public interface.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <string>
+#include <vector>
+
+#include "uepm_common.cuh"
+#include "uepm_gb300.h"
+
+struct uepm_ctx {
+    int           device    = 0;
+    uepm_material mat{};
+    uepm::DevParams P{};
+    int           N = 0, n = 0;
+    uint32_t      flags     = 0;
+    int           precision = UEPM_PREC_FP64;
+    bool          real_h    = false;  // H(k) is exactly real for this material and flags
+    bool          force_cx  = false;  // run the complex kernels even when H(k) is real
+    bool          real      = false;  // real_h && !force_cx
+    size_t        ws_limit  = (size_t)8 << 30;
+    uepm_tuning   tune{};  // kernel-shape choices (0: automatic)
+    int*          d_G       = nullptr;
+    uepm::cx<double>* d_Vloc    = nullptr;
+    double2*      d_phNL    = nullptr;
+    double2*      d_phSO    = nullptr;
+    void*         d_ws      = nullptr;
+    size_t        ws_bytes  = 0;
+    // buffers of the host-pointer entry point
+    cudaStream_t  stream    = nullptr;
+    void*         d_io      = nullptr;
+    size_t        io_bytes  = 0;
+    std::vector<int32_t> G;
+    // per-kernel timing (uepm_ctx_set_profiling)
+    struct Rec {
+        int         kind;
+        cudaEvent_t a, b;
+    };
+    int                      profiling = 0;
+    std::vector<Rec>         pending;
+    std::vector<cudaEvent_t> pool;
+    double                   prof_ms[UEPM_KERNEL_KINDS] = {0};
+    uint64_t                 prof_n[UEPM_KERNEL_KINDS]  = {0};
+};
+
+namespace uepm {
+
+void set_error(const std::string& msg);
+
+// Workspace plan of one pipeline pass: chunk (k-points per pass) and the bytes it needs.
+struct SolvePlan {
+    size_t chunk = 0, ws_bytes = 0;
+    int    m     = 0;
+};
+// Validates nb / want against the context and plans the passes of an nk-point solve (no allocation).
+int plan_solve(uepm_ctx* ctx, size_t nk, int nb, uint32_t want, SolvePlan* out);
+// Grows the context's device workspace to at least `bytes` (allocates: not while capturing).
+int ensure_workspace(uepm_ctx* ctx, size_t bytes);
+// Enqueues the solve on s; the workspace must hold plan.ws_bytes. No allocation, no host sync.
+int enqueue_solve(uepm_ctx* ctx, const SolvePlan& plan, const double* d_k, size_t nk, int nb, uint32_t want, double* d_E,
+                  double* d_X, double* d_grad, int32_t* d_status, cudaStream_t s);
+uint64_t launches_total();
+void     uncount_launches(uint64_t n);
+
+}  // namespace uepm

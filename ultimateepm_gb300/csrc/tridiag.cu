@@ -223,7 +223,7 @@ static int sm_count() {
 
 template <typename S, int NT, int MAXT, bool SMEM>
 static void tridiag_launch_t(S* H, int n, int ld, size_t mstride, typename ST<S>::R* d, typename ST<S>::R* e, S* tq,
-                             int* status, int batch, cudaStream_t s) {
+                             int* status, int batch, cudaStream_t s, int ctas_per_sm) {
     using R           = typename ST<S>::R;
     const size_t smem = sizeof(S) * ((SMEM ? (size_t)n * (n | 1) : 0) + (size_t)(2 + NT / 32) * n) + sizeof(R) * 3 * (NT / 32);
     auto         kern = k_tridiag<S, NT, MAXT, SMEM>;
@@ -232,9 +232,10 @@ static void tridiag_launch_t(S* H, int n, int ld, size_t mstride, typename ST<S>
     if (!SMEM) {
         // keep the matrices in flight within ~96 MB so that they stay resident in the 129 MB L2:
         // each step re-reads the whole trailing matrix
-        const size_t bytes = sizeof(S) * (size_t)n * n;
-        const int    per_sm = (int)std::max<size_t>(1, std::min<size_t>(8, (96u << 20) / (bytes * (size_t)sm_count())));
-        grid                = std::min(batch, per_sm * sm_count());
+        const size_t bytes  = sizeof(S) * (size_t)n * n;
+        int          per_sm = (int)std::max<size_t>(1, std::min<size_t>(8, (96u << 20) / (bytes * (size_t)sm_count())));
+        if (ctas_per_sm > 0) per_sm = std::min(ctas_per_sm, 8);
+        grid = std::min(batch, per_sm * sm_count());
     }
     kern<<<grid, NT, smem, s>>>(H, n, ld, mstride, d, e, tq, status, batch);
     count_launch();
@@ -249,31 +250,31 @@ static bool use_smem(int n) {
 
 template <typename S, int MAXT>
 static void tridiag_pick(S* H, int n, int ld, size_t mstride, typename ST<S>::R* d, typename ST<S>::R* e, S* tq,
-                         int* status, int batch, cudaStream_t s) {
-    if (use_smem<S>(n)) tridiag_launch_t<S, 256, MAXT, true>(H, n, ld, mstride, d, e, tq, status, batch, s);
-    else tridiag_launch_t<S, 256, MAXT, false>(H, n, ld, mstride, d, e, tq, status, batch, s);
+                         int* status, int batch, cudaStream_t s, int ctas_per_sm) {
+    if (use_smem<S>(n)) tridiag_launch_t<S, 256, MAXT, true>(H, n, ld, mstride, d, e, tq, status, batch, s, ctas_per_sm);
+    else tridiag_launch_t<S, 256, MAXT, false>(H, n, ld, mstride, d, e, tq, status, batch, s, ctas_per_sm);
 }
 
 template <typename S>
 void launch_tridiag(S* H, int n, int ld, size_t mstride, typename ST<S>::R* d, typename ST<S>::R* e, S* tq, int* status,
-                    int batch, cudaStream_t s) {
+                    int batch, cudaStream_t s, int variant, int ctas_per_sm) {
     if constexpr (std::is_same<S, float>::value) {
-        if (n <= tridiag_reg_max_n()) {
+        if (variant != 2 && n <= tridiag_reg_max_n()) {
             launch_tridiag_reg(H, n, ld, mstride, d, e, tq, status, batch, s);
             return;
         }
     }
     // rows of the trailing matrix are at most n - 1 <= 32 * MAXT
-    if (n <= 129) tridiag_pick<S, 4>(H, n, ld, mstride, d, e, tq, status, batch, s);
-    else if (n <= 161) tridiag_pick<S, 5>(H, n, ld, mstride, d, e, tq, status, batch, s);
-    else if (n <= 257) tridiag_pick<S, 8>(H, n, ld, mstride, d, e, tq, status, batch, s);
-    else if (n <= 385) tridiag_pick<S, 12>(H, n, ld, mstride, d, e, tq, status, batch, s);
-    else tridiag_pick<S, 16>(H, n, ld, mstride, d, e, tq, status, batch, s);
+    if (n <= 129) tridiag_pick<S, 4>(H, n, ld, mstride, d, e, tq, status, batch, s, ctas_per_sm);
+    else if (n <= 161) tridiag_pick<S, 5>(H, n, ld, mstride, d, e, tq, status, batch, s, ctas_per_sm);
+    else if (n <= 257) tridiag_pick<S, 8>(H, n, ld, mstride, d, e, tq, status, batch, s, ctas_per_sm);
+    else if (n <= 385) tridiag_pick<S, 12>(H, n, ld, mstride, d, e, tq, status, batch, s, ctas_per_sm);
+    else tridiag_pick<S, 16>(H, n, ld, mstride, d, e, tq, status, batch, s, ctas_per_sm);
 }
 
-template void launch_tridiag<cx<double>>(cx<double>*, int, int, size_t, double*, double*, cx<double>*, int*, int, cudaStream_t);
-template void launch_tridiag<cx<float>>(cx<float>*, int, int, size_t, float*, float*, cx<float>*, int*, int, cudaStream_t);
-template void launch_tridiag<double>(double*, int, int, size_t, double*, double*, double*, int*, int, cudaStream_t);
-template void launch_tridiag<float>(float*, int, int, size_t, float*, float*, float*, int*, int, cudaStream_t);
+template void launch_tridiag<cx<double>>(cx<double>*, int, int, size_t, double*, double*, cx<double>*, int*, int, cudaStream_t, int, int);
+template void launch_tridiag<cx<float>>(cx<float>*, int, int, size_t, float*, float*, cx<float>*, int*, int, cudaStream_t, int, int);
+template void launch_tridiag<double>(double*, int, int, size_t, double*, double*, double*, int*, int, cudaStream_t, int, int);
+template void launch_tridiag<float>(float*, int, int, size_t, float*, float*, float*, int*, int, cudaStream_t, int, int);
 
 }  // namespace uepm

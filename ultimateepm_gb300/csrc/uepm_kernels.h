@@ -21,9 +21,12 @@ void launch_assemble(const DevParams& P, const cx<double>* Vloc, const double2* 
 
 // tridiag.cu: Householder reduction in place. d, e: [batch][n]; tq: [batch][n] reflector scalars;
 // status: [batch] (ORed with UEPM_K_NONFINITE on NaN/Inf).
+// variant: 0 automatic (register-resident FP32 kernel where it fits), 1 register-resident where it
+// fits, 2 shared/global-memory kernel; ctas_per_sm (0: automatic) caps the persistent grid of the
+// global-memory kernel.
 template <typename S>
 void launch_tridiag(S* H, int n, int ld, size_t mstride, typename ST<S>::R* d, typename ST<S>::R* e, S* tq, int* status,
-                    int batch, cudaStream_t s);
+                    int batch, cudaStream_t s, int variant = 0, int ctas_per_sm = 0);
 // tridiag_reg.cu: the same reduction for real FP32 matrices with n <= tridiag_reg_max_n(), held in
 // registers (launch_tridiag<float> dispatches to it).
 int  tridiag_reg_max_n();
@@ -48,7 +51,7 @@ __host__ __device__ inline size_t invit_work_elems(int n) {
 template <typename S>
 void launch_backtransform(const S* H, int n, int ld, size_t mstride, const S* tq, const typename ST<S>::R* z, int nb,
                           cx<typename ST<S>::R>* Xout, const DevParams& P, const double* d_k, const int* d_G, double* grad,
-                          int batch, cudaStream_t s);
+                          int batch, cudaStream_t s, int lanes = 0);
 
 // refine.cu: FP64 Rayleigh-Ritz in the m-dimensional subspace of FP32 vectors X32 ([batch][m][n]);
 // the nb lowest Ritz values go to Eout, optionally vectors / gradients.
