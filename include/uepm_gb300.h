@@ -220,6 +220,34 @@ int  uepm_batch_run(uepm_batch* b, void* stream);
 /* Kernels enqueued by one run of the batch (counted while capturing). */
 uint64_t uepm_batch_kernels_per_run(const uepm_batch* b);
 
+/* ---- Serving (no reference counterpart; the reference's full-band Monte Carlo interpolates bands
+ * on a mesh, src/FBMC/particle.cpp:52-63) -------------------------------------------------------
+ * A query server over resident contexts (all on one device; not owned: keep them alive and unused
+ * by other calls until the server is destroyed). A scheduler thread cuts each request into work
+ * items of at most max_chunk k-points and runs them on `slots` streams, admitting an item only when
+ * a slot is free and a sub-range of the device arena (hbm_budget bytes, allocated here once) can hold
+ * its footprint: the solve workspace plus its k-points, energies and status. Items of requests that
+ * arrive while others run are admitted as slots and memory free up (continuous batching); results
+ * are the same whether a request runs alone or in the mix.
+ * uepm_server_submit copies k (nk x 3, reduced units) and returns a request id (>= 0) at once; the
+ * server writes E (nk x nb, eV), status (nk, optional) and, with UEPM_SERVE_VELOCITY, the group
+ * velocities V (nk x nb x 3, m/s) by central differences of step fd_step (reduced units) along each
+ * axis (7 solves per k-point). The host buffers must stay valid until uepm_server_wait returns for the
+ * id (UEPM_OK when done, 1 on timeout; timeout_s < 0 waits indefinitely). uepm_server_stats reports
+ * the latency (submission to completion) percentiles of the requests completed since the last reset,
+ * how many, their k-points and the span from the first submission to the last completion. */
+#define UEPM_SERVE_VELOCITY 1u
+typedef struct uepm_server uepm_server;
+int     uepm_server_create(uepm_ctx* const* ctxs, int nctx, size_t hbm_budget, int slots, size_t max_chunk, int max_nb,
+                           uepm_server** out);
+int     uepm_server_destroy(uepm_server* sv);
+int64_t uepm_server_submit(uepm_server* sv, int ctx_index, const double* k, size_t nk, int nb, uint32_t flags,
+                           double fd_step, double* E, double* V, int32_t* status);
+int     uepm_server_wait(uepm_server* sv, int64_t id, double timeout_s);
+int     uepm_server_stats(uepm_server* sv, double* p50_ms, double* p99_ms, uint64_t* completed, uint64_t* kpoints,
+                          double* span_s);
+int     uepm_server_reset_stats(uepm_server* sv);
+
 #ifdef __cplusplus
 }
 #endif

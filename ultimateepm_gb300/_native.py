@@ -37,7 +37,10 @@ EXPORTED = [
     "uepm_kernel_name", "uepm_measure_peak", "uepm_ctx_force_complex", "uepm_assemble_device_noalloc",
     "uepm_ctx_get_tuning", "uepm_ctx_set_tuning", "uepm_ctx_autotune", "uepm_batch_create", "uepm_batch_destroy",
     "uepm_batch_add", "uepm_batch_clear", "uepm_batch_set_graph", "uepm_batch_run", "uepm_batch_kernels_per_run",
+    "uepm_server_create", "uepm_server_destroy", "uepm_server_submit", "uepm_server_wait", "uepm_server_stats",
+    "uepm_server_reset_stats",
 ]
+UEPM_SERVE_VELOCITY = 1
 NOALLOC_SCRATCH_BYTES = 16 << 20
 KERNEL_KINDS = 10
 
@@ -130,6 +133,14 @@ def load():
             "uepm_batch_set_graph": (C.c_int, [vp, C.c_int]),
             "uepm_batch_run": (C.c_int, [vp, vp]),
             "uepm_batch_kernels_per_run": (C.c_uint64, [vp]),
+            "uepm_server_create": (C.c_int, [C.POINTER(vp), C.c_int, C.c_size_t, C.c_int, C.c_size_t, C.c_int,
+                                             C.POINTER(vp)]),
+            "uepm_server_destroy": (C.c_int, [vp]),
+            "uepm_server_submit": (C.c_int64, [vp, C.c_int, dp, C.c_size_t, C.c_int, C.c_uint32, C.c_double, dp, dp,
+                                               ip]),
+            "uepm_server_wait": (C.c_int, [vp, C.c_int64, C.c_double]),
+            "uepm_server_stats": (C.c_int, [vp, dp, dp, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64), dp]),
+            "uepm_server_reset_stats": (C.c_int, [vp]),
         }
         for name, (res, args) in sig.items():
             f = getattr(L, name)

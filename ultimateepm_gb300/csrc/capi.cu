@@ -330,16 +330,16 @@ int plan_solve(uepm_ctx* ctx, size_t nk, int nb, uint32_t want, SolvePlan* out) 
 }
 
 int enqueue_solve(uepm_ctx* ctx, const SolvePlan& sp, const double* d_k, size_t nk, int nb, uint32_t want, double* d_E,
-                  double* d_X, double* d_grad, int32_t* d_status, cudaStream_t s) {
+                  double* d_X, double* d_grad, int32_t* d_status, cudaStream_t s, void* ws_ext, size_t ws_ext_bytes) {
     if (nk == 0) return UEPM_OK;
-    if (ctx->ws_bytes < sp.ws_bytes) {
+    if ((ws_ext ? ws_ext_bytes : ctx->ws_bytes) < sp.ws_bytes) {
         set_error("enqueue_solve: workspace smaller than the plan");
         return UEPM_ERR_RUNTIME;
     }
     const int    n     = ctx->n;
     const size_t chunk = sp.chunk;
     const Layout L     = plan(ctx, nb, want, chunk);
-    char*        ws    = static_cast<char*>(ctx->d_ws);
+    char*        ws    = static_cast<char*>(ws_ext ? ws_ext : ctx->d_ws);
     if (d_status) UEPM_CUDA(cudaMemsetAsync(d_status, 0, sizeof(int32_t) * nk, s));
     const bool want_vec  = (want & UEPM_WANT_VECTORS) != 0;
     const bool want_grad = (want & UEPM_WANT_GRADIENT) != 0;

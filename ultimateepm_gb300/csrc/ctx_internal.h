@@ -58,9 +58,12 @@ struct SolvePlan {
 int plan_solve(uepm_ctx* ctx, size_t nk, int nb, uint32_t want, SolvePlan* out);
 // Grows the context's device workspace to at least `bytes` (allocates: not while capturing).
 int ensure_workspace(uepm_ctx* ctx, size_t bytes);
-// Enqueues the solve on s; the workspace must hold plan.ws_bytes. No allocation, no host sync.
+// Enqueues the solve on s; the workspace (the context's own, or ws / ws_bytes when given, so that
+// several solves of one context can be in flight at once) must hold plan.ws_bytes. No allocation,
+// no host sync.
 int enqueue_solve(uepm_ctx* ctx, const SolvePlan& plan, const double* d_k, size_t nk, int nb, uint32_t want, double* d_E,
-                  double* d_X, double* d_grad, int32_t* d_status, cudaStream_t s);
+                  double* d_X, double* d_grad, int32_t* d_status, cudaStream_t s, void* ws = nullptr,
+                  size_t ws_bytes = 0);
 uint64_t launches_total();
 void     uncount_launches(uint64_t n);
 
