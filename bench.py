@@ -306,7 +306,86 @@ def run_ours(args):
                                    f"{cpu_dt:.1f} s, FP64 eigenvalues only"},
         "clocks": clk,
     }
+    if ws == 1 and not args.no_extras:
+        out["uneven_batch"] = run_uneven_batch(args)
+        out["serve"] = run_serve()
     emit(out)
+
+
+def run_uneven_batch(args, steps: int = 3, warmup: int = 2, total_k: int = 16384, seed: int = 20261203):
+    """The uneven mixed-material batch: 8 contexts (orders 89..458, real and complex, SOC on for four),
+    total_k first-zone k-points split by seeded multinomial proportions, 16 bands, mixed precision,
+    run as one uepm_batch (per-context streams; replayed CUDA graph after the first two runs).
+    Returns k-points/s over the whole batch with the per-group split."""
+    import torch
+
+    from ultimateepm_gb300 import _native as N
+    from ultimateepm_gb300.serve import MIXED_SET, make_contexts, sample_bz
+
+    L = N.load()
+    rng = np.random.default_rng(seed)
+    ctxs = make_contexts(N.UEPM_PREC_MIXED)
+    orders = [int(c.n) for c in ctxs]
+    counts = rng.multinomial(total_k, rng.dirichlet(np.ones(len(ctxs))))
+    s = torch.cuda.current_stream()
+    sp = C.c_void_p(s.cuda_stream)
+    bufs = []
+    b = C.c_void_p()
+    N.check(L.uepm_batch_create(C.byref(b)))
+    try:
+        for ctx, nk in zip(ctxs, counts):
+            if nk == 0:
+                continue
+            dk = torch.from_numpy(sample_bz(int(nk), rng)).cuda()
+            dE = torch.zeros((int(nk), NB), dtype=torch.float64, device="cuda")
+            ds = torch.zeros(int(nk), dtype=torch.int32, device="cuda")
+            bufs.append((dk, dE, ds))
+            N.check(L.uepm_batch_add(b, ctx.h, C.c_void_p(dk.data_ptr()), int(nk), NB, N.UEPM_WANT_VALUES,
+                                     C.c_void_p(dE.data_ptr()), None, None, C.c_void_p(ds.data_ptr())))
+        for _ in range(warmup):
+            N.check(L.uepm_batch_run(b, sp))
+        torch.cuda.synchronize()
+        a, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(s)
+        for _ in range(steps):
+            N.check(L.uepm_batch_run(b, sp))
+        e.record(s)
+        e.synchronize()
+        ms = a.elapsed_time(e) / steps
+        assert not any(ds.any().item() for _, _, ds in bufs), "a k-point reported a non-zero status"
+        kpr = int(L.uepm_batch_kernels_per_run(b))
+    finally:
+        L.uepm_batch_destroy(b)
+        for c in ctxs:
+            c.close()
+    return {"value": total_k / (ms * 1e-3), "unit": "k-points/s", "ms_per_step": ms, "steps": steps,
+            "workload": f"{total_k} seeded first-zone k-points over 8 (material, cutoff, SOC) groups, 16 bands, "
+                        "mixed precision, one uepm_batch (CUDA graph replay)",
+            "groups": [{"material": m, "shells": sh, "soc": so, "order": o, "k_points": int(nk)}
+                       for (m, sh, so), o, nk in zip(MIXED_SET, orders, counts)],
+            "kernels_per_step": kpr, "graph": True}
+
+
+def run_serve(rate: float = 4.0, requests: int = 16, kmax: int = 1000, seed: int = 20261203):
+    """Serving at a stated load: seeded Poisson arrivals, each request for a random group of the
+    mixed-material set, log-uniform 1..kmax k-points, 8..16 bands and finite-difference group
+    velocities (7 solves per k-point), mixed precision, 4 slots, 16 GB arena."""
+    from ultimateepm_gb300 import _native as N
+    from ultimateepm_gb300.serve import Server, make_contexts, poisson_requests, run_load
+
+    ctxs = make_contexts(N.UEPM_PREC_MIXED)
+    srv = Server(ctxs, hbm_budget=16 << 30, slots=4, max_chunk=512)
+    try:
+        run_load(srv, poisson_requests(4, 50.0, seed + 7, len(ctxs), 1, 64), seed=seed + 7)  # warm-up
+        res = run_load(srv, poisson_requests(requests, rate, seed, len(ctxs), 1, kmax), seed=seed)
+    finally:
+        srv.close()
+        for c in ctxs:
+            c.close()
+    res.update({"rate_req_per_s": rate, "k_per_request": f"log-uniform 1..{kmax}", "bands": "8..16",
+                "velocities": "central differences, h = 1e-4 (reduced units)", "precision": "mixed",
+                "slots": 4, "hbm_budget_gb": 16})
+    return res
 
 
 def run_reference(args):
@@ -347,6 +426,7 @@ def main():
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", choices=["ours", "reference"], default="ours")
     p.add_argument("--cpu-budget", type=float, default=10.0, help="seconds of oracle timing for cpu_baseline")
+    p.add_argument("--no-extras", action="store_true", help="skip the uneven-batch and serving sub-measurements")
     args = p.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
