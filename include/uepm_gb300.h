@@ -178,7 +178,8 @@ int uepm_measure_peak(int precision, double* tflops);
  * Kernel-shape choices of a context. 0 in a field means "automatic":
  *   fp32_reduction    1: register-resident FP32 reduction where the matrix fits (real, n <= 176),
  *                     2: the shared/global-memory kernel
- *   fp64_ctas_per_sm  CTAs per SM of the FP64 reduction (its L2 working set), 1..8
+ *   fp64_ctas_per_sm  CTAs per SM of the global-memory reduction (every FP64 reduction, and FP32
+ *                     matrices too large for the on-chip kernels): its L2 working set, 1..8
  *   vector_lanes      lanes per eigenvector in the back-transformation: 8, 16 or 32
  *   chunk             k-points per pipeline pass (smaller keeps H(k) resident in L2 between the
  *                     kernels of a pass), 64..32768

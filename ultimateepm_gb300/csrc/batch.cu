@@ -181,7 +181,7 @@ int uepm_ctx_autotune(uepm_ctx* ctx, int nb, uint32_t want, size_t sample_k, voi
     std::vector<int> chunks, ctas, reds, lanes;
     for (int c : {256, 512, 1024, 2048, 4096, 8192})
         if ((size_t)c < sample_k) chunks.push_back(c);
-    if (!mixed) ctas = {1, 2, 3, 4, 6, 8};
+    if (!mixed || !(ctx->real && ctx->n <= tridiag_reg_max_n())) ctas = {1, 2, 3, 4, 6, 8};
     if (mixed && ctx->real && ctx->n <= tridiag_reg_max_n()) reds = {2};
     if (mixed || wv || wg)
         for (int l : {8, 16, 32})

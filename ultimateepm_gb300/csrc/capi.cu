@@ -270,7 +270,7 @@ void run_chunk(uepm_ctx* ctx, const Layout& L, char* ws, const double* kk, int c
     auto* small = reinterpret_cast<S*>(ws + L.small);
     {
         ProfScope p(ctx, s, KK_TRIDIAG32);
-        launch_tridiag<S32>(H32, n, n, mstride, d, e, tq, st, c, s, ctx->tune.fp32_reduction, 0);
+        launch_tridiag<S32>(H32, n, n, mstride, d, e, tq, st, c, s, ctx->tune.fp32_reduction, ctx->tune.fp64_ctas_per_sm);
     }
     {
         ProfScope p(ctx, s, KK_BISECT);

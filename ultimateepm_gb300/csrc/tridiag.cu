@@ -230,10 +230,11 @@ static void tridiag_launch_t(S* H, int n, int ld, size_t mstride, typename ST<S>
     if (smem > 48 * 1024) cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     int grid = batch;
     if (!SMEM) {
-        // keep the matrices in flight within ~96 MB so that they stay resident in the 129 MB L2:
-        // each step re-reads the whole trailing matrix
+        // automatic: keep the matrices in flight within ~96 MB so that they stay in the 129 MB L2, but
+        // never below 4 CTAs per SM: for large (complex / spin-orbit) matrices, latency hiding wins
+        // over L2 residency (measured 1.5-2x over 1 CTA per SM at n = 178..458, FP32)
         const size_t bytes  = sizeof(S) * (size_t)n * n;
-        int          per_sm = (int)std::max<size_t>(1, std::min<size_t>(8, (96u << 20) / (bytes * (size_t)sm_count())));
+        int          per_sm = (int)std::max<size_t>(4, std::min<size_t>(8, (96u << 20) / (bytes * (size_t)sm_count())));
         if (ctas_per_sm > 0) per_sm = std::min(ctas_per_sm, 8);
         grid = std::min(batch, per_sm * sm_count());
     }
