@@ -176,23 +176,27 @@ int uepm_measure_peak(int precision, double* tflops);
 
 /* ---- Tuning (no reference counterpart) -------------------------------------------------------
  * Kernel-shape choices of a context. 0 in a field means "automatic":
- *   fp32_reduction    1: register-resident FP32 reduction where the matrix fits (real, n <= 176),
- *                     2: the shared/global-memory kernel
- *   fp64_ctas_per_sm  CTAs per SM of the global-memory reduction (every FP64 reduction, and FP32
- *                     matrices too large for the on-chip kernels): its L2 working set, 1..8
- *   vector_lanes      lanes per eigenvector in the back-transformation: 8, 16 or 32
- *   chunk             k-points per pipeline pass (smaller keeps H(k) resident in L2 between the
- *                     kernels of a pass), 64..32768
+ *   reduction     the Householder reduction kernel: 1 register-resident (FP32 real matrices, n <= 176),
+ *                 2 one CTA per matrix (shared memory where the matrix fits, else global memory with
+ *                 a persistent grid), 3 one thread-block cluster per matrix, the matrix spread over
+ *                 the cluster's shared memory (orders beyond one SM); automatic: 1 where it applies,
+ *                 3 for complex FP32 matrices just beyond one SM (n <= 300), else 2
+ *   ctas_per_sm   CTAs per SM of the global-memory reduction (its L2 working set), 1..8
+ *   vector_lanes  lanes per eigenvector in the back-transformation: 8, 16 or 32
+ *   chunk         k-points per pipeline pass (smaller keeps H(k) resident in L2 between the
+ *                 kernels of a pass), 64..32768
+ *   cluster       CTAs per cluster of reduction 3: 2, 4, 8 or 16
  * Every choice gives results within the parity tolerances; a given choice is deterministic.
  * uepm_ctx_autotune times candidate shapes on sample_k seeded random first-zone k-points (coordinate
- * descent over the four fields, CUDA events on `stream`) and keeps the fastest; results are cached
+ * descent over the fields, CUDA events on `stream`) and keeps the fastest; results are cached
  * process-wide per (device, n, real/complex, precision, nb, vectors) so that contexts of the same
  * shape reuse them. It allocates and synchronises: call it before capturing work into a graph. */
 typedef struct uepm_tuning {
-    int32_t fp32_reduction;
-    int32_t fp64_ctas_per_sm;
+    int32_t reduction;
+    int32_t ctas_per_sm;
     int32_t vector_lanes;
     int32_t chunk;
+    int32_t cluster;
 } uepm_tuning;
 int uepm_ctx_get_tuning(const uepm_ctx* ctx, uepm_tuning* out);
 int uepm_ctx_set_tuning(uepm_ctx* ctx, const uepm_tuning* t);

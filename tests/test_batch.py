@@ -149,11 +149,13 @@ def test_batch_replay_reads_the_registered_buffers(gpu, oracle, mats):
 
 
 @pytest.mark.parametrize("prec,tuning", [
-    (N.UEPM_PREC_MIXED, dict(fp32_reduction=2)),
-    (N.UEPM_PREC_MIXED, dict(fp32_reduction=1, vector_lanes=16, chunk=256)),
+    (N.UEPM_PREC_MIXED, dict(reduction=2)),
+    (N.UEPM_PREC_MIXED, dict(reduction=1, vector_lanes=16, chunk=256)),
+    (N.UEPM_PREC_MIXED, dict(reduction=3, cluster=2)),
     (N.UEPM_PREC_MIXED, dict(vector_lanes=32, chunk=64)),
-    (N.UEPM_PREC_FP64, dict(fp64_ctas_per_sm=1, chunk=512)),
-    (N.UEPM_PREC_FP64, dict(fp64_ctas_per_sm=8, vector_lanes=16)),
+    (N.UEPM_PREC_FP64, dict(ctas_per_sm=1, chunk=512)),
+    (N.UEPM_PREC_FP64, dict(ctas_per_sm=8, vector_lanes=16)),
+    (N.UEPM_PREC_FP64, dict(reduction=3, cluster=4)),
 ])
 def test_every_tuning_choice_keeps_parity(gpu, oracle, mats, prec, tuning):
     G = oracle.generate_basis(10)
@@ -173,7 +175,7 @@ def test_every_tuning_choice_keeps_parity(gpu, oracle, mats, prec, tuning):
 
 def test_set_tuning_rejects_out_of_range_fields(gpu, oracle, mats):
     ctx = api._Context(_mat(mats["Si-CB"]), oracle.generate_basis(8), False, False)
-    for bad in (dict(fp32_reduction=3), dict(fp64_ctas_per_sm=9), dict(vector_lanes=12), dict(chunk=10)):
+    for bad in (dict(reduction=4), dict(ctas_per_sm=9), dict(vector_lanes=12), dict(chunk=10), dict(cluster=3)):
         assert gpu.uepm_ctx_set_tuning(ctx.h, C.byref(N.UepmTuning(**bad))) == N.UEPM_ERR_OUT_OF_RANGE
     ctx.close()
 
@@ -189,7 +191,7 @@ def test_autotune_picks_a_valid_shape_and_caches_it(gpu, oracle, mats):
     N.check(gpu.uepm_ctx_autotune(a.h, 16, N.UEPM_WANT_VALUES, 1024, sp))
     ta = N.UepmTuning()
     N.check(gpu.uepm_ctx_get_tuning(a.h, C.byref(ta)))
-    assert ta.fp32_reduction in (0, 1, 2) and ta.vector_lanes in (0, 8, 16, 32)
+    assert ta.reduction in (0, 1, 2, 3) and ta.vector_lanes in (0, 8, 16, 32) and ta.cluster in (0, 2, 4, 8, 16)
     assert ta.chunk == 0 or 64 <= ta.chunk <= 32768
     b = api._Context(_mat(mats["Si-CB"]), G, False, False, N.UEPM_PREC_MIXED)
     t0 = time.perf_counter()

@@ -51,8 +51,9 @@ TuneKey tune_key(const uepm_ctx* ctx, int nb, uint32_t want) {
 }
 
 bool valid_tuning(const uepm_ctx* ctx, const uepm_tuning& t) {
-    if (t.fp32_reduction < 0 || t.fp32_reduction > 2) return false;
-    if (t.fp64_ctas_per_sm < 0 || t.fp64_ctas_per_sm > 8) return false;
+    if (t.reduction < 0 || t.reduction > 3) return false;
+    if (t.ctas_per_sm < 0 || t.ctas_per_sm > 8) return false;
+    if (t.cluster != 0 && t.cluster != 2 && t.cluster != 4 && t.cluster != 8 && t.cluster != 16) return false;
     if (t.vector_lanes != 0 && t.vector_lanes != 8 && t.vector_lanes != 16 && t.vector_lanes != 32) return false;
     if (t.chunk != 0 && (t.chunk < 64 || t.chunk > 32768)) return false;
     (void)ctx;
@@ -171,28 +172,38 @@ int uepm_ctx_autotune(uepm_ctx* ctx, int nb, uint32_t want, size_t sample_k, voi
         return UEPM_OK;
     };
 
-    uepm_tuning best = uepm_tuning{0, 0, 0, 0};
+    uepm_tuning best = uepm_tuning{0, 0, 0, 0, 0};
     ctx->tune        = best;
     double best_ms   = 0;
     rc               = timed(&best_ms);
     // candidates per field, tried one field at a time from the current best
-    const bool     mixed = ctx->precision == UEPM_PREC_MIXED;
-    const int      tmax  = ctx->real ? 32 : 24;
-    std::vector<int> chunks, ctas, reds, lanes;
+    const bool mixed = ctx->precision == UEPM_PREC_MIXED;
+    const int  tmax  = ctx->real ? 32 : 24;
+    const bool regok = mixed && ctx->real && ctx->n <= tridiag_reg_max_n();
+    const int  es    = mixed ? (ctx->real ? 4 : 8) : (ctx->real ? 8 : 16);  // bytes of a reduced element
+    std::vector<int> chunks, reds, ctas, lanes, clusters;
     for (int c : {256, 512, 1024, 2048, 4096, 8192})
         if ((size_t)c < sample_k) chunks.push_back(c);
-    if (!mixed || !(ctx->real && ctx->n <= tridiag_reg_max_n())) ctas = {1, 2, 3, 4, 6, 8};
-    if (mixed && ctx->real && ctx->n <= tridiag_reg_max_n()) reds = {2};
+    reds = regok ? std::vector<int>{2, 3} : std::vector<int>{2, 3};
+    ctas = {1, 2, 4, 6, 8};
+    for (int c : {2, 4, 8, 16})
+        if ((size_t)es * ctx->n * ((ctx->n + c - 1) / c) <= (200u << 10)) clusters.push_back(c);
     if (mixed || wv || wg)
         for (int l : {8, 16, 32})
             if ((ctx->n + l - 1) / l <= tmax) lanes.push_back(l);
-    for (int field = 0; field < 4 && !rc; ++field) {
-        const std::vector<int>& cand = field == 0 ? chunks : field == 1 ? ctas : field == 2 ? reds : lanes;
+    auto field_of = [](uepm_tuning& t, int f) -> int32_t& {
+        return f == 0 ? t.chunk : f == 1 ? t.reduction : f == 2 ? t.ctas_per_sm : f == 3 ? t.cluster : t.vector_lanes;
+    };
+    for (int field = 0; field < 5 && !rc; ++field) {
+        std::vector<int> cand = field == 0 ? chunks : field == 1 ? reds : field == 2 ? ctas : field == 3 ? clusters : lanes;
+        // ctas_per_sm matters only for the global-memory kernel, cluster only for the cluster kernel
+        if (field == 2 && best.reduction == 3) continue;
+        if (field == 3 && best.reduction != 3 && !(best.reduction == 0 && !ctx->real)) continue;
         for (int v : cand) {
-            uepm_tuning t = best;
-            (field == 0 ? t.chunk : field == 1 ? t.fp64_ctas_per_sm : field == 2 ? t.fp32_reduction : t.vector_lanes) = v;
-            ctx->tune = t;
-            double ms = 0;
+            uepm_tuning t    = best;
+            field_of(t, field) = v;
+            ctx->tune        = t;
+            double ms        = 0;
             if ((rc = timed(&ms))) break;
             if (ms < best_ms * 0.99) {  // keep a change only for a clear gain
                 best_ms = ms;

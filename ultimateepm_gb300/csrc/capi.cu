@@ -233,7 +233,8 @@ void run_chunk(uepm_ctx* ctx, const Layout& L, char* ws, const double* kk, int c
         auto* tq = reinterpret_cast<S*>(ws + L.tq);
         {
             ProfScope p(ctx, s, KK_TRIDIAG64);
-            launch_tridiag<S>(H, n, n, mstride, d, e, tq, st, c, s, 0, ctx->tune.fp64_ctas_per_sm);
+            launch_tridiag<S>(H, n, n, mstride, d, e, tq, st, c, s, ctx->tune.reduction, ctx->tune.ctas_per_sm,
+                              ctx->tune.cluster);
         }
         {
             ProfScope p(ctx, s, KK_BISECT);
@@ -270,7 +271,8 @@ void run_chunk(uepm_ctx* ctx, const Layout& L, char* ws, const double* kk, int c
     auto* small = reinterpret_cast<S*>(ws + L.small);
     {
         ProfScope p(ctx, s, KK_TRIDIAG32);
-        launch_tridiag<S32>(H32, n, n, mstride, d, e, tq, st, c, s, ctx->tune.fp32_reduction, ctx->tune.fp64_ctas_per_sm);
+        launch_tridiag<S32>(H32, n, n, mstride, d, e, tq, st, c, s, ctx->tune.reduction, ctx->tune.ctas_per_sm,
+                                ctx->tune.cluster);
     }
     {
         ProfScope p(ctx, s, KK_BISECT);

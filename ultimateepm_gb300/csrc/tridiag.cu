@@ -258,13 +258,21 @@ static void tridiag_pick(S* H, int n, int ld, size_t mstride, typename ST<S>::R*
 
 template <typename S>
 void launch_tridiag(S* H, int n, int ld, size_t mstride, typename ST<S>::R* d, typename ST<S>::R* e, S* tq, int* status,
-                    int batch, cudaStream_t s, int variant, int ctas_per_sm) {
+                    int batch, cudaStream_t s, int variant, int ctas_per_sm, int cluster) {
     if constexpr (std::is_same<S, float>::value) {
-        if (variant != 2 && n <= tridiag_reg_max_n()) {
+        if ((variant == 0 || variant == 1) && n <= tridiag_reg_max_n()) {
             launch_tridiag_reg(H, n, ld, mstride, d, e, tq, status, batch, s);
             return;
         }
     }
+    // automatic cluster reduction where it measured faster than the global-memory kernel: complex
+    // FP32 matrices just beyond one SM (orders 178..274: 1.15-1.25x); for larger orders and for FP64
+    // the global-memory kernel's 32 warps per SM hide more latency than the cluster's barriers allow
+    constexpr bool CX = !std::is_same<S, typename ST<S>::R>::value;
+    constexpr bool F32 = sizeof(typename ST<S>::R) == 4;
+    const bool auto_cluster = variant == 0 && CX && F32 && !use_smem<S>(n) && n <= 300;
+    if ((variant == 3 || auto_cluster) && launch_tridiag_cluster<S>(H, n, ld, mstride, d, e, tq, status, batch, s, cluster))
+        return;
     // rows of the trailing matrix are at most n - 1 <= 32 * MAXT
     if (n <= 129) tridiag_pick<S, 4>(H, n, ld, mstride, d, e, tq, status, batch, s, ctas_per_sm);
     else if (n <= 161) tridiag_pick<S, 5>(H, n, ld, mstride, d, e, tq, status, batch, s, ctas_per_sm);
@@ -273,9 +281,9 @@ void launch_tridiag(S* H, int n, int ld, size_t mstride, typename ST<S>::R* d, t
     else tridiag_pick<S, 16>(H, n, ld, mstride, d, e, tq, status, batch, s, ctas_per_sm);
 }
 
-template void launch_tridiag<cx<double>>(cx<double>*, int, int, size_t, double*, double*, cx<double>*, int*, int, cudaStream_t, int, int);
-template void launch_tridiag<cx<float>>(cx<float>*, int, int, size_t, float*, float*, cx<float>*, int*, int, cudaStream_t, int, int);
-template void launch_tridiag<double>(double*, int, int, size_t, double*, double*, double*, int*, int, cudaStream_t, int, int);
-template void launch_tridiag<float>(float*, int, int, size_t, float*, float*, float*, int*, int, cudaStream_t, int, int);
+template void launch_tridiag<cx<double>>(cx<double>*, int, int, size_t, double*, double*, cx<double>*, int*, int, cudaStream_t, int, int, int);
+template void launch_tridiag<cx<float>>(cx<float>*, int, int, size_t, float*, float*, cx<float>*, int*, int, cudaStream_t, int, int, int);
+template void launch_tridiag<double>(double*, int, int, size_t, double*, double*, double*, int*, int, cudaStream_t, int, int, int);
+template void launch_tridiag<float>(float*, int, int, size_t, float*, float*, float*, int*, int, cudaStream_t, int, int, int);
 
 }  // namespace uepm

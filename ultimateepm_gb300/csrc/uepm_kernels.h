@@ -21,12 +21,21 @@ void launch_assemble(const DevParams& P, const cx<double>* Vloc, const double2* 
 
 // tridiag.cu: Householder reduction in place. d, e: [batch][n]; tq: [batch][n] reflector scalars;
 // status: [batch] (ORed with UEPM_K_NONFINITE on NaN/Inf).
-// variant: 0 automatic (register-resident FP32 kernel where it fits), 1 register-resident where it
-// fits, 2 shared/global-memory kernel; ctas_per_sm (0: automatic) caps the persistent grid of the
-// global-memory kernel.
+// variant: 0 automatic, 1 register-resident (FP32 real, n <= tridiag_reg_max_n()), 2 one CTA per
+// matrix (shared memory where the matrix fits, else global memory with a persistent grid), 3 one
+// thread-block cluster per matrix (tridiag_cluster.cu). Automatic: 1 where it applies, 3 for complex
+// FP32 matrices just beyond one SM's shared memory (n <= 300), else 2. ctas_per_sm (0: automatic) caps the persistent grid
+// of the global-memory kernel; cluster (0: automatic) is the cluster size of variant 3.
 template <typename S>
 void launch_tridiag(S* H, int n, int ld, size_t mstride, typename ST<S>::R* d, typename ST<S>::R* e, S* tq, int* status,
-                    int batch, cudaStream_t s, int variant = 0, int ctas_per_sm = 0);
+                    int batch, cudaStream_t s, int variant = 0, int ctas_per_sm = 0, int cluster = 0);
+// tridiag_cluster.cu: cluster size for order n (want = 0: automatic; 0 returned when it cannot fit)
+// and the launch (false when the cluster kernel cannot run this case).
+template <typename S>
+int tridiag_cluster_size(int n, int want);
+template <typename S>
+bool launch_tridiag_cluster(S* H, int n, int ld, size_t mstride, typename ST<S>::R* d, typename ST<S>::R* e, S* tq,
+                            int* status, int batch, cudaStream_t s, int want_c);
 // tridiag_reg.cu: the same reduction for real FP32 matrices with n <= tridiag_reg_max_n(), held in
 // registers (launch_tridiag<float> dispatches to it).
 int  tridiag_reg_max_n();
