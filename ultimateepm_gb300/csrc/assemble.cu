@@ -14,11 +14,16 @@
 //   k_rows      one thread per (k, G_i): k+G, K = (k+G) 2pi/a, |K|, the kinetic term and all
 //               quantities that depend on a single plane wave (spherical Bessel values at |K| R,
 //               gaussian-well exponentials, spin-orbit radial factors B(|K|)).
-//   k_assemble  one thread per lower-triangle element (i >= j) of the scalar N x N problem; writes
-//               the element and its Hermitian mirror into the FULL n x n column-major H (n = 2N
-//               with SOC: [[UU, UD], [DU, DD]]), optionally also an FP32 copy for the mixed path.
-//               When H(k) is exactly real (no SOC, no antisymmetric form factors, identical
-//               anion/cation nonlocal parameters) only the real parts are stored.
+//   k_assemble_tiles (no spin-orbit) one CTA per 32 x 32 tile of the lower triangle of the N x N
+//               matrix: the tile and, through a shared-memory transpose, its Hermitian mirror are
+//               written with coalesced stores into the FULL column-major H;
+//   k_assemble  (spin-orbit) one thread per lower-triangle element (i >= j) of the scalar N x N
+//               problem, writing the four spin blocks [[UU, UD], [DU, DD]] of the 2N x 2N matrix
+//               and their mirrors.
+//   Both optionally write an FP32 copy for the mixed path, and store H itself as FP64 or as FP32
+//   (hi, lo) pairs (the mixed path's Rayleigh-Ritz operand). When H(k) is exactly real (no SOC, no
+//   antisymmetric form factors, identical anion/cation nonlocal parameters) only real parts are
+//   stored.
 #include "uepm_common.cuh"
 #include "uepm_kernels.h"
 
@@ -246,6 +251,93 @@ __device__ __forceinline__ void put_pair(SO* Hb, SF* Fb, int ld, int r, int c, c
     }
 }
 
+// Element (i, j), i >= j, of the scalar N x N problem: local form factor, kinetic diagonal and the
+// nonlocal correction, in the reference's order of operations.
+template <bool NL>
+__device__ __forceinline__ cx<double> scalar_element(const DevParams& P, const cx<double>* __restrict__ Vloc,
+                                                     const double2* __restrict__ phNL, const double* __restrict__ rows,
+                                                     int b, int i, int j) {
+    const int     N  = P.N;
+    const double* Ri = rows + ((size_t)b * N + i) * ROW_STRIDE;
+    const double* Rj = rows + ((size_t)b * N + j) * ROW_STRIDE;
+    cx<double>    h  = Vloc[(size_t)j * N + i];
+    if (i == j) h.x = h.x + Ri[RF_KIN];
+    if (NL) {
+        const double2    ph = phNL[(size_t)j * N + i];
+        const cx<double> v  = nl_element(P, Ri, Rj, ph.x, ph.y);
+        h.x                 = h.x + v.x;
+        h.y                 = h.y + v.y;
+    }
+    return h;
+}
+
+// The stored form of an element (FP64, or the FP32 pair whose hi part is also the FP32 copy), its
+// Hermitian conjugate, and the FP32 copy: each element is converted once and its mirror and copy are
+// written from that form (conversions between FP64 and FP32 run at the FP64 rate).
+__device__ __forceinline__ double stored(double*, cx<double> h) { return h.x; }
+__device__ __forceinline__ cx<double> stored(cx<double>*, cx<double> h) { return h; }
+__device__ __forceinline__ ds2 stored(ds2*, cx<double> h) { return split_fp32(h.x); }
+__device__ __forceinline__ ds4 stored(ds4*, cx<double> h) {
+    const ds2 r = split_fp32(h.x), i = split_fp32(h.y);
+    return ds4{r.hi, r.lo, i.hi, i.lo};
+}
+__device__ __forceinline__ double conj_stored(double v) { return v; }
+__device__ __forceinline__ cx<double> conj_stored(cx<double> v) { return conjd(v); }
+__device__ __forceinline__ ds2 conj_stored(ds2 v) { return v; }
+__device__ __forceinline__ ds4 conj_stored(ds4 v) { return ds4{v.rhi, v.rlo, -v.ihi, -v.ilo}; }
+__device__ __forceinline__ float copy32(ds2 v) { return v.hi; }
+__device__ __forceinline__ cx<float> copy32(ds4 v) { return mk(v.rhi, v.ihi); }
+__device__ __forceinline__ float copy32(double v) { return (float)v; }
+__device__ __forceinline__ cx<float> copy32(cx<double> v) { return mk((float)v.x, (float)v.y); }
+
+// Without spin-orbit coupling: one CTA per 32 x 32 tile of the lower triangle, 32 x 8 threads, four
+// elements per thread. The tile is written directly (coalesced down its columns) and, through a
+// shared-memory transpose, as its Hermitian mirror (coalesced down the mirror's columns), so no
+// store is strided and no thread idles on the upper triangle.
+template <bool NL, typename SO>
+__global__ void __launch_bounds__(256) k_assemble_tiles(const DevParams P, const cx<double>* __restrict__ Vloc,
+                                                        const double2* __restrict__ phNL, const double* __restrict__ rows,
+                                                        SO* __restrict__ H, int ld, size_t mstride,
+                                                        typename Lower<SO>::type* __restrict__ H32, size_t mstride32,
+                                                        int batch) {
+    using SF = typename Lower<SO>::type;
+    __shared__ SO tile[32][33];  // tile[jl][il] = stored form of h(i, j)
+    const int b = blockIdx.y;
+    if (b >= batch) return;
+    // lower tile index -> (ti, tj), ti >= tj, row-major over the lower triangle of tiles
+    int t = blockIdx.x, ti = 0;
+    while (t > ti) {
+        t -= ti + 1;
+        ++ti;
+    }
+    const int tj = t;
+    const int N  = P.N;
+    const int tx = threadIdx.x, ty = threadIdx.y;
+    SO*       Hb = H + (size_t)b * mstride;
+    SF*       Fb = H32 ? H32 + (size_t)b * mstride32 : nullptr;
+#pragma unroll
+    for (int s = 0; s < 4; ++s) {
+        const int jl = ty + 8 * s, i = ti * 32 + tx, j = tj * 32 + jl;
+        if (i < N && j < N && i >= j) {
+            const SO v   = stored(Hb, scalar_element<NL>(P, Vloc, phNL, rows, b, i, j));
+            tile[jl][tx] = v;
+            Hb[(size_t)j * ld + i] = v;
+            if (Fb) Fb[(size_t)j * ld + i] = copy32(v);
+        }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int s = 0; s < 4; ++s) {
+        // mirror (row j, column i) = conj h(i, j) for i > j: threads run down the rows j
+        const int il = ty + 8 * s, j = tj * 32 + tx, i = ti * 32 + il;
+        if (i < N && j < N && i > j) {
+            const SO v = conj_stored(tile[tx][il]);
+            Hb[(size_t)i * ld + j] = v;
+            if (Fb) Fb[(size_t)i * ld + j] = copy32(v);
+        }
+    }
+}
+
 template <bool NL, bool SOC, typename SO>
 __global__ void k_assemble(const DevParams P, const cx<double>* __restrict__ Vloc, const double2* __restrict__ phNL,
                            const double2* __restrict__ phSO, const double* __restrict__ rows, SO* __restrict__ H, int ld,
@@ -258,14 +350,7 @@ __global__ void k_assemble(const DevParams P, const cx<double>* __restrict__ Vlo
     if (i >= N || j >= N || i < j || b >= batch) return;
     const double* Ri = rows + ((size_t)b * N + i) * ROW_STRIDE;
     const double* Rj = rows + ((size_t)b * N + j) * ROW_STRIDE;
-    cx<double>    h  = Vloc[(size_t)j * N + i];
-    if (i == j) h.x = h.x + Ri[RF_KIN];
-    if (NL) {
-        const double2    ph = phNL[(size_t)j * N + i];
-        const cx<double> v  = nl_element(P, Ri, Rj, ph.x, ph.y);
-        h.x                 = h.x + v.x;
-        h.y                 = h.y + v.y;
-    }
+    const cx<double> h = scalar_element<NL>(P, Vloc, phNL, rows, b, i, j);
     SO* Hb = H + (size_t)b * mstride;
     SF* Fb = H32 ? H32 + (size_t)b * mstride32 : nullptr;
     if (!SOC) {
@@ -293,12 +378,19 @@ template <typename SO>
 void launch_assemble(const DevParams& P, const cx<double>* Vloc, const double2* phNL, const double2* phSO, const double* rows,
                      SO* H, int ld, size_t mstride, typename Lower<SO>::type* H32, size_t mstride32, int batch,
                      cudaStream_t s) {
-    dim3 blk(32, 8), grd((P.N + 31) / 32, (P.N + 7) / 8, batch);
+    dim3 blk(32, 8);
+    if (!P.soc) {
+        const int T = (P.N + 31) / 32;
+        dim3      grd(T * (T + 1) / 2, batch);
+        if (P.nl) k_assemble_tiles<true, SO><<<grd, blk, 0, s>>>(P, Vloc, phNL, rows, H, ld, mstride, H32, mstride32, batch);
+        else k_assemble_tiles<false, SO><<<grd, blk, 0, s>>>(P, Vloc, phNL, rows, H, ld, mstride, H32, mstride32, batch);
+        count_launch();
+        return;
+    }
+    dim3 grd((P.N + 31) / 32, (P.N + 7) / 8, batch);
 #define UEPM_ASM(NL_, SO_) k_assemble<NL_, SO_, SO><<<grd, blk, 0, s>>>(P, Vloc, phNL, phSO, rows, H, ld, mstride, H32, mstride32, batch)
-    if (P.nl && P.soc) UEPM_ASM(true, true);
-    else if (P.nl) UEPM_ASM(true, false);
-    else if (P.soc) UEPM_ASM(false, true);
-    else UEPM_ASM(false, false);
+    if (P.nl) UEPM_ASM(true, true);
+    else UEPM_ASM(false, true);
 #undef UEPM_ASM
     count_launch();
 }
