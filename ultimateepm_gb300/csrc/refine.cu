@@ -145,14 +145,23 @@ __global__ void __launch_bounds__(kProjNT) k_refine_project(const typename Split
 // instructions are issued with most lanes busy.
 constexpr int kSmallWarps = 2;
 
-// shared memory of one warp's matrix: L, C, V (m x (m+1) scalars each), 4 rotation arrays and the
-// round's pair table
+// shared memory of one warp's matrix: L, C, V (m x (m+1) scalars each), 4 rotation arrays, the
+// round's pair table, then FP32 copies of E = S - I and A for the Loewdin correction
 template <typename S>
-__host__ __device__ inline size_t small_eigh_warp_bytes(int m) {
+__host__ __device__ inline size_t small_eigh_lowdin_offset(int m) {
     const int me = (m + 1) & ~1;
     return (sizeof(S) * 3 * (size_t)m * (m + 1) + sizeof(double) * 4 * (size_t)me + sizeof(int) * (size_t)me + 15) &
            ~(size_t)15;
 }
+template <typename S>
+__host__ __device__ inline size_t small_eigh_warp_bytes(int m) {
+    return (small_eigh_lowdin_offset<S>(m) + sizeof(typename Lower<S>::type) * 2 * (size_t)m * m + 15) & ~(size_t)15;
+}
+
+__device__ __forceinline__ float to_lower(double v) { return (float)v; }
+__device__ __forceinline__ cx<float> to_lower(cx<double> v) { return mk((float)v.x, (float)v.y); }
+__device__ __forceinline__ double from_lower(float v) { return (double)v; }
+__device__ __forceinline__ cx<double> from_lower(cx<float> v) { return mk((double)v.x, (double)v.y); }
 
 template <typename S>
 __global__ void __launch_bounds__(32 * kSmallWarps) k_small_eigh(S* __restrict__ small, int m, int nb, double* __restrict__ Eout,
@@ -196,16 +205,26 @@ __global__ void __launch_bounds__(32 * kSmallWarps) k_small_eigh(S* __restrict__
     emax             = warp_max(emax);
     const bool lowdin = emax <= 1e-4;
     if (lowdin) {
+        // the correction (E A + A E) / 2 is ~|E| |A| ~ 1e-4 eV and needs ~1e-5 relative accuracy:
+        // FP32 products (on copies converted once), subtracted from A in FP64
+        using F = typename Lower<S>::type;
+        F* Ef   = reinterpret_cast<F*>(smraw + (size_t)warp * small_eigh_warp_bytes<S>(m) + small_eigh_lowdin_offset<S>(m));
+        F* Af   = Ef + (size_t)m * m;
         for (int q = lane; q < m * m; q += 32) {
             const int i = q / m, c = q - i * m;
-            S         acc = ST<S>::zero();
+            const S   e = (i == c) ? ST<S>::make(ST<S>::re(LL(i, c)) - 1.0, ST<S>::im(LL(i, c))) : LL(i, c);
+            Ef[q]       = to_lower(e);
+            Af[q]       = to_lower(VV(i, c));
+        }
+        __syncwarp();
+        for (int q = lane; q < m * m; q += 32) {
+            const int i = q / m, c = q - i * m;
+            F         acc = ST<F>::zero();
             for (int j = 0; j < m; ++j) {
-                const S eij = (i == j) ? ST<S>::make(ST<S>::re(LL(i, j)) - 1.0, ST<S>::im(LL(i, j))) : LL(i, j);
-                const S ejc = (j == c) ? ST<S>::make(ST<S>::re(LL(j, c)) - 1.0, ST<S>::im(LL(j, c))) : LL(j, c);
-                acc         = cfma(eij, VV(j, c), acc);
-                acc         = cfma(VV(i, j), ejc, acc);
+                acc = cfma(Ef[i * m + j], Af[j * m + c], acc);
+                acc = cfma(Af[i * m + j], Ef[j * m + c], acc);
             }
-            CC(i, c) = cfma(acc, ST<S>::make(-0.5, 0.0), VV(i, c));
+            CC(i, c) = cfma(from_lower(acc), ST<S>::make(-0.5, 0.0), VV(i, c));
         }
         __syncwarp();
         for (int q = lane; q < m * m; q += 32) {
@@ -345,9 +364,11 @@ __global__ void __launch_bounds__(32 * kSmallWarps) k_small_eigh(S* __restrict__
                 const S   cp = CC(r, p), cq = CC(r, q);
                 CC(r, p) = cfma(cq, jqp, cscale(cp, c));
                 CC(r, q) = cfma(cq, jqq, cscale(cp, s));
-                const S vp = VV(r, p), vq = VV(r, q);
-                VV(r, p) = cfma(vq, jqp, cscale(vp, c));
-                VV(r, q) = cfma(vq, jqq, cscale(vp, s));
+                if (want_w) {  // the accumulated rotations only matter for the Ritz vectors
+                    const S vp = VV(r, p), vq = VV(r, q);
+                    VV(r, p) = cfma(vq, jqp, cscale(vp, c));
+                    VV(r, q) = cfma(vq, jqq, cscale(vp, s));
+                }
             }
             __syncwarp();
             // rows: C <- J^H C
