@@ -281,6 +281,12 @@ __device__ __forceinline__ ds4 stored(ds4*, cx<double> h) {
     const ds2 r = split_fp32(h.x), i = split_fp32(h.y);
     return ds4{r.hi, r.lo, i.hi, i.lo};
 }
+__device__ __forceinline__ float stored(float*, cx<double> h) { return (float)h.x; }
+__device__ __forceinline__ cx<float> stored(cx<float>*, cx<double> h) { return mk((float)h.x, (float)h.y); }
+__device__ __forceinline__ float conj_stored(float v) { return v; }
+__device__ __forceinline__ cx<float> conj_stored(cx<float> v) { return mk(v.x, -v.y); }
+__device__ __forceinline__ float copy32(float v) { return v; }
+__device__ __forceinline__ cx<float> copy32(cx<float> v) { return v; }
 __device__ __forceinline__ double conj_stored(double v) { return v; }
 __device__ __forceinline__ cx<double> conj_stored(cx<double> v) { return conjd(v); }
 __device__ __forceinline__ ds2 conj_stored(ds2 v) { return v; }
@@ -399,6 +405,10 @@ template void launch_assemble<double>(const DevParams&, const cx<double>*, const
                                       double*, int, size_t, float*, size_t, int, cudaStream_t);
 template void launch_assemble<cx<double>>(const DevParams&, const cx<double>*, const double2*, const double2*, const double*,
                                           cx<double>*, int, size_t, cx<float>*, size_t, int, cudaStream_t);
+template void launch_assemble<float>(const DevParams&, const cx<double>*, const double2*, const double2*, const double*,
+                                     float*, int, size_t, float*, size_t, int, cudaStream_t);
+template void launch_assemble<cx<float>>(const DevParams&, const cx<double>*, const double2*, const double2*, const double*,
+                                         cx<float>*, int, size_t, cx<float>*, size_t, int, cudaStream_t);
 template void launch_assemble<ds2>(const DevParams&, const cx<double>*, const double2*, const double2*, const double*, ds2*,
                                    int, size_t, float*, size_t, int, cudaStream_t);
 template void launch_assemble<ds4>(const DevParams&, const cx<double>*, const double2*, const double2*, const double*, ds4*,

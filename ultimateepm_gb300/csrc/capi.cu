@@ -166,7 +166,7 @@ Layout plan(const uepm_ctx* ctx, int nb, uint32_t want, size_t c) {
         return o;
     };
     L.rows = take(c * N * ROW_STRIDE * sizeof(double));
-    L.H    = take(c * n * n * es);
+    L.H    = take(mixed && ctx->sparse_local ? 0 : c * n * n * es);  // the sparse path never forms it
     L.H32  = mixed ? take(c * n * n * es32) : 0;
     L.d    = take(c * n * rs);
     L.e    = take(c * n * rs);
@@ -257,8 +257,12 @@ void run_chunk(uepm_ctx* ctx, const Layout& L, char* ws, const double* kk, int c
     auto* Hs  = reinterpret_cast<SP*>(ws + L.H);
     {
         ProfScope p(ctx, s, KK_ASSEMBLE);
-        // the FP64 matrix is kept only for the Rayleigh-Ritz products: stored as FP32 pairs in place
-        launch_assemble<SP>(ctx->P, ctx->d_Vloc, ctx->d_phNL, ctx->d_phSO, rows, Hs, n, mstride, H32, mstride, c, s);
+        // the FP64 matrix is kept only for the Rayleigh-Ritz products: stored as FP32 pairs in place;
+        // with a local potential only, those products use the resident sparse V instead
+        if (ctx->sparse_local)
+            launch_assemble<S32>(ctx->P, ctx->d_Vloc, ctx->d_phNL, ctx->d_phSO, rows, H32, n, mstride, nullptr, 0, c, s);
+        else
+            launch_assemble<SP>(ctx->P, ctx->d_Vloc, ctx->d_phNL, ctx->d_phSO, rows, Hs, n, mstride, H32, mstride, c, s);
     }
     auto* d     = reinterpret_cast<float*>(ws + L.d);
     auto* e     = reinterpret_cast<float*>(ws + L.e);
@@ -289,7 +293,8 @@ void run_chunk(uepm_ctx* ctx, const Layout& L, char* ws, const double* kk, int c
     }
     {
         ProfScope p(ctx, s, KK_REFINE_PROJECT);
-        launch_refine_project<S>(Hs, n, n, mstride, X32, m, rw, small, c, s);
+        const SparseV sv{ctx->sparse_local, ctx->d_csr_ptr, ctx->d_csr_col, ctx->d_csr_val, ctx->d_Vloc, rows, ctx->N};
+        launch_refine_project<S>(Hs, n, n, mstride, X32, m, rw, small, c, s, sv);
     }
     S* W = small + (size_t)2 * m * m;  // W block of the first matrix; matrices are refine_small_elems apart
     {
@@ -502,6 +507,36 @@ int uepm_ctx_create(const uepm_material* mat, const int32_t* G, int N, uint32_t 
         if ((e = cudaMemcpy(ctx->d_phSO, phSO.data(), sizeof(double2) * phSO.size(), cudaMemcpyHostToDevice)) != cudaSuccess)
             return fail(e, "copy phSO");
     }
+    if (!nl && !soc) {
+        // CSR of V by rows, columns ascending, the diagonal always listed (its value gets the kinetic
+        // term per k on the device); values split into FP32 pairs (round to nearest, as on the device)
+        std::vector<int> ptr(N + 1, 0), col;
+        std::vector<ds4> val;
+        auto             split = [](double v, float* hi, float* lo) {
+            *hi = (float)v;
+            *lo = (float)(v - (double)*hi);
+        };
+        for (int i = 0; i < N; ++i) {
+            for (int j = 0; j < N; ++j) {
+                const double2 v = V[(size_t)j * N + i];
+                if (j != i && v.x == 0.0 && v.y == 0.0) continue;
+                ds4 d;
+                split(v.x, &d.rhi, &d.rlo);
+                split(v.y, &d.ihi, &d.ilo);
+                col.push_back(j);
+                val.push_back(d);
+            }
+            ptr[i + 1] = (int)col.size();
+        }
+        if ((e = cudaMalloc(&ctx->d_csr_ptr, sizeof(int) * ptr.size())) != cudaSuccess) return fail(e, "cudaMalloc(csr)");
+        if ((e = cudaMalloc(&ctx->d_csr_col, sizeof(int) * col.size())) != cudaSuccess) return fail(e, "cudaMalloc(csr)");
+        if ((e = cudaMalloc(&ctx->d_csr_val, sizeof(ds4) * val.size())) != cudaSuccess) return fail(e, "cudaMalloc(csr)");
+        if ((e = cudaMemcpy(ctx->d_csr_ptr, ptr.data(), sizeof(int) * ptr.size(), cudaMemcpyHostToDevice)) != cudaSuccess ||
+            (e = cudaMemcpy(ctx->d_csr_col, col.data(), sizeof(int) * col.size(), cudaMemcpyHostToDevice)) != cudaSuccess ||
+            (e = cudaMemcpy(ctx->d_csr_val, val.data(), sizeof(ds4) * val.size(), cudaMemcpyHostToDevice)) != cudaSuccess)
+            return fail(e, "copy csr");
+        ctx->sparse_local = true;
+    }
     *out = ctx;
     return UEPM_OK;
 }
@@ -512,6 +547,9 @@ int uepm_ctx_destroy(uepm_ctx* ctx) {
     if (ctx->d_Vloc) cudaFree(ctx->d_Vloc);
     if (ctx->d_phNL) cudaFree(ctx->d_phNL);
     if (ctx->d_phSO) cudaFree(ctx->d_phSO);
+    if (ctx->d_csr_ptr) cudaFree(ctx->d_csr_ptr);
+    if (ctx->d_csr_col) cudaFree(ctx->d_csr_col);
+    if (ctx->d_csr_val) cudaFree(ctx->d_csr_val);
     if (ctx->d_ws) cudaFree(ctx->d_ws);
     if (ctx->d_io) cudaFree(ctx->d_io);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);

@@ -26,6 +26,13 @@ struct uepm_ctx {
     uepm::cx<double>* d_Vloc    = nullptr;
     double2*      d_phNL    = nullptr;
     double2*      d_phSO    = nullptr;
+    // local potential only (no nonlocal, no spin-orbit): H(k) = V + diag(kinetic(k)) with V the
+    // k-independent local form-factor matrix, sparse (|G_i - G_j|^2 in {3, 4, 8, 11}); its rows as
+    // CSR (every row also lists its diagonal) with values as FP32 pairs, for the mixed path's H X
+    bool          sparse_local = false;
+    int*          d_csr_ptr = nullptr;
+    int*          d_csr_col = nullptr;
+    uepm::ds4*    d_csr_val = nullptr;
     void*         d_ws      = nullptr;
     size_t        ws_bytes  = 0;
     // buffers of the host-pointer entry point

@@ -49,10 +49,32 @@ __device__ __forceinline__ XElem<S> x_at(const XElem<S>* Xs, const cx<float>* Xg
     else return make_float2(v.x, v.y);
 }
 
-template <typename S, bool STAGED>
+// The stored pair of element (r, c) of a local-potential H: the CSR value, or on the diagonal
+// V_rr + kinetic in FP64 (the sum the assembly forms) split into FP32 pairs.
+__device__ __forceinline__ ds2 split_pair(double v) {
+    const float hi = __double2float_rn(v);
+    return ds2{hi, __double2float_rn(v - (double)hi)};
+}
+template <typename S>
+__device__ __forceinline__ typename Split<S>::type sparse_elem(const SparseV& sv, int b, int r, int e) {
+    const int c = sv.col[e];
+    if constexpr (std::is_same<S, double>::value) {
+        if (c != r) return ds2{sv.val[e].rhi, sv.val[e].rlo};
+        return split_pair(sv.Vloc[(size_t)r * sv.N + r].x + sv.rows[((size_t)b * sv.N + r) * ROW_STRIDE + RF_KIN]);
+    } else {
+        if (c != r) return sv.val[e];
+        const cx<double> v  = sv.Vloc[(size_t)r * sv.N + r];
+        const ds2        re = split_pair(v.x + sv.rows[((size_t)b * sv.N + r) * ROW_STRIDE + RF_KIN]);
+        const ds2        im = split_pair(v.y);
+        return ds4{re.hi, re.lo, im.hi, im.lo};
+    }
+}
+
+template <typename S, bool STAGED, bool SPARSE>
 __global__ void __launch_bounds__(kProjNT) k_refine_project(const typename Split<S>::type* __restrict__ H, int n, int ld,
                                                             size_t mstride, const cx<float>* __restrict__ X32, int m,
-                                                            void* __restrict__ work, S* __restrict__ small, int batch) {
+                                                            void* __restrict__ work, S* __restrict__ small, int batch,
+                                                            const SparseV sv) {
     constexpr bool CX = !std::is_same<S, double>::value;
     using SE          = typename Split<S>::type;
     using XT          = XElem<S>;
@@ -79,8 +101,10 @@ __global__ void __launch_bounds__(kProjNT) k_refine_project(const typename Split
         dsacc     yr[kProjVB], yi[kProjVB];
 #pragma unroll
         for (int q = 0; q < kProjVB; ++q) yr[q] = yi[q] = dsacc{0.f, 0.f};
-        for (int c = 0; c < n; ++c) {
-            const SE h = A[(size_t)c * ld + r];
+        const int e0 = SPARSE ? sv.ptr[r] : 0, e1 = SPARSE ? sv.ptr[r + 1] : n;
+        for (int e = e0; e < e1; ++e) {
+            const int c = SPARSE ? sv.col[e] : e;
+            const SE  h = SPARSE ? sparse_elem<S>(sv, b, r, e) : A[(size_t)c * ld + r];
 #pragma unroll
             for (int q = 0; q < kProjVB; ++q) {
                 const XT x = x_at<S, STAGED>(Xs, Xg, n, m, mp, c, j0 + q);
@@ -486,18 +510,25 @@ __global__ void k_refine_vectors(int n, int m, int nb, const cx<float>* __restri
     }
 }
 
-template <typename S>
-void launch_refine_project(const typename Split<S>::type* H, int n, int ld, size_t mstride, const cx<float>* X32, int m,
-                           S* work, S* small, int batch, cudaStream_t s) {
+template <typename S, bool SPARSE>
+static void refine_project_t(const typename Split<S>::type* H, int n, int ld, size_t mstride, const cx<float>* X32, int m,
+                             S* work, S* small, int batch, cudaStream_t s, const SparseV& sv) {
     const size_t stage = proj_stage_bytes<S>(n, m);
     if (stage <= kProjStageBytes) {
-        auto kern = k_refine_project<S, true>;
+        auto kern = k_refine_project<S, true, SPARSE>;
         if (stage > 48 * 1024) cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)stage);
-        kern<<<batch, kProjNT, stage, s>>>(H, n, ld, mstride, X32, m, work, small, batch);
+        kern<<<batch, kProjNT, stage, s>>>(H, n, ld, mstride, X32, m, work, small, batch, sv);
     } else {
-        k_refine_project<S, false><<<batch, kProjNT, 0, s>>>(H, n, ld, mstride, X32, m, work, small, batch);
+        k_refine_project<S, false, SPARSE><<<batch, kProjNT, 0, s>>>(H, n, ld, mstride, X32, m, work, small, batch, sv);
     }
     count_launch();
+}
+
+template <typename S>
+void launch_refine_project(const typename Split<S>::type* H, int n, int ld, size_t mstride, const cx<float>* X32, int m,
+                           S* work, S* small, int batch, cudaStream_t s, const SparseV& sv) {
+    if (sv.on) refine_project_t<S, true>(H, n, ld, mstride, X32, m, work, small, batch, s, sv);
+    else refine_project_t<S, false>(H, n, ld, mstride, X32, m, work, small, batch, s, sv);
 }
 
 template <typename S>
@@ -519,7 +550,7 @@ void launch_refine_vectors(int n, int m, int nb, const cx<float>* X32, const S* 
 
 #define UEPM_RF_INST(S)                                                                                             \
     template void launch_refine_project<S>(const typename Split<S>::type*, int, int, size_t, const cx<float>*, int, S*, S*, \
-                                           int, cudaStream_t);                                                    \
+                                           int, cudaStream_t, const SparseV&);                                    \
     template void launch_small_eigh<S>(S*, int, int, double*, S*, int*, int, cudaStream_t);                        \
     template void launch_refine_vectors<S>(int, int, int, const cx<float>*, const S*, cx<double>*, double*, const DevParams&, \
                                            const double*, const int*, int, cudaStream_t);

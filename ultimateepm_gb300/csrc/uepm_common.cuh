@@ -162,6 +162,14 @@ struct Split<cx<double>> {
     using type = ds4;
 };
 template <>
+struct Lower<float> {
+    using type = float;
+};
+template <>
+struct Lower<cx<float>> {
+    using type = cx<float>;
+};
+template <>
 struct Lower<ds2> {
     using type = float;
 };

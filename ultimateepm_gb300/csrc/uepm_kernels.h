@@ -69,10 +69,22 @@ __host__ __device__ inline size_t refine_work_elems(int n, int m) { return (size
 // small-solve scratch per matrix, contiguous: S (m x m), A (m x m), then the m x nb (<= m x m) Ritz
 // coefficients W at offset 2 m^2
 __host__ __device__ inline size_t refine_small_elems(int m, int) { return (size_t)3 * m * m; }
-// H is the FP32-pair copy the mixed-path assembly writes (Split<S>); work holds Y = H X.
+// H is the FP32-pair copy the mixed-path assembly writes (Split<S>); work holds Y = H X. With a
+// local potential only (sv.on), H is not formed: H X = V X + diag(kinetic) X from the resident CSR
+// of V (every row lists its diagonal, whose FP64 value V_ii + kinetic is split per k as the
+// assembly would), summed in the same column order, so Y is the same as from the dense pairs.
+struct SparseV {
+    bool              on;
+    const int*        ptr;
+    const int*        col;
+    const ds4*        val;
+    const cx<double>* Vloc;  // N x N column-major, for the diagonal
+    const double*     rows;  // [batch][N][ROW_STRIDE], for the kinetic term
+    int               N;
+};
 template <typename S>
 void launch_refine_project(const typename Split<S>::type* H, int n, int ld, size_t mstride, const cx<float>* X32, int m,
-                           S* work, S* small, int batch, cudaStream_t s);
+                           S* work, S* small, int batch, cudaStream_t s, const SparseV& sv);
 template <typename S>
 void launch_small_eigh(S* small, int m, int nb, double* Eout, S* W, int* status, int batch, cudaStream_t s);
 template <typename S>
