@@ -249,6 +249,9 @@ def run_ours(args):
         "backtransform": f * n * n * NB,
     }
     pipe_of = {"tridiag_fp32": "fp32", "backtransform": "fp32"}
+    # DRAM bytes (read + write) per launch of the reduction on this 2000-matrix workload, from one ncu
+    # capture of the same kernels (profiles/k_tridiag_si137_2000k.md)
+    traffic = {"tridiag_fp32": 192.9e6, "tridiag_fp64": 5.947e9}
     peak64 = C.c_double()
     peak32 = C.c_double()
     N.check(L.uepm_measure_peak(N.UEPM_PREC_FP64, C.byref(peak64)))
@@ -261,8 +264,9 @@ def run_ours(args):
         pipe = "fp64" if fp64_path else pipe_of.get(dom, "fp64")
         peak = peak64.value if pipe == "fp64" else peak32.value
         ach = flops_per_k[dom] * nk / (ms * 1e-3) / 1e12
+        tb = traffic.get(dom) if nk == NPOINTS else None
         return {"bound": f"{pipe}_pipe", "kernel": dom, "achieved": ach, "peak": peak, "unit": "TFLOP/s",
-                "frac": ach / peak, "traffic": None, "kernel_ms": ms,
+                "frac": ach / peak, "traffic": tb, "traffic_unit": "bytes per launch (ncu)", "kernel_ms": ms,
                 "peak_source": "measured in-run (pure-FMA kernel, uepm_measure_peak)"}
 
     roof_mixed = roof(prof_mixed, False)
