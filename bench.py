@@ -249,8 +249,8 @@ def run_ours(args):
         "backtransform": f * n * n * NB,
     }
     pipe_of = {"tridiag_fp32": "fp32", "backtransform": "fp32"}
-    # DRAM bytes (read + write) per launch of the reduction on this 2000-matrix workload, from one ncu
-    # capture of the same kernels (profiles/k_tridiag_si137_2000k.md)
+    # DRAM bytes per launch of the reduction on this 2000-matrix workload: dram__bytes_read.sum +
+    # dram__bytes_write.sum from one ncu capture of the same kernels (ncu cannot run inside a bench)
     traffic = {"tridiag_fp32": 192.9e6, "tridiag_fp64": 5.947e9}
     peak64 = C.c_double()
     peak32 = C.c_double()
