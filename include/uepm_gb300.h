@@ -225,6 +225,20 @@ int  uepm_batch_run(uepm_batch* b, void* stream);
 /* Kernels enqueued by one run of the batch (counted while capturing). */
 uint64_t uepm_batch_kernels_per_run(const uepm_batch* b);
 
+/* Irreducible wedge -> full Brillouin zone (MeshBZ::distribute_energies_from_iw_wedge_to_full_bz,
+ * src/BZ_MESH/bz_mesh.cpp:1383-1414), as a device gather after the solve of the wedge vertices:
+ * for each of n_full vertices v, E_full[v][:] = E_iw[src[v]][:] and, when gradients are given,
+ * grad_full[v][b][j] = s_j * grad_iw[src[v]][b][p_j], the signed permutation (p, s) that maps the
+ * wedge k-point onto vertex v (apply_same_symmetry_operation, bz_mesh.cpp:1312-1381), packed in
+ * op[v] as p_0 | p_1 << 2 | p_2 << 4 | (s_0 < 0) << 6 | (s_1 < 0) << 7 | (s_2 < 0) << 8.
+ * All pointers are device pointers; E is [.][nb], gradients [.][nb][3]; enqueued on `stream`. */
+int uepm_star_expand_device(const double* d_E_iw, const double* d_grad_iw, const int64_t* d_src, const uint16_t* d_op,
+                            size_t n_full, int nb, double* d_E_full, double* d_grad_full, void* stream);
+/* Host: the packed signed permutations op[q] mapping k_src[q] onto k_dst[q] (n pairs of reduced or
+ * SI k-points, the rule of apply_same_symmetry_operation); found[q] = 0 (optional) where none
+ * exists, with the identity written. */
+int uepm_star_operations(const double* k_src, const double* k_dst, size_t n, uint16_t* op, int32_t* found);
+
 /* ---- Serving (no reference counterpart; the reference's full-band Monte Carlo interpolates bands
  * on a mesh, src/FBMC/particle.cpp:52-63) -------------------------------------------------------
  * A query server over resident contexts (all on one device; not owned: keep them alive and unused

@@ -715,4 +715,55 @@ int or_generate_path(const char* labels, unsigned nrPoints, double* out, int cap
     return cnt;
 }
 
+// MeshBZ::is_irreducible_wedge (src/BZ_MESH/bz_mesh.cpp:1176-1183), on a reduced k-point.
+int or_is_irreducible_wedge(const double* kr) {
+    const double eps = 1e-12;
+    const double x = kr[0], y = kr[1], z = kr[2];
+    return (z >= -eps) && (z <= y + eps) && (y <= x + eps) && (x <= 1.0 + eps) && ((x + y + z) <= 1.5 + eps);
+}
+
+// apply_same_symmetry_operation (src/BZ_MESH/bz_mesh.cpp:1312-1381): the signed permutation that
+// maps k_iw onto k_bz, found component by component of k_bz (the first unused component of k_iw
+// whose magnitude matches within 1e-8 * max(1, largest magnitude)); perm[j] and sign[j] such that
+// v_bz[j] = sign[j] * v[perm[j]]. Returns 0 (and the identity) when no signed permutation matches,
+// where the reference returns v unchanged.
+int or_symmetry_operation(const double* a, const double* b, int* perm, int* sign) {
+    const double eps = 1e-8;
+    int          used[3] = {0, 0, 0};
+    double       scale = 0.0;
+    for (int q = 0; q < 3; ++q) {
+        scale = std::max(scale, std::fabs(a[q]));
+        scale = std::max(scale, std::fabs(b[q]));
+    }
+    if (scale < 1.0) scale = 1.0;
+    const double tol = eps * scale;
+    for (int jb = 0; jb < 3; ++jb) {
+        int found = 0;
+        for (int ia = 0; ia < 3; ++ia) {
+            if (used[ia]) continue;
+            if (std::fabs(std::fabs(a[ia]) - std::fabs(b[jb])) <= tol) {
+                perm[jb] = ia;
+                used[ia] = 1;
+                if (std::fabs(a[ia]) > tol) {
+                    const int sa = (a[ia] >= 0.0) ? 1 : -1;
+                    const int sb = (b[jb] >= 0.0) ? 1 : -1;
+                    sign[jb]     = sb * sa;
+                } else {
+                    sign[jb] = (b[jb] >= 0.0) ? 1 : -1;
+                }
+                found = 1;
+                break;
+            }
+        }
+        if (!found) {
+            for (int q = 0; q < 3; ++q) {
+                perm[q] = q;
+                sign[q] = 1;
+            }
+            return 0;
+        }
+    }
+    return 1;
+}
+
 }  // extern "C"

@@ -191,6 +191,10 @@ def lib():
         L.or_band_structure.argtypes = [mp, ip, C.c_int, dp, C.c_int64, C.c_int, C.c_int, C.c_int,
                                         C.c_int, C.c_int, dp, dp, dp, ip]
         L.or_band_structure.restype = C.c_int
+        L.or_is_irreducible_wedge.argtypes = [dp]
+        L.or_is_irreducible_wedge.restype = C.c_int
+        L.or_symmetry_operation.argtypes = [dp, dp, C.POINTER(C.c_int), C.POINTER(C.c_int)]
+        L.or_symmetry_operation.restype = C.c_int
         L.or_adjust_values.argtypes = [dp, C.c_int64, C.c_int, C.c_int, C.c_int, C.POINTER(C.c_int)]
         L.or_adjust_values.restype = C.c_double
         L.or_generate_path.argtypes = [C.c_char_p, C.c_uint, dp, C.c_int, C.POINTER(C.c_uint32)]
@@ -301,6 +305,23 @@ def adjust_values(E: np.ndarray, soc=False, min_cond_zero=False):
     found = C.c_int(0)
     gap = L.or_adjust_values(_dp(E), E.shape[0], E.shape[1], int(soc), int(min_cond_zero), C.byref(found))
     return gap, bool(found.value)
+
+
+def is_irreducible_wedge(k_reduced) -> bool:
+    """MeshBZ::is_irreducible_wedge on a reduced k-point."""
+    k = np.ascontiguousarray(k_reduced, dtype=np.float64)
+    return bool(lib().or_is_irreducible_wedge(_dp(k)))
+
+
+def symmetry_operation(k_iw, k_bz):
+    """apply_same_symmetry_operation's signed permutation: (found, perm[3], sign[3]) with
+    v_bz[j] = sign[j] * v[perm[j]]."""
+    a = np.ascontiguousarray(k_iw, dtype=np.float64)
+    b = np.ascontiguousarray(k_bz, dtype=np.float64)
+    perm = (C.c_int * 3)()
+    sign = (C.c_int * 3)()
+    found = lib().or_symmetry_operation(_dp(a), _dp(b), perm, sign)
+    return bool(found), list(perm), list(sign)
 
 
 def gradient(mat: OrMaterial, G: np.ndarray, k, ev: np.ndarray) -> np.ndarray:

@@ -104,12 +104,10 @@ def test_adjust_values_matches_oracle(native, oracle, nb, soc, mcz):
 
 def test_no_cpu_fallback_when_library_missing(monkeypatch, tmp_path):
     """The binding refuses to run without the native library (it never computes on the CPU)."""
-    import importlib
-
     import ultimateepm_gb300._native as nat
 
     monkeypatch.setattr(nat, "LIB_PATH", str(tmp_path / "absent.so"))
     monkeypatch.setattr(nat, "_lib", None)
     with pytest.raises(RuntimeError, match="no CPU fallback"):
         nat.load()
-    importlib.reload(nat)
+    # monkeypatch restores the path and the loaded library afterwards

@@ -410,4 +410,42 @@ int uepm_adjust_values(double* E, size_t nk, int nb, int soc, int min_cond_zero,
     return UEPM_OK;
 }
 
+// The signed permutation that maps each k_src[q] onto k_dst[q] (component by component of k_dst: the
+// first unused component of k_src whose magnitude matches within 1e-8 * max(1, largest magnitude),
+// the sign from the two components' signs, or from k_dst's where the component vanishes), the rule
+// of apply_same_symmetry_operation (src/BZ_MESH/bz_mesh.cpp:1312-1381), packed for
+// uepm_star_expand_device. found[q] = 0 where no signed permutation matches (identity written; the
+// reference leaves the vector unchanged there).
+int uepm_star_operations(const double* k_src, const double* k_dst, size_t n, uint16_t* op, int32_t* found) {
+    if (n && (!k_src || !k_dst || !op)) return UEPM_ERR_INVALID;
+    for (size_t q = 0; q < n; ++q) {
+        const double* a = k_src + 3 * q;
+        const double* b = k_dst + 3 * q;
+        double        scale = 1.0;
+        for (int c = 0; c < 3; ++c) scale = std::max(scale, std::max(std::fabs(a[c]), std::fabs(b[c])));
+        const double tol = 1e-8 * scale;
+        bool         used[3] = {false, false, false}, ok = true;
+        unsigned     packed  = 0;
+        for (int j = 0; j < 3 && ok; ++j) {
+            int p = -1;
+            for (int i = 0; i < 3; ++i)
+                if (!used[i] && std::fabs(std::fabs(a[i]) - std::fabs(b[j])) <= tol) {
+                    p = i;
+                    break;
+                }
+            if (p < 0) {
+                ok = false;
+                break;
+            }
+            used[p]        = true;
+            const bool neg = std::fabs(a[p]) > tol ? ((a[p] >= 0.0) != (b[j] >= 0.0)) : (b[j] < 0.0);
+            packed |= (unsigned)p << (2 * j);
+            if (neg) packed |= 1u << (6 + j);
+        }
+        op[q] = ok ? (uint16_t)packed : (uint16_t)(0 | 1 << 2 | 2 << 4);
+        if (found) found[q] = ok ? 1 : 0;
+    }
+    return UEPM_OK;
+}
+
 }  // extern "C"

@@ -1,0 +1,235 @@
+"""Band structure over a Brillouin-zone mesh: the caller behind the reference's BandsOnBZ.
+
+Mirrors MeshBZ (src/BZ_MESH/bz_mesh.cpp) for the band-structure part:
+  read_mesh_geometry_from_msh_file   the mesh vertices, scaled by 2 pi / a when asked (:67-105);
+                                     read here from the MSH file itself (ASCII 4.1 or 2.2 $Nodes),
+                                     in the node order gmsh returns them
+  is_irreducible_wedge               z >= 0, z <= y <= x <= 1, x + y + z <= 3/2 in reduced units (:1176)
+  load_kstar_ibz_to_bz               the reference's "<mesh>_kstar_ibz_to_bz.txt" (:198-271)
+  build_kstar_ibz_to_bz              the same map computed here: every vertex folded into the wedge
+                                     (absolute values, sorted descending) and matched to a wedge vertex
+  compute_band_structure_over_mesh   solve the wedge (or every) vertex, AdjustValues, then the wedge
+                                     -> full-zone distribution (:1230-1303)
+  distribute_energies_from_iw_wedge_to_full_bz
+                                     energies copied, gradients taken through the signed permutation
+                                     apply_same_symmetry_operation finds (:1312-1414): on the host, or
+                                     as one device gather (uepm_star_expand_device) after a device solve
+Energies in eV, gradients in eV m (the reference's units), vertex positions in SI (1/m).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import math
+import os
+
+import numpy as np
+
+from . import _native as N
+
+
+def read_msh_nodes(path: str) -> tuple[np.ndarray, np.ndarray]:
+    """Node tags and coordinates (n x 3) of an ASCII MSH 4.1 or 2.2 file, in file order."""
+    with open(path, "r") as f:
+        lines = f.read().splitlines()
+    ver = None
+    i = 0
+    while i < len(lines):
+        t = lines[i].strip()
+        if t == "$MeshFormat":
+            parts = lines[i + 1].split()
+            ver, ftype = float(parts[0]), int(parts[1])
+            if ftype != 0:
+                raise ValueError("binary MSH files are not supported; save the mesh as ASCII")
+            i += 2
+            continue
+        if t == "$Nodes":
+            if ver is None:
+                raise ValueError("$Nodes before $MeshFormat")
+            i += 1
+            if ver >= 4.0:
+                nblocks, nnodes = (int(x) for x in lines[i].split()[:2])
+                i += 1
+                tags = np.empty(nnodes, dtype=np.int64)
+                xyz = np.empty((nnodes, 3))
+                pos = 0
+                for _ in range(nblocks):
+                    _, _, param, nin = (int(x) for x in lines[i].split()[:4])
+                    i += 1
+                    tags[pos:pos + nin] = [int(lines[i + q]) for q in range(nin)]
+                    i += nin
+                    for q in range(nin):
+                        xyz[pos + q] = [float(x) for x in lines[i + q].split()[:3]]
+                    i += nin
+                    pos += nin
+                    del param
+                return tags, xyz
+            n = int(lines[i])
+            i += 1
+            tags = np.empty(n, dtype=np.int64)
+            xyz = np.empty((n, 3))
+            for q in range(n):
+                p = lines[i + q].split()
+                tags[q] = int(p[0])
+                xyz[q] = [float(x) for x in p[1:4]]
+            return tags, xyz
+        i += 1
+    raise ValueError(f"{path}: no $Nodes section")
+
+
+def _fold_key(kr: np.ndarray, digits: int) -> list[tuple]:
+    f = -np.sort(-np.abs(kr), axis=1)  # |k| sorted descending: the wedge representative
+    return [tuple(r) for r in np.round(f, digits)]
+
+
+class MeshBZ:
+    def __init__(self, material):
+        """material: api.Material (its lattice constant sets the SI <-> reduced scale)."""
+        self.material = material
+        self.positions = np.zeros((0, 3))  # SI
+        self.node_tags = np.zeros(0, dtype=np.int64)
+        self.kstar: list[list[int]] = []  # indexed by wedge vertex
+        self.iw_vertices: list[int] = []
+        self.energies = None
+        self.gradients = None
+
+    # ---- geometry --------------------------------------------------------------------------------
+    def si_to_reduced_scale(self) -> float:
+        return self.material.get_lattice_constant_meter() / (2.0 * math.pi)
+
+    def read_mesh_geometry_from_msh_file(self, filename: str, normalize_by_fourier_factor: bool = True):
+        tags, xyz = read_msh_nodes(filename)
+        f = 2.0 * math.pi / self.material.get_lattice_constant_meter() if normalize_by_fourier_factor else 1.0
+        self.node_tags = tags
+        self.positions = xyz * f
+        self.filename = filename
+        return self
+
+    def set_vertices(self, k_reduced: np.ndarray):
+        """Vertices given directly as reduced k-points (n x 3)."""
+        self.positions = np.asarray(k_reduced, dtype=np.float64) / self.si_to_reduced_scale()
+        self.node_tags = np.arange(1, len(self.positions) + 1)
+        return self
+
+    def reduced(self) -> np.ndarray:
+        return self.positions * self.si_to_reduced_scale()
+
+    def is_irreducible_wedge(self, k_si: np.ndarray) -> np.ndarray:
+        k = np.atleast_2d(np.asarray(k_si, dtype=np.float64)) * self.si_to_reduced_scale()
+        x, y, z = k[:, 0], k[:, 1], k[:, 2]
+        eps = 1e-12
+        return (z >= -eps) & (z <= y + eps) & (y <= x + eps) & (x <= 1.0 + eps) & ((x + y + z) <= 1.5 + eps)
+
+    # ---- the k-star of every wedge vertex ---------------------------------------------------------
+    def build_kstar_ibz_to_bz(self, digits: int = 9):
+        """Maps each wedge vertex to the vertices of its star: every vertex folded into the wedge is
+        matched to the wedge vertex at the same reduced position (rounded to `digits` places)."""
+        kr = self.reduced()
+        inw = np.nonzero(self.is_irreducible_wedge(self.positions))[0]
+        if len(inw) == 0:
+            raise RuntimeError("No vertices in irreducible wedge. Cannot distribute energies to full BZ.")
+        where = {}
+        for idx, key in zip(inw, _fold_key(kr[inw], digits)):
+            where.setdefault(key, int(idx))
+        src = np.empty(len(kr), dtype=np.int64)
+        for v, key in enumerate(_fold_key(kr, digits)):
+            if key not in where:
+                raise RuntimeError(f"vertex {v} at {kr[v]} has no image in the irreducible wedge: the mesh is not "
+                                   "symmetric under the cubic group")
+            src[v] = where[key]
+        self._set_star(src)
+        return self
+
+    def load_kstar_ibz_to_bz(self, filename: str):
+        """The reference's kstar file: lines "iw m id_1 ... id_m" (comments '#')."""
+        rows = []
+        with open(filename) as f:
+            for line in f:
+                if not line.strip() or line.startswith("#"):
+                    continue
+                p = line.split()
+                iw, m = int(p[0]), int(p[1])
+                rows.append((iw, [int(x) for x in p[2:2 + m]]))
+        n = len(self.positions)
+        src = np.full(n, -1, dtype=np.int64)
+        inw = self.is_irreducible_wedge(self.positions)
+        for iw, ids in rows:
+            if not inw[iw]:
+                raise RuntimeError(f"load_kstar_file: vertex {iw} does not lie in the irreducible wedge, but it should")
+            for v in ids:
+                if v >= n:
+                    raise RuntimeError(f"load_kstar_file: index {v} out of range")
+                src[v] = iw
+        if (src < 0).any():
+            raise RuntimeError("load_kstar_file: number of k-points in IBZ does not match number of vertices in mesh")
+        self._set_star(src)
+        return self
+
+    def _set_star(self, src: np.ndarray):
+        self.src = src
+        self.iw_vertices = sorted(set(int(s) for s in src))
+        self.kstar = {iw: [] for iw in self.iw_vertices}
+        for v, s in enumerate(src):
+            self.kstar[int(s)].append(v)
+        # signed permutation of every vertex relative to its wedge source (host C ABI)
+        L = N.load()
+        kr = np.ascontiguousarray(self.reduced())
+        ks = np.ascontiguousarray(kr[src])
+        self.ops = np.zeros(len(kr), dtype=np.uint16)
+        found = np.zeros(len(kr), dtype=np.int32)
+        dp = lambda a: a.ctypes.data_as(C.POINTER(C.c_double))
+        N.check(L.uepm_star_operations(dp(ks), dp(kr), len(kr), self.ops.ctypes.data_as(C.POINTER(C.c_uint16)),
+                                       found.ctypes.data_as(C.POINTER(C.c_int32))))
+        self.ops_found = found.astype(bool)
+
+    # ---- band structure ----------------------------------------------------------------------------
+    def compute_band_structure_over_mesh(self, band_structure, use_iwedge: bool = True):
+        """band_structure: an api.BandStructure already Initialize-d (material, bands, basis, flags).
+        Solves the wedge vertices (or all of them), with gradients, shifts by AdjustValues(False), and
+        distributes to the full zone. Returns (energies [n][nb], gradients [n][nb][3])."""
+        kr = self.reduced()
+        if use_iwedge:
+            if not self.iw_vertices:
+                self.build_kstar_ibz_to_bz()
+            used = np.asarray(self.iw_vertices, dtype=np.int64)
+        else:
+            used = np.arange(len(kr))
+        band_structure.set_kpoints(np.ascontiguousarray(kr[used]))
+        band_structure.Compute_parallel(True)
+        band_structure.AdjustValues(False)
+        E = np.asarray(band_structure.get_band_energies())
+        g = np.asarray(band_structure.get_band_energy_gradients())
+        if not use_iwedge:
+            self.energies, self.gradients = E, g
+            return E, g
+        pos = np.full(len(kr), -1, dtype=np.int64)
+        pos[used] = np.arange(len(used))
+        self.energies, self.gradients = self.distribute_energies_from_iw_wedge_to_full_bz(E, g, pos[self.src])
+        return self.energies, self.gradients
+
+    def distribute_energies_from_iw_wedge_to_full_bz(self, E_iw: np.ndarray, g_iw: np.ndarray, src_rows: np.ndarray):
+        """Host gather: rows src_rows[v] of the wedge results for every vertex v, gradients through
+        the vertex's signed permutation."""
+        E = E_iw[src_rows]
+        perm = np.stack([(self.ops >> (2 * j)) & 3 for j in range(3)], axis=1).astype(np.int64)
+        sign = np.stack([np.where((self.ops >> (6 + j)) & 1, -1.0, 1.0) for j in range(3)], axis=1)
+        gs = g_iw[src_rows]  # [n][nb][3]
+        g = np.take_along_axis(gs, perm[:, None, :].repeat(gs.shape[1], axis=1), axis=2) * sign[:, None, :]
+        return E, g
+
+    def distribute_on_device(self, dE_iw, dg_iw, src_rows, stream=None):
+        """Device gather with uepm_star_expand_device: dE_iw [m][nb], dg_iw [m][nb][3] (torch CUDA
+        tensors, float64), src_rows [n] wedge rows. Returns device tensors (E [n][nb], g [n][nb][3])."""
+        import torch
+
+        L = N.load()
+        n, nb = len(src_rows), dE_iw.shape[1]
+        dev = dE_iw.device
+        d_src = torch.from_numpy(np.ascontiguousarray(src_rows, dtype=np.int64)).to(dev)
+        d_op = torch.from_numpy(self.ops.astype(np.int16)).to(dev)
+        E = torch.empty((n, nb), dtype=torch.float64, device=dev)
+        g = torch.empty((n, nb, 3), dtype=torch.float64, device=dev) if dg_iw is not None else None
+        s = stream if stream is not None else torch.cuda.current_stream()
+        p = lambda t: C.c_void_p(t.data_ptr()) if t is not None else None
+        N.check(L.uepm_star_expand_device(p(dE_iw), p(dg_iw), p(d_src), p(d_op), n, nb, p(E), p(g),
+                                          C.c_void_p(s.cuda_stream)))
+        return E, g
