@@ -62,12 +62,57 @@ __device__ __forceinline__ int sturm_count(const float* __restrict__ d, const fl
 
 // One group of LPM lanes per matrix (LPM = smallest power of two >= nb, at most 32), so a warp
 // bisects 32 / LPM matrices at once and every lane carries an eigenvalue.
-// Shared memory of one matrix in k_bisect: d and e^2 in T, plus FP32 copies for the FP64 kernel's
-// FP32 pre-bracketing.
+// Shared memory of one matrix in k_bisect: d and e^2 in T; for the FP64 kernel also their FP32
+// rounding (hi) and remainders (lo), for the FP32 pre-bracketing and the double-single counts.
 template <typename T>
 __host__ __device__ inline size_t bisect_matrix_bytes(int n) {
-    const size_t b = sizeof(T) * 2 * (size_t)n + (sizeof(T) == 8 ? sizeof(float) * 2 * (size_t)n : 0);
+    const size_t b = sizeof(T) * 2 * (size_t)n + (sizeof(T) == 8 ? sizeof(float) * 4 * (size_t)n : 0);
     return (b + 15) & ~(size_t)15;
+}
+
+// Double-single Sturm count: the same LDL^T recurrence with every quantity carried as an unevaluated
+// FP32 pair (about 48 significant bits) on the FP32 pipe, ~30 FP32 instructions per step instead of
+// 6 FP64 ones (64x wider pipe). Its backward error, a few 2^-48 ||T||, bounds how far the
+// double-single phase of the bisection may go; the final bracket is confirmed and finished with
+// FP64 counts. Two-sum (Knuth) and exact products (fmaf) with non-contracted operations.
+struct dsf {
+    float h, l;
+};
+__device__ __forceinline__ dsf ds_norm(float s, float e) {  // |s| >= |e|
+    const float t = __fadd_rn(s, e);
+    return dsf{t, __fsub_rn(e, __fsub_rn(t, s))};
+}
+__device__ __forceinline__ dsf ds_sub(dsf a, dsf b) {
+    const float s  = __fsub_rn(a.h, b.h);
+    const float bb = __fsub_rn(s, a.h);
+    const float e  = __fadd_rn(__fsub_rn(a.h, __fsub_rn(s, bb)), __fsub_rn(__fsub_rn(0.f, b.h), bb));
+    return ds_norm(s, __fadd_rn(e, __fsub_rn(a.l, b.l)));
+}
+__device__ __forceinline__ dsf ds_div(dsf a, dsf q) {
+    const float rq = __frcp_rn(q.h);
+    const float r1 = __fmul_rn(a.h, rq);
+    const float p  = __fmul_rn(r1, q.h);
+    const float pe = fmaf(r1, q.h, -p);
+    float       t  = __fsub_rn(__fsub_rn(a.h, p), pe);
+    t              = fmaf(-r1, q.l, __fadd_rn(t, a.l));
+    return ds_norm(r1, __fmul_rn(t, rq));
+}
+__device__ __forceinline__ int sturm_count_ds(const float* dh, const float* dl, const float* e2h, const float* e2l, int n,
+                                              dsf x, float pivmin) {
+    dsf q = ds_sub(dsf{dh[0], dl[0]}, x);
+    if (fabsf(q.h) <= pivmin) q = dsf{-pivmin, 0.f};
+    int cnt = q.h < 0.f;
+    for (int i = 1; i < n; ++i) {
+        const dsf r = ds_div(dsf{e2h[i - 1], e2l[i - 1]}, q);
+        q           = ds_sub(ds_sub(dsf{dh[i], dl[i]}, x), r);
+        if (fabsf(q.h) <= pivmin) q = dsf{-pivmin, 0.f};
+        cnt += q.h < 0.f;
+    }
+    return cnt;
+}
+__device__ __forceinline__ dsf ds_of(double v) {
+    const float h = __double2float_rn(v);
+    return dsf{h, __double2float_rn(v - (double)h)};
 }
 
 template <typename T>
@@ -81,8 +126,10 @@ __global__ void k_bisect(const T* __restrict__ dIn, const T* __restrict__ eIn, i
     unsigned char* mine = smraw + ((size_t)warp * mpw + g) * bisect_matrix_bytes<T>(n);
     T*             d    = reinterpret_cast<T*>(mine);
     T*             e2   = d + n;
-    float*         df   = reinterpret_cast<float*>(e2 + n);  // FP64 kernel only
+    float*         df   = reinterpret_cast<float*>(e2 + n);  // FP64 kernel only: hi parts
     float*         e2f  = df + n;
+    float*         dlo  = e2f + n;                           // lo parts
+    float*         e2lo = dlo + n;
     const bool valid = b < batch;
     T          lo = T(3.0e38), hi = T(-3.0e38), emax2 = T(0);
     if (valid) {
@@ -93,11 +140,17 @@ __global__ void k_bisect(const T* __restrict__ dIn, const T* __restrict__ eIn, i
             const T em = (i > 0) ? fabs(eg[i - 1]) : T(0);
             const T ep = (i < n - 1) ? fabs(eg[i]) : T(0);
             d[i]       = di;
-            if (sizeof(T) == 8) df[i] = (float)di;
+            if (sizeof(T) == 8) {
+                df[i]  = (float)di;
+                dlo[i] = (float)((double)di - (double)df[i]);
+            }
             if (i < n - 1) {
                 e2[i] = eg[i] * eg[i];
                 emax2 = max(emax2, e2[i]);
-                if (sizeof(T) == 8) e2f[i] = (float)e2[i];
+                if (sizeof(T) == 8) {
+                    e2f[i]  = (float)e2[i];
+                    e2lo[i] = (float)((double)e2[i] - (double)e2f[i]);
+                }
             }
             lo = min(lo, di - em - ep);
             hi = max(hi, di + em + ep);
@@ -138,6 +191,21 @@ __global__ void k_bisect(const T* __restrict__ dIn, const T* __restrict__ eIn, i
             if (lo2 < hi2 && sturm_count(d, e2, n, lo2, pivmin) <= j && sturm_count(d, e2, n, hi2, pivmin) > j) {
                 a = lo2;
                 c = hi2;
+                // double-single phase: bisect down to a few units of its backward error, widen by
+                // that error and keep the bracket only if two FP64 counts confirm it
+                const T ulp_ds = T(3.552713678800501e-15) * tnorm;  // 2^-48 ||T||
+                T       ad = a, cd = c;
+                for (int it = 0; it < 64; ++it) {
+                    const T mid = T(0.5) * (ad + cd);
+                    if (cd - ad <= T(64) * ulp_ds || mid <= ad || mid >= cd) break;
+                    if (sturm_count_ds(df, dlo, e2f, e2lo, n, ds_of((double)mid), pivf) > j) cd = mid;
+                    else ad = mid;
+                }
+                const T lo3 = max(a, ad - T(16) * ulp_ds), hi3 = min(c, cd + T(16) * ulp_ds);
+                if (lo3 < hi3 && sturm_count(d, e2, n, lo3, pivmin) <= j && sturm_count(d, e2, n, hi3, pivmin) > j) {
+                    a = lo3;
+                    c = hi3;
+                }
             }
         }
         // count(a) <= j < count(c) holds throughout; at most ~log2(range / atol) < 200 steps.
