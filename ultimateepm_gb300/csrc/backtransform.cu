@@ -32,10 +32,12 @@ __global__ void __launch_bounds__(32 * kBtMaxWarps) k_backtransform(const S* __r
     const int     b  = blockIdx.x;
     if (b >= batch) return;
     extern __shared__ __align__(16) unsigned char smraw[];
-    S*        Vs   = reinterpret_cast<S*>(smraw);  // [kb][n]: reflector i0 + q in row q
-    S*        taus = Vs + (size_t)kb * n;          // [kb]
+    const int ldv  = (n + LPV - 1) / LPV * LPV;     // staged row length, zero-padded beyond n
+    S*        Vs   = reinterpret_cast<S*>(smraw);  // [kb][ldv]: reflector i0 + q in row q
+    S*        taus = Vs + (size_t)kb * ldv;        // [kb]
     const int tid = threadIdx.x, nthr = blockDim.x;
     const int lane = tid & 31, gl = lane & (LPV - 1);
+    const int warp = tid >> 5, nwarp = nthr >> 5;
     const int grp = tid / LPV, ngrp = nthr / LPV;
     const S*  A   = H + (size_t)b * mstride;
     const S*  tb  = tq + (size_t)b * n;
@@ -52,40 +54,54 @@ __global__ void __launch_bounds__(32 * kBtMaxWarps) k_backtransform(const S* __r
         for (int i1 = n - 2; i1 >= 0; i1 -= kb) {
             const int i0 = max(0, i1 - kb + 1), cnt = i1 - i0 + 1;
             __syncthreads();  // previous block consumed
-            for (int q = tid; q < cnt * n; q += nthr) {
-                const int k = q / n, r = q - k * n, i = i0 + k;
-                S         v = ST<S>::zero();
-                if (r == i + 1) v = ST<S>::one();
-                else if (r > i + 1) v = ldc(A + (size_t)i * ld + r);
-                Vs[q] = v;
+            for (int k = warp; k < cnt; k += nwarp) {
+                const int i  = i0 + k;
+                const S*  ac = A + (size_t)i * ld;
+                S*        vs = Vs + (size_t)k * ldv;
+                for (int r = lane; r < ldv; r += 32) {
+                    S v = ST<S>::zero();
+                    if (r == i + 1) v = ST<S>::one();
+                    else if (r > i + 1 && r < n) v = ldc(ac + r);
+                    vs[r] = v;
+                }
             }
             for (int q = tid; q < cnt; q += nthr) taus[q] = tb[i0 + q];
             __syncthreads();
-            for (int i = i1; i >= i0; --i) {
-                const S tau = taus[i - i0];
-                if (ST<S>::re(tau) == R(0) && ST<S>::im(tau) == R(0)) continue;  // uniform
-                const S*  vrow = Vs + (size_t)(i - i0) * n;
-                const int t0   = (i + 1) / LPV;
-                S         dot  = ST<S>::zero();
+            // Reflector i is zero on rows <= i, i.e. on the chunks t < (i + 1) / LPV of every lane:
+            // the reflectors are taken in runs of equal first live chunk tc, and with the run loop
+            // unrolled tc is a constant, so the dead chunks are not issued at all. The staged rows
+            // are zero-padded to ldv (a multiple of LPV), so no per-row bound is needed below ldv.
 #pragma unroll
-                for (int t = 0; t < T; ++t) {
-                    const int r = gl + LPV * t;
-                    if (t >= t0 && r < n) dot = cfmac(vrow[r], zr[t], dot);
-                }
+            for (int tc = T - 1; tc >= 0; --tc) {
+                if (LPV * tc >= ldv) continue;  // uniform
+                const int ihi = min(i1, LPV * tc + LPV - 2), ilo = max(i0, LPV * tc - 1);
+                for (int i = ihi; i >= ilo; --i) {
+                    const S tau = taus[i - i0];
+                    if (ST<S>::re(tau) == R(0) && ST<S>::im(tau) == R(0)) continue;  // uniform
+                    const S* vrow = Vs + (size_t)(i - i0) * ldv + gl;
+                    S        dot0 = ST<S>::zero(), dot1 = ST<S>::zero();
 #pragma unroll
-                for (int o = LPV / 2; o > 0; o >>= 1) {
-                    if constexpr (sizeof(S) == sizeof(R)) {
-                        dot += __shfl_xor_sync(0xffffffffu, dot, o);
-                    } else {
-                        dot = ST<S>::make(ST<S>::re(dot) + __shfl_xor_sync(0xffffffffu, ST<S>::re(dot), o),
-                                          ST<S>::im(dot) + __shfl_xor_sync(0xffffffffu, ST<S>::im(dot), o));
+                    for (int t = tc; t < T; ++t) {
+                        if (LPV * t < ldv) {  // uniform
+                            if ((t - tc) & 1) dot1 = cfmac(vrow[LPV * t], zr[t], dot1);
+                            else dot0 = cfmac(vrow[LPV * t], zr[t], dot0);
+                        }
                     }
-                }
-                const S sdt = ST<S>::neg(cmul(tau, dot));
+                    S dot = cadd(dot0, dot1);
 #pragma unroll
-                for (int t = 0; t < T; ++t) {
-                    const int r = gl + LPV * t;
-                    if (t >= t0 && r < n) zr[t] = cfma(vrow[r], sdt, zr[t]);
+                    for (int o = LPV / 2; o > 0; o >>= 1) {
+                        if constexpr (sizeof(S) == sizeof(R)) {
+                            dot += __shfl_xor_sync(0xffffffffu, dot, o);
+                        } else {
+                            dot = ST<S>::make(ST<S>::re(dot) + __shfl_xor_sync(0xffffffffu, ST<S>::re(dot), o),
+                                              ST<S>::im(dot) + __shfl_xor_sync(0xffffffffu, ST<S>::im(dot), o));
+                        }
+                    }
+                    const S sdt = ST<S>::neg(cmul(tau, dot));
+#pragma unroll
+                    for (int t = tc; t < T; ++t) {
+                        if (LPV * t < ldv) zr[t] = cfma(vrow[LPV * t], sdt, zr[t]);
+                    }
                 }
             }
         }
@@ -135,8 +151,9 @@ static void bt_launch(const S* H, int n, int ld, size_t mstride, const S* tq, co
                       int batch, cudaStream_t s) {
     constexpr int GW    = 32 / LPV;
     const int     warps = std::min(kBtMaxWarps, (nb + GW - 1) / GW);
-    const int     kb    = std::max(4, std::min(64, (int)(kBtStageBytes / (sizeof(S) * (size_t)(n + 1)))));
-    const size_t  smem  = sizeof(S) * ((size_t)kb * n + kb);
+    const int     ldv   = (n + LPV - 1) / LPV * LPV;
+    const int     kb    = std::max(4, std::min(64, (int)(kBtStageBytes / (sizeof(S) * (size_t)(ldv + 1)))));
+    const size_t  smem  = sizeof(S) * ((size_t)kb * ldv + kb);
     auto          kern  = k_backtransform<S, LPV, T>;
     if (smem > 48 * 1024) cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     kern<<<batch, 32 * warps, smem, s>>>(H, n, ld, mstride, tq, z, nb, kb, Xout, P, d_k, d_G, grad, batch);
