@@ -18,6 +18,14 @@
 namespace uepm {
 
 constexpr int kBtMaxWarps = 8;
+
+// cp.async of one naturally aligned element of B = 4 or 8 bytes, global -> shared
+template <int B>
+__device__ __forceinline__ void cp_async_elem(void* dst, const void* src) {
+    const unsigned sa = (unsigned)__cvta_generic_to_shared(dst);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], %2;\n" ::"r"(sa), "l"(src), "n"(B) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
 constexpr int kBtStageBytes = 48 << 10;
 
 template <typename S, int LPV, int T>
@@ -54,18 +62,25 @@ __global__ void __launch_bounds__(32 * kBtMaxWarps) k_backtransform(const S* __r
         for (int i1 = n - 2; i1 >= 0; i1 -= kb) {
             const int i0 = max(0, i1 - kb + 1), cnt = i1 - i0 + 1;
             __syncthreads();  // previous block consumed
+            // asynchronous element copies: every load of the block is in flight at once, so the
+            // memory latency is paid once per block rather than once per element of each thread
             for (int k = warp; k < cnt; k += nwarp) {
                 const int i  = i0 + k;
                 const S*  ac = A + (size_t)i * ld;
                 S*        vs = Vs + (size_t)k * ldv;
                 for (int r = lane; r < ldv; r += 32) {
-                    S v = ST<S>::zero();
-                    if (r == i + 1) v = ST<S>::one();
-                    else if (r > i + 1 && r < n) v = ldc(ac + r);
-                    vs[r] = v;
+                    if (r > i + 1 && r < n) {
+                        // per real component: each copy is then aligned to its own size
+                        const R* src = reinterpret_cast<const R*>(ac + r);
+                        R*       dst = reinterpret_cast<R*>(vs + r);
+                        cp_async_elem<sizeof(R)>(dst, src);
+                        if constexpr (sizeof(S) != sizeof(R)) cp_async_elem<sizeof(R)>(dst + 1, src + 1);
+                    }
+                    else vs[r] = (r == i + 1) ? ST<S>::one() : ST<S>::zero();
                 }
             }
             for (int q = tid; q < cnt; q += nthr) taus[q] = tb[i0 + q];
+            cp_async_wait_all();
             __syncthreads();
             // Reflector i is zero on rows <= i, i.e. on the chunks t < (i + 1) / LPV of every lane:
             // the reflectors are taken in runs of equal first live chunk tc, and with the run loop
