@@ -26,12 +26,21 @@ __device__ __forceinline__ void cp_async_elem(void* dst, const void* src) {
     asm volatile("cp.async.ca.shared.global [%0], [%1], %2;\n" ::"r"(sa), "l"(src), "n"(B) : "memory");
 }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
+
+// Start of reflector i in the packed staging of reflectors 0, 1, ...: reflector i' keeps the rows
+// LPV floor((i' + 1) / LPV) .. ldv - 1, so the first i rows sum to
+// i ldv - LPV sum_{q=1..i} floor(q / LPV) = i ldv - LPV (LPV c (c - 1) / 2 + c (i - c LPV + 1)), c = floor(i / LPV).
+template <int LPV>
+__host__ __device__ __forceinline__ int packed_off(int i, int ldv) {
+    const int c = i / LPV;
+    return i * ldv - LPV * (LPV * c * (c - 1) / 2 + c * (i - c * LPV + 1));
+}
 constexpr int kBtStageBytes = 48 << 10;
 
 template <typename S, int LPV, int T>
 __global__ void __launch_bounds__(32 * kBtMaxWarps) k_backtransform(const S* __restrict__ H, int n, int ld, size_t mstride,
                                                                    const S* __restrict__ tq,
-                                                                   const typename ST<S>::R* __restrict__ z, int nb, int kb,
+                                                                   const typename ST<S>::R* __restrict__ z, int nb, int cap,
                                                                    cx<typename ST<S>::R>* __restrict__ Xout,
                                                                    const DevParams P, const double* __restrict__ kpts,
                                                                    const int* __restrict__ G, double* __restrict__ grad,
@@ -40,9 +49,14 @@ __global__ void __launch_bounds__(32 * kBtMaxWarps) k_backtransform(const S* __r
     const int     b  = blockIdx.x;
     if (b >= batch) return;
     extern __shared__ __align__(16) unsigned char smraw[];
-    const int ldv  = (n + LPV - 1) / LPV * LPV;     // staged row length, zero-padded beyond n
-    S*        Vs   = reinterpret_cast<S*>(smraw);  // [kb][ldv]: reflector i0 + q in row q
-    S*        taus = Vs + (size_t)kb * ldv;        // [kb]
+    // Reflector i is zero on rows <= i, i.e. on the row chunks t < tc(i) = (i + 1) / LPV of every
+    // lane, so it is staged packed: rows LPV tc(i) .. ldv - 1 only (ldv = n rounded up to LPV, the
+    // rows from n on zero), at packed_off(i) - packed_off(i0) in a block [i0, i1] of reflectors
+    // whose packed rows fit `cap` elements. At basis 137 (FP32) all 136 reflectors take 43 KB: one
+    // block, one wait.
+    const int ldv  = (n + LPV - 1) / LPV * LPV;
+    S*        Vs   = reinterpret_cast<S*>(smraw);  // [cap] packed reflector rows
+    S*        taus = Vs + cap;                     // [n]
     const int tid = threadIdx.x, nthr = blockDim.x;
     const int lane = tid & 31, gl = lane & (LPV - 1);
     const int warp = tid >> 5, nwarp = nthr >> 5;
@@ -54,47 +68,67 @@ __global__ void __launch_bounds__(32 * kBtMaxWarps) k_backtransform(const S* __r
         const int  j   = ch * ngrp + grp;
         const bool has = j < nb;
         S          zr[T];
+        int        i0 = 0;
+        if (n < 2) {  // no reflectors: the vectors are those of T
 #pragma unroll
-        for (int t = 0; t < T; ++t) {
-            const int r = gl + LPV * t;
-            zr[t]       = ST<S>::make((has && r < n) ? z[((size_t)b * nb + j) * n + r] : R(0), R(0));
+            for (int t = 0; t < T; ++t) {
+                const int r = gl + LPV * t;
+                zr[t]       = ST<S>::make((has && r < n) ? z[((size_t)b * nb + j) * n + r] : R(0), R(0));
+            }
         }
-        for (int i1 = n - 2; i1 >= 0; i1 -= kb) {
-            const int i0 = max(0, i1 - kb + 1), cnt = i1 - i0 + 1;
+        for (int i1 = n - 2; i1 >= 0; i1 = i0 - 1) {
+            // smallest i0 whose block [i0, i1] fits (one reflector always does: cap >= ldv)
+            const int end = packed_off<LPV>(i1 + 1, ldv);
+            int       lo = 0, hi = i1;
+            while (lo < hi) {
+                const int mid = (lo + hi) >> 1;
+                if (end - packed_off<LPV>(mid, ldv) <= cap) hi = mid;
+                else lo = mid + 1;
+            }
+            i0             = lo;
+            const int off0 = packed_off<LPV>(i0, ldv);
             __syncthreads();  // previous block consumed
             // asynchronous element copies: every load of the block is in flight at once, so the
             // memory latency is paid once per block rather than once per element of each thread
-            for (int k = warp; k < cnt; k += nwarp) {
-                const int i  = i0 + k;
+            for (int i = i0 + warp; i <= i1; i += nwarp) {
+                const int r0 = LPV * ((i + 1) / LPV);
                 const S*  ac = A + (size_t)i * ld;
-                S*        vs = Vs + (size_t)k * ldv;
-                for (int r = lane; r < ldv; r += 32) {
+                S*        vs = Vs + (packed_off<LPV>(i, ldv) - off0) - r0;
+                for (int r = r0 + lane; r < ldv; r += 32) {
                     if (r > i + 1 && r < n) {
                         // per real component: each copy is then aligned to its own size
                         const R* src = reinterpret_cast<const R*>(ac + r);
                         R*       dst = reinterpret_cast<R*>(vs + r);
                         cp_async_elem<sizeof(R)>(dst, src);
                         if constexpr (sizeof(S) != sizeof(R)) cp_async_elem<sizeof(R)>(dst + 1, src + 1);
+                    } else {
+                        vs[r] = (r == i + 1) ? ST<S>::one() : ST<S>::zero();
                     }
-                    else vs[r] = (r == i + 1) ? ST<S>::one() : ST<S>::zero();
                 }
             }
-            for (int q = tid; q < cnt; q += nthr) taus[q] = tb[i0 + q];
+            for (int i = i0 + tid; i <= i1; i += nthr) taus[i] = tb[i];
+            if (i1 == n - 2) {  // first block: the vectors load while the reflectors are in flight
+#pragma unroll
+                for (int t = 0; t < T; ++t) {
+                    const int r = gl + LPV * t;
+                    zr[t]       = ST<S>::make((has && r < n) ? z[((size_t)b * nb + j) * n + r] : R(0), R(0));
+                }
+            }
             cp_async_wait_all();
             __syncthreads();
-            // Reflector i is zero on rows <= i, i.e. on the chunks t < (i + 1) / LPV of every lane:
-            // the reflectors are taken in runs of equal first live chunk tc, and with the run loop
-            // unrolled tc is a constant, so the dead chunks are not issued at all. The staged rows
-            // are zero-padded to ldv (a multiple of LPV), so no per-row bound is needed below ldv.
+            // the reflectors in runs of equal tc; with the run loop unrolled tc is a constant, so
+            // the dead chunks are not issued at all
 #pragma unroll
             for (int tc = T - 1; tc >= 0; --tc) {
                 if (LPV * tc >= ldv) continue;  // uniform
                 const int ihi = min(i1, LPV * tc + LPV - 2), ilo = max(i0, LPV * tc - 1);
-                for (int i = ihi; i >= ilo; --i) {
-                    const S tau = taus[i - i0];
+                if (ihi < ilo) continue;
+                const int len  = ldv - LPV * tc;
+                const S*  vrow = Vs + (packed_off<LPV>(ihi, ldv) - off0) - LPV * tc + gl;
+                for (int i = ihi; i >= ilo; --i, vrow -= len) {
+                    const S tau = taus[i];
                     if (ST<S>::re(tau) == R(0) && ST<S>::im(tau) == R(0)) continue;  // uniform
-                    const S* vrow = Vs + (size_t)(i - i0) * ldv + gl;
-                    S        dot0 = ST<S>::zero(), dot1 = ST<S>::zero();
+                    S dot0 = ST<S>::zero(), dot1 = ST<S>::zero();
 #pragma unroll
                     for (int t = tc; t < T; ++t) {
                         if (LPV * t < ldv) {  // uniform
@@ -167,11 +201,12 @@ static void bt_launch(const S* H, int n, int ld, size_t mstride, const S* tq, co
     constexpr int GW    = 32 / LPV;
     const int     warps = std::min(kBtMaxWarps, (nb + GW - 1) / GW);
     const int     ldv   = (n + LPV - 1) / LPV * LPV;
-    const int     kb    = std::max(4, std::min(64, (int)(kBtStageBytes / (sizeof(S) * (size_t)(ldv + 1)))));
-    const size_t  smem  = sizeof(S) * ((size_t)kb * ldv + kb);
+    const int     total = packed_off<LPV>(std::max(n - 1, 0), ldv);  // all n - 1 reflectors
+    const int     cap   = std::max(ldv, std::min(total, (int)(kBtStageBytes / sizeof(S))));
+    const size_t  smem  = sizeof(S) * ((size_t)cap + n);
     auto          kern  = k_backtransform<S, LPV, T>;
     if (smem > 48 * 1024) cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    kern<<<batch, 32 * warps, smem, s>>>(H, n, ld, mstride, tq, z, nb, kb, Xout, P, d_k, d_G, grad, batch);
+    kern<<<batch, 32 * warps, smem, s>>>(H, n, ld, mstride, tq, z, nb, cap, Xout, P, d_k, d_G, grad, batch);
     count_launch();
 }
 
