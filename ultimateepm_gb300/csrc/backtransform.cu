@@ -19,13 +19,6 @@ namespace uepm {
 
 constexpr int kBtMaxWarps = 8;
 
-// cp.async of one naturally aligned element of B = 4 or 8 bytes, global -> shared
-template <int B>
-__device__ __forceinline__ void cp_async_elem(void* dst, const void* src) {
-    const unsigned sa = (unsigned)__cvta_generic_to_shared(dst);
-    asm volatile("cp.async.ca.shared.global [%0], [%1], %2;\n" ::"r"(sa), "l"(src), "n"(B) : "memory");
-}
-__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
 
 // Start of reflector i in the packed staging of reflectors 0, 1, ...: reflector i' keeps the rows
 // LPV floor((i' + 1) / LPV) .. ldv - 1, so the first i rows sum to

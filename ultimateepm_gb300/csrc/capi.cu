@@ -8,6 +8,7 @@
 //         -> k_invit<float> -> k_backtransform<float> -> k_refine (FP64 Rayleigh-Ritz: E, X, gradient)
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <atomic>
 #include <cmath>
 #include <cstdio>
@@ -293,7 +294,8 @@ void run_chunk(uepm_ctx* ctx, const Layout& L, char* ws, const double* kk, int c
     }
     {
         ProfScope p(ctx, s, KK_REFINE_PROJECT);
-        const SparseV sv{ctx->sparse_local, ctx->d_csr_ptr, ctx->d_csr_col, ctx->d_csr_val, ctx->d_Vloc, rows, ctx->N};
+        const SparseV sv{ctx->sparse_local, ctx->ell_w,  ctx->d_ell_col, ctx->d_ell_re,
+                         ctx->d_ell_im,       ctx->d_Vloc, rows,            ctx->N};
         launch_refine_project<S>(Hs, n, n, mstride, X32, m, rw, small, c, s, sv);
     }
     S* W = small + (size_t)2 * m * m;  // W block of the first matrix; matrices are refine_small_elems apart
@@ -508,33 +510,48 @@ int uepm_ctx_create(const uepm_material* mat, const int32_t* G, int N, uint32_t 
             return fail(e, "copy phSO");
     }
     if (!nl && !soc) {
-        // CSR of V by rows, columns ascending, the diagonal always listed (its value gets the kinetic
-        // term per k on the device); values split into FP32 pairs (round to nearest, as on the device)
-        std::vector<int> ptr(N + 1, 0), col;
-        std::vector<ds4> val;
-        auto             split = [](double v, float* hi, float* lo) {
-            *hi = (float)v;
-            *lo = (float)(v - (double)*hi);
-        };
+        // V off the diagonal in transposed ELL form (slot e of row i at [e][i], columns ascending
+        // within a row, short rows padded with zero values at column i); values split into FP32
+        // pairs (round to nearest, as on the device). The diagonal gets the kinetic term per k on
+        // the device.
+        std::vector<std::vector<int>> nz(N);
+        int                           W = 0;
         for (int i = 0; i < N; ++i) {
             for (int j = 0; j < N; ++j) {
                 const double2 v = V[(size_t)j * N + i];
-                if (j != i && v.x == 0.0 && v.y == 0.0) continue;
-                ds4 d;
-                split(v.x, &d.rhi, &d.rlo);
-                split(v.y, &d.ihi, &d.ilo);
-                col.push_back(j);
-                val.push_back(d);
+                if (j != i && (v.x != 0.0 || v.y != 0.0)) nz[i].push_back(j);
             }
-            ptr[i + 1] = (int)col.size();
+            W = std::max(W, (int)nz[i].size());
         }
-        if ((e = cudaMalloc(&ctx->d_csr_ptr, sizeof(int) * ptr.size())) != cudaSuccess) return fail(e, "cudaMalloc(csr)");
-        if ((e = cudaMalloc(&ctx->d_csr_col, sizeof(int) * col.size())) != cudaSuccess) return fail(e, "cudaMalloc(csr)");
-        if ((e = cudaMalloc(&ctx->d_csr_val, sizeof(ds4) * val.size())) != cudaSuccess) return fail(e, "cudaMalloc(csr)");
-        if ((e = cudaMemcpy(ctx->d_csr_ptr, ptr.data(), sizeof(int) * ptr.size(), cudaMemcpyHostToDevice)) != cudaSuccess ||
-            (e = cudaMemcpy(ctx->d_csr_col, col.data(), sizeof(int) * col.size(), cudaMemcpyHostToDevice)) != cudaSuccess ||
-            (e = cudaMemcpy(ctx->d_csr_val, val.data(), sizeof(ds4) * val.size(), cudaMemcpyHostToDevice)) != cudaSuccess)
-            return fail(e, "copy csr");
+        const size_t        cnt = std::max<size_t>(1, (size_t)W * N);
+        std::vector<int>    col(cnt, 0);
+        std::vector<float2> re(cnt, float2{0.f, 0.f}), im(cnt, float2{0.f, 0.f});
+        auto                split = [](double v) {
+            const float hi = (float)v;
+            return float2{hi, (float)(v - (double)hi)};
+        };
+        for (int i = 0; i < N; ++i) {
+            for (int e = 0; e < W; ++e) {
+                const size_t o = (size_t)e * N + i;
+                if (e < (int)nz[i].size()) {
+                    const int     j = nz[i][e];
+                    const double2 v = V[(size_t)j * N + i];
+                    col[o]          = j;
+                    re[o]           = split(v.x);
+                    im[o]           = split(v.y);
+                } else {
+                    col[o] = i;
+                }
+            }
+        }
+        ctx->ell_w = W;
+        if ((e = cudaMalloc(&ctx->d_ell_col, sizeof(int) * cnt)) != cudaSuccess) return fail(e, "cudaMalloc(ell)");
+        if ((e = cudaMalloc(&ctx->d_ell_re, sizeof(float2) * cnt)) != cudaSuccess) return fail(e, "cudaMalloc(ell)");
+        if ((e = cudaMalloc(&ctx->d_ell_im, sizeof(float2) * cnt)) != cudaSuccess) return fail(e, "cudaMalloc(ell)");
+        if ((e = cudaMemcpy(ctx->d_ell_col, col.data(), sizeof(int) * cnt, cudaMemcpyHostToDevice)) != cudaSuccess ||
+            (e = cudaMemcpy(ctx->d_ell_re, re.data(), sizeof(float2) * cnt, cudaMemcpyHostToDevice)) != cudaSuccess ||
+            (e = cudaMemcpy(ctx->d_ell_im, im.data(), sizeof(float2) * cnt, cudaMemcpyHostToDevice)) != cudaSuccess)
+            return fail(e, "copy ell");
         ctx->sparse_local = true;
     }
     *out = ctx;
@@ -547,9 +564,9 @@ int uepm_ctx_destroy(uepm_ctx* ctx) {
     if (ctx->d_Vloc) cudaFree(ctx->d_Vloc);
     if (ctx->d_phNL) cudaFree(ctx->d_phNL);
     if (ctx->d_phSO) cudaFree(ctx->d_phSO);
-    if (ctx->d_csr_ptr) cudaFree(ctx->d_csr_ptr);
-    if (ctx->d_csr_col) cudaFree(ctx->d_csr_col);
-    if (ctx->d_csr_val) cudaFree(ctx->d_csr_val);
+    if (ctx->d_ell_col) cudaFree(ctx->d_ell_col);
+    if (ctx->d_ell_re) cudaFree(ctx->d_ell_re);
+    if (ctx->d_ell_im) cudaFree(ctx->d_ell_im);
     if (ctx->d_ws) cudaFree(ctx->d_ws);
     if (ctx->d_io) cudaFree(ctx->d_io);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);

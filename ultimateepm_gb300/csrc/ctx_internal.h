@@ -30,9 +30,10 @@ struct uepm_ctx {
     // k-independent local form-factor matrix, sparse (|G_i - G_j|^2 in {3, 4, 8, 11}); its rows as
     // CSR (every row also lists its diagonal) with values as FP32 pairs, for the mixed path's H X
     bool          sparse_local = false;
-    int*          d_csr_ptr = nullptr;
-    int*          d_csr_col = nullptr;
-    uepm::ds4*    d_csr_val = nullptr;
+    int           ell_w     = 0;        // off-diagonal slots per row of V (transposed ELL)
+    int*          d_ell_col = nullptr;  // [ell_w][N]
+    float2*       d_ell_re  = nullptr;  // [ell_w][N] FP32 pairs of Re V
+    float2*       d_ell_im  = nullptr;  // [ell_w][N] FP32 pairs of Im V
     void*         d_ws      = nullptr;
     size_t        ws_bytes  = 0;
     // buffers of the host-pointer entry point

@@ -49,24 +49,50 @@ __device__ __forceinline__ XElem<S> x_at(const XElem<S>* Xs, const cx<float>* Xg
     else return make_float2(v.x, v.y);
 }
 
-// The stored pair of element (r, c) of a local-potential H: the CSR value, or on the diagonal
-// V_rr + kinetic in FP64 (the sum the assembly forms) split into FP32 pairs.
+// The diagonal of a local-potential H as stored pairs: V_rr + kinetic in FP64 (the sum the
+// assembly forms) split into FP32 pairs.
 __device__ __forceinline__ ds2 split_pair(double v) {
     const float hi = __double2float_rn(v);
     return ds2{hi, __double2float_rn(v - (double)hi)};
 }
 template <typename S>
-__device__ __forceinline__ typename Split<S>::type sparse_elem(const SparseV& sv, int b, int r, int e) {
-    const int c = sv.col[e];
+__device__ __forceinline__ typename Split<S>::type sparse_diag(const SparseV& sv, int b, int r) {
+    const cx<double> v  = sv.Vloc[(size_t)r * sv.N + r];
+    const ds2        re = split_pair(v.x + sv.rows[((size_t)b * sv.N + r) * ROW_STRIDE + RF_KIN]);
     if constexpr (std::is_same<S, double>::value) {
-        if (c != r) return ds2{sv.val[e].rhi, sv.val[e].rlo};
-        return split_pair(sv.Vloc[(size_t)r * sv.N + r].x + sv.rows[((size_t)b * sv.N + r) * ROW_STRIDE + RF_KIN]);
+        return re;
     } else {
-        if (c != r) return sv.val[e];
-        const cx<double> v  = sv.Vloc[(size_t)r * sv.N + r];
-        const ds2        re = split_pair(v.x + sv.rows[((size_t)b * sv.N + r) * ROW_STRIDE + RF_KIN]);
-        const ds2        im = split_pair(v.y);
+        const ds2 im = split_pair(v.y);
         return ds4{re.hi, re.lo, im.hi, im.lo};
+    }
+}
+template <typename S>
+__device__ __forceinline__ typename Split<S>::type sparse_slot(const SparseV& sv, size_t o) {
+    const float2 a = sv.re[o];
+    if constexpr (std::is_same<S, double>::value) {
+        return ds2{a.x, a.y};
+    } else {
+        const float2 c = sv.im[o];
+        return ds4{a.x, a.y, c.x, c.y};
+    }
+}
+
+// y[q] += h x(c, j0 + q), q < kProjVB
+template <typename S, bool STAGED>
+__device__ __forceinline__ void proj_accumulate(dsacc (&yr)[kProjVB], dsacc (&yi)[kProjVB], const typename Split<S>::type& h,
+                                                const XElem<S>* Xs, const cx<float>* Xg, int n, int m, int mp, int c,
+                                                int j0) {
+#pragma unroll
+    for (int q = 0; q < kProjVB; ++q) {
+        const XElem<S> x = x_at<S, STAGED>(Xs, Xg, n, m, mp, c, j0 + q);
+        if constexpr (!std::is_same<S, double>::value) {  // (hr + i hi)(xr + i xi)
+            ds_add_prod(yr[q], h.rhi, h.rlo, x.x);
+            ds_add_prod(yr[q], -h.ihi, -h.ilo, x.y);
+            ds_add_prod(yi[q], h.rhi, h.rlo, x.y);
+            ds_add_prod(yi[q], h.ihi, h.ilo, x.x);
+        } else {
+            ds_add_prod(yr[q], h.hi, h.lo, x);
+        }
     }
 }
 
@@ -86,10 +112,16 @@ __global__ void __launch_bounds__(kProjNT) k_refine_project(const typename Split
     extern __shared__ __align__(16) unsigned char smraw[];
     XT* Xs = reinterpret_cast<XT*>(smraw);  // [r][mp]
     if (STAGED) {
-        for (int q = tid; q < n * mp; q += kProjNT) {
-            const int j = q / n, r = q - j * n;
-            Xs[(size_t)r * mp + j] = x_at<S, false>(nullptr, Xg, n, m, mp, r, j);
+        // asynchronous element copies (all in flight at once); the padding vectors j >= m are zero
+        const int warp = tid >> 5, lane = tid & 31;
+        for (int j = warp; j < mp; j += kProjNT / 32) {
+            for (int r = lane; r < n; r += 32) {
+                XT* dst = Xs + (size_t)r * mp + j;
+                if (j < m) cp_async_elem<sizeof(XT)>(dst, Xg + (size_t)j * n + r);  // Re, or (Re, Im)
+                else *dst = XT{};
+            }
         }
+        cp_async_wait_all();
         __syncthreads();
     }
     // ---- Y = H X: item (block of kProjVB vectors, row r); H(r, c) coalesced over r ----------------
@@ -101,22 +133,16 @@ __global__ void __launch_bounds__(kProjNT) k_refine_project(const typename Split
         dsacc     yr[kProjVB], yi[kProjVB];
 #pragma unroll
         for (int q = 0; q < kProjVB; ++q) yr[q] = yi[q] = dsacc{0.f, 0.f};
-        const int e0 = SPARSE ? sv.ptr[r] : 0, e1 = SPARSE ? sv.ptr[r + 1] : n;
-        for (int e = e0; e < e1; ++e) {
-            const int c = SPARSE ? sv.col[e] : e;
-            const SE  h = SPARSE ? sparse_elem<S>(sv, b, r, e) : A[(size_t)c * ld + r];
-#pragma unroll
-            for (int q = 0; q < kProjVB; ++q) {
-                const XT x = x_at<S, STAGED>(Xs, Xg, n, m, mp, c, j0 + q);
-                if constexpr (CX) {  // (hr + i hi)(xr + i xi)
-                    ds_add_prod(yr[q], h.rhi, h.rlo, x.x);
-                    ds_add_prod(yr[q], -h.ihi, -h.ilo, x.y);
-                    ds_add_prod(yi[q], h.rhi, h.rlo, x.y);
-                    ds_add_prod(yi[q], h.ihi, h.ilo, x.x);
-                } else {
-                    ds_add_prod(yr[q], h.hi, h.lo, x);
-                }
+        if constexpr (SPARSE) {
+            // the diagonal, then the off-diagonal slots (coalesced over r)
+            proj_accumulate<S, STAGED>(yr, yi, sparse_diag<S>(sv, b, r), Xs, Xg, n, m, mp, r, j0);
+#pragma unroll 4
+            for (int e = 0; e < sv.W; ++e) {
+                const size_t o = (size_t)e * sv.N + r;
+                proj_accumulate<S, STAGED>(yr, yi, sparse_slot<S>(sv, o), Xs, Xg, n, m, mp, sv.col[o], j0);
             }
+        } else {
+            for (int c = 0; c < n; ++c) proj_accumulate<S, STAGED>(yr, yi, A[(size_t)c * ld + r], Xs, Xg, n, m, mp, c, j0);
         }
 #pragma unroll
         for (int q = 0; q < kProjVB; ++q) {

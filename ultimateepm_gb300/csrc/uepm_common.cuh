@@ -204,6 +204,14 @@ __device__ __forceinline__ void ds_add_prod(dsacc& a, float x, float y) {
 }
 __device__ __forceinline__ double ds_value(dsacc a) { return (double)a.h + (double)a.l; }
 
+// cp.async of one naturally aligned element of B = 4 or 8 bytes, global -> shared
+template <int B>
+__device__ __forceinline__ void cp_async_elem(void* dst, const void* src) {
+    const unsigned sa = (unsigned)__cvta_generic_to_shared(dst);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], %2;\n" ::"r"(sa), "l"(src), "n"(B) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
+
 template <typename T>
 __device__ __forceinline__ T warp_sum(T v) {
 #pragma unroll

@@ -73,11 +73,14 @@ __host__ __device__ inline size_t refine_small_elems(int m, int) { return (size_
 // local potential only (sv.on), H is not formed: H X = V X + diag(kinetic) X from the resident CSR
 // of V (every row lists its diagonal, whose FP64 value V_ii + kinetic is split per k as the
 // assembly would), summed in the same column order, so Y is the same as from the dense pairs.
+// V without its diagonal in transposed ELL form: slot e of row r at [e * N + r], padded with zero
+// values (column r) to the widest row, so that threads on consecutive rows load consecutive words.
 struct SparseV {
     bool              on;
-    const int*        ptr;
-    const int*        col;
-    const ds4*        val;
+    int               W;     // slots per row
+    const int*        col;   // [W][N]
+    const float2*     re;    // [W][N] (hi, lo) of Re V
+    const float2*     im;    // [W][N] (hi, lo) of Im V
     const cx<double>* Vloc;  // N x N column-major, for the diagonal
     const double*     rows;  // [batch][N][ROW_STRIDE], for the kinetic term
     int               N;
