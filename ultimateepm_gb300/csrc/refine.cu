@@ -200,7 +200,8 @@ constexpr int kSmallWarps = 2;
 template <typename S>
 __host__ __device__ inline size_t small_eigh_lowdin_offset(int m) {
     const int me = (m + 1) & ~1;
-    return (sizeof(S) * 3 * (size_t)m * (m + 1) + sizeof(double) * 4 * (size_t)me + sizeof(int) * (size_t)me + 15) &
+    return (sizeof(S) * 3 * (size_t)m * (m + 1) + (sizeof(double) + sizeof(S)) * 2 * (size_t)me + sizeof(int) * (size_t)me +
+            15) &
            ~(size_t)15;
 }
 template <typename S>
@@ -225,10 +226,10 @@ __global__ void __launch_bounds__(32 * kSmallWarps) k_small_eigh(S* __restrict__
     S*  L    = reinterpret_cast<S*>(smraw + (size_t)warp * small_eigh_warp_bytes<S>(m));
     S*  Cm   = L + (size_t)m * mp;
     S*  V    = Cm + (size_t)m * mp;
-    R*  rc   = reinterpret_cast<R*>(V + (size_t)m * mp);  // per pair: cosine
-    R*  rs   = rc + me;                                   // sine
-    R*  rex  = rs + me;                                   // unit phase e of the off-diagonal (re, im)
-    R*  rey  = rex + me;
+    R*  rc   = reinterpret_cast<R*>(V + (size_t)m * mp);  // per pair: cosine c
+    R*  rs   = rc + me;                                   // sine s
+    S*  jp   = reinterpret_cast<S*>(rs + me);             // -s conj(e), e the unit phase of C_pq
+    S*  jq   = jp + me;                                   // c conj(e)
     if (b >= batch) return;
     S*       Sg  = small + (size_t)b * refine_small_elems(m, nb);
     const S* Ag  = Sg + (size_t)m * m;
@@ -246,14 +247,14 @@ __global__ void __launch_bounds__(32 * kSmallWarps) k_small_eigh(S* __restrict__
     // FP32 eigenvectors are orthonormal to ~1e-6, so S = I + E with a small E and, to first order,
     // S^-1/2 = I - E/2 (Loewdin): C = A - (E A + A E)/2 and W = (I - E/2) V, with an O(|E|^2 |A|)
     // error (~1e-11 eV at |E| = 1e-6). When some |E_ij| exceeds 1e-4 the Cholesky route runs instead.
-    R emax = 0;
+    R emax2 = 0;
     for (int q = lane; q < m * m; q += 32) {
         const int i = q / m, j = q - i * m;
         const S   e = (i == j) ? ST<S>::make(ST<S>::re(LL(i, j)) - 1.0, ST<S>::im(LL(i, j))) : LL(i, j);
-        emax        = fmax(emax, sqrt(ST<S>::norm(e)));
+        emax2       = fmax(emax2, ST<S>::norm(e));
     }
-    emax             = warp_max(emax);
-    const bool lowdin = emax <= 1e-4;
+    emax2             = warp_max(emax2);
+    const bool lowdin = emax2 <= 1e-8;  // max |E_ij| <= 1e-4
     if (lowdin) {
         // the correction (E A + A E) / 2 is ~|E| |A| ~ 1e-4 eV and needs ~1e-5 relative accuracy:
         // FP32 products (on copies converted once), subtracted from A in FP64
@@ -342,7 +343,8 @@ __global__ void __launch_bounds__(32 * kSmallWarps) k_small_eigh(S* __restrict__
     // Pairs below the stopping threshold are not rotated, and a round with no pair above it is
     // skipped: once the nearly diagonal C has converged, the final sweep costs only its checks.
     const int npair = me / 2;
-    int*      pp    = reinterpret_cast<int*>(rey + me);  // pair table of the round: p, q
+    const int nblk  = npair * (npair + 1) / 2;           // 2 x 2 blocks (k, l), k <= l, of C
+    int*      pp    = reinterpret_cast<int*>(jq + me);  // pair table of the round: p, q
     int*      pq    = pp + npair;
     for (int sweep = 0; sweep < 12; ++sweep) {
         R off2 = 0, dia = 0;
@@ -393,46 +395,58 @@ __global__ void __launch_bounds__(32 * kSmallWarps) k_small_eigh(S* __restrict__
                         }
                     }
                 }
-                pp[lane]  = p;
-                pq[lane]  = q;
-                rc[lane]  = cc;
-                rs[lane]  = ss;
-                rex[lane] = ex;
-                rey[lane] = ey;
+                pp[lane] = p;
+                pq[lane] = q;
+                rc[lane] = cc;
+                rs[lane] = ss;
+                jp[lane] = ST<S>::make(-ss * ex, ss * ey);
+                jq[lane] = ST<S>::make(cc * ex, -cc * ey);
             }
             if (!__any_sync(0xffffffffu, act)) continue;  // warp-uniform: nothing to rotate
             __syncwarp();
-            // columns: C <- C J, V <- V J  (work items: pair x row)
-            for (int it = lane; it < npair * m; it += 32) {
-                const int k = it / m, r = it - k * m;
-                const R   c = rc[k], s = rs[k];
-                if (s == 0.0) continue;
-                const int p = pp[k], q = pq[k];
-                const R   ex = rex[k], ey = rey[k];
-                const S   jqp = ST<S>::make(-s * ex, s * ey);
-                const S   jqq = ST<S>::make(c * ex, -c * ey);
-                const S   cp = CC(r, p), cq = CC(r, q);
-                CC(r, p) = cfma(cq, jqp, cscale(cp, c));
-                CC(r, q) = cfma(cq, jqq, cscale(cp, s));
-                if (want_w) {  // the accumulated rotations only matter for the Ritz vectors
-                    const S vp = VV(r, p), vq = VV(r, q);
-                    VV(r, p) = cfma(vq, jqp, cscale(vp, c));
-                    VV(r, q) = cfma(vq, jqq, cscale(vp, s));
+            // V <- V J, the accumulated rotations (only needed for the Ritz vectors)
+            if (want_w) {
+                for (int it = lane; it < npair * m; it += 32) {
+                    const int k = it / m, r = it - k * m;
+                    const R   c = rc[k], sn = rs[k];
+                    if (sn == 0.0) continue;
+                    const int p = pp[k], q = pq[k];
+                    const S   vp = VV(r, p), vq = VV(r, q);
+                    VV(r, p) = cfma(vq, jp[k], cscale(vp, c));
+                    VV(r, q) = cfma(vq, jq[k], cscale(vp, sn));
                 }
             }
-            __syncwarp();
-            // rows: C <- J^H C
-            for (int it = lane; it < npair * m; it += 32) {
-                const int k = it / m, r = it - k * m;
-                const R   c = rc[k], s = rs[k];
-                if (s == 0.0) continue;
-                const int p = pp[k], q = pq[k];
-                const R   ex = rex[k], ey = rey[k];
-                const S   jqp = ST<S>::make(-s * ex, s * ey);
-                const S   jqq = ST<S>::make(c * ex, -c * ey);
-                const S   cp = CC(p, r), cq = CC(q, r);
-                CC(p, r) = cfma(ST<S>::conj(jqp), cq, cscale(cp, c));
-                CC(q, r) = cfma(ST<S>::conj(jqq), cq, cscale(cp, s));
+            // C <- J^H C J in 2 x 2 blocks: rows of pair k, columns of pair l, one block per lane,
+            // k <= l computed and the block below the diagonal mirrored (C stays exactly Hermitian),
+            // so each off-diagonal pair of entries costs one two-sided rotation
+            for (int it = lane; it < nblk; it += 32) {
+                int k = 0, rem = it;
+                while (rem >= npair - k) {
+                    rem -= npair - k;
+                    ++k;
+                }
+                const int l = k + rem;
+                if (rs[k] == 0.0 && rs[l] == 0.0) continue;  // both rotations are the identity
+                const int  pk = pp[k], qk = pq[k], pl = pp[l], ql = pq[l];
+                const bool hk = qk < m, hl = ql < m;  // q = m is the bye of an odd m
+                const S    b00 = CC(pk, pl), b01 = hl ? CC(pk, ql) : ST<S>::zero();
+                const S    b10 = hk ? CC(qk, pl) : ST<S>::zero(), b11 = (hk && hl) ? CC(qk, ql) : ST<S>::zero();
+                const R    cl = rc[l], sl = rs[l], ck = rc[k], sk = rs[k];
+                const S    jpl = jp[l], jql = jq[l], jpk = ST<S>::conj(jp[k]), jqk = ST<S>::conj(jq[k]);
+                const S    t00 = cfma(b01, jpl, cscale(b00, cl)), t01 = cfma(b01, jql, cscale(b00, sl));
+                const S    t10 = cfma(b11, jpl, cscale(b10, cl)), t11 = cfma(b11, jql, cscale(b10, sl));
+                const S    n00 = cfma(jpk, t10, cscale(t00, ck)), n01 = cfma(jpk, t11, cscale(t01, ck));
+                const S    n10 = cfma(jqk, t10, cscale(t00, sk)), n11 = cfma(jqk, t11, cscale(t01, sk));
+                CC(pk, pl) = n00;
+                if (hl) CC(pk, ql) = n01;
+                if (hk) CC(qk, pl) = n10;
+                if (hk && hl) CC(qk, ql) = n11;
+                if (k != l) {
+                    CC(pl, pk) = ST<S>::conj(n00);
+                    if (hl) CC(ql, pk) = ST<S>::conj(n01);
+                    if (hk) CC(pl, qk) = ST<S>::conj(n10);
+                    if (hk && hl) CC(ql, qk) = ST<S>::conj(n11);
+                }
             }
             __syncwarp();
             if (lane < npair && rs[lane] != 0.0) {  // Hermitian diagonal stays real
@@ -443,20 +457,23 @@ __global__ void __launch_bounds__(32 * kSmallWarps) k_small_eigh(S* __restrict__
             __syncwarp();
         }
     }
-    // ascending order of the Ritz values (lane 0), nb smallest out
-    int* ord = reinterpret_cast<int*>(rc);  // reuse: 4 me doubles hold m ints
-    if (lane == 0) {
-        for (int i = 0; i < m; ++i) ord[i] = i;
-        for (int i = 1; i < m; ++i) {
-            const int o = ord[i];
-            const R   ev = ST<S>::re(CC(o, o));
-            int       k  = i - 1;
-            while (k >= 0 && ST<S>::re(CC(ord[k], ord[k])) > ev) {
-                ord[k + 1] = ord[k];
-                --k;
-            }
-            ord[k + 1] = o;
+    // ascending order of the Ritz values, nb smallest out: the rank of each value among all (ties
+    // by index, i.e. a stable sort) from integer keys that order as the doubles do (-0 as +0)
+    long long* key = reinterpret_cast<long long*>(rc);  // reuse: me doubles hold m keys
+    int*       ord = reinterpret_cast<int*>(jp);
+    for (int i = lane; i < m; i += 32) {
+        const long long v = __double_as_longlong(ST<S>::re(CC(i, i)) + 0.0);
+        key[i]            = v >= 0 ? v : v ^ 0x7fffffffffffffffLL;
+    }
+    __syncwarp();
+    for (int i = lane; i < m; i += 32) {
+        const long long ki = key[i];
+        int             rk = 0;
+        for (int j = 0; j < m; ++j) {
+            const long long kj = key[j];
+            rk += (kj < ki) || (kj == ki && j < i);
         }
+        ord[rk] = i;
     }
     __syncwarp();
     for (int j = lane; j < nb; j += 32) {
