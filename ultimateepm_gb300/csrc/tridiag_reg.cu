@@ -6,22 +6,22 @@
 // (the first half of Eigen's SelfAdjointEigenSolver behind Hamiltonian::Diagonalize,
 // src/EPP/Hamiltonian.cpp:125-134).
 //
-// Layout. The 256 threads form a 16 x 16 grid; thread (r, c) owns A[r + 16t][c + 16u] for
-// t, u < K = ceil(n / 16) in registers (2-D cyclic distribution: the trailing matrix of every step
-// stays spread over all threads). Shared memory holds only the current column (double-buffered) and
-// the product vector y, so each step is
-//   (a) every thread computes the Householder scalars of column j from the shared column and the
-//       norm partials published with it (identical arithmetic everywhere, no barrier); warp 0
-//       writes d, e, tau and the reflector tail;
-//   (b) p = A v: K x K FMAs per thread, a 16-lane butterfly per row, y and the warp partials of
-//       v^T p to shared memory;                                             -- barrier
-//   (c) w = tau p - (tau^2 / 2)(v^T p) v, A -= v w^T + w v^T on the registers; the owners of column
-//       j + 1 publish it, with the partial sums of squares of its tail.     -- barrier
-// (Working with the unnormalised reflector x - beta e_{j+1} and tau' = 1 / (beta (beta - alpha))
-// saves the scaling of v but measured slower and less accurate on the 2000-point Si path.)
-// Rows and columns that are already reduced (index <= j) are skipped at compile time: the steps are
-// run in blocks of 16 with the first live local index S0 = floor((j + 1) / 16) as a template
-// parameter, so the unrolled loops start at S0 and no register array is indexed at run time.
+// Layout. The 256 threads form a 16 x 16 grid, thread (r, c) = (tid % 16, tid / 16), and own
+// A[r + 16t][c + 16u] for t, u < K = ceil(n / 16) in registers (2-D cyclic distribution: the
+// trailing matrix of every step stays spread over all threads). Rows are the fast index, so the 16
+// owners of a column are one half-warp, and the 16 threads that share a column group reduce over
+// rows within their half-warp. Shared memory holds the reflector v (double-buffered by step
+// parity) and y = tau A v, both transposed ([q][t] = element q + 16t, so a thread's rows or
+// columns are contiguous float4s), and a per-half-warp buffer for the column sums. Step j:
+//   (a) product: y = tau A v as column sums (A is symmetric): each thread sums its rows for each of
+//       its columns, the 16 partials of a column meet in the half-warp's buffer and lane u adds
+//       those of column c + 16u; the warps' partials of v^T y go to shared memory.  -- barrier
+//   (b) w = y - (tau/2)(v^T y) v and A -= v w^T + w v^T on the registers; the half-warp that owns
+//       column j + 1 then forms its reflector (norm by shuffles, the Householder scalars, v scaled)
+//       and publishes v, tau, d, e and the reflector tail.                         -- barrier
+// Rows and columns that are already reduced (index <= j) are skipped at compile time: the steps run
+// in blocks of 16 with the first live local index S0 = floor((j + 1) / 16) as a template parameter,
+// so the unrolled loops start at S0 and no register array is indexed at run time.
 #include <algorithm>
 
 #include "uepm_common.cuh"
@@ -30,180 +30,208 @@
 namespace uepm {
 namespace {
 
-constexpr int kGrid = 16;               // thread grid kGrid x kGrid
-constexpr int kThreads = kGrid * kGrid;  // 256
-constexpr int kWarps = kThreads / 32;
+constexpr int kGrid    = 16;              // thread grid kGrid x kGrid
+constexpr int kThreads = kGrid * kGrid;   // 256
+constexpr int kWarps   = kThreads / 32;
+constexpr int kKP      = 12;              // row length of the transposed vectors (K <= 11; 48 B rows
+                                          // keep 8 consecutive float4 rows on distinct banks)
+constexpr int kPP      = 20;              // row pitch of the column-sum buffer (conflict-free float4 rows)
+constexpr int kPartW   = kGrid * kPP + 16;  // per half-warp (the +16 puts the two halves of a warp on
+                                            // different banks)
 
-template <int K>
 struct RegShared {
-    float               col[2][kGrid * K];  // column j (buffer j & 1), zero beyond n
-    __align__(16) float nrm[2][kGrid];      // per-row-group partial sums of squares of col[j+2:]
-    float               y[kGrid * K];       // p = A v of the current step, zero for rows <= j
-    __align__(16) float red[kWarps];        // per-warp partials of v^T p
+    __align__(16) float v[2][kGrid][kKP];  // v[b][q][t] = v_{q + 16t} of the step with parity b
+    __align__(16) float y[kGrid][kKP];     // y[q][t] = (tau A v)_{q + 16t}, zero at reduced indices
+    __align__(16) float part[kGrid][kPartW];  // [c][u * kPP + r]: row group r's sum for column c + 16u
+    __align__(16) float red[kWarps];       // per-warp partials of v^T y
+    float               tau[2];
 };
 
-// Sum of 16 shared partials in a fixed order (identical in every thread).
-__device__ __forceinline__ float sum16(const float* p) {
-    const float4 a = reinterpret_cast<const float4*>(p)[0], b = reinterpret_cast<const float4*>(p)[1];
-    const float4 c = reinterpret_cast<const float4*>(p)[2], d = reinterpret_cast<const float4*>(p)[3];
-    return (((a.x + a.y) + (a.z + a.w)) + ((b.x + b.y) + (b.z + b.w))) +
-           (((c.x + c.y) + (c.z + c.w)) + ((d.x + d.y) + (d.z + d.w)));
+// Loads row q, entries [S0, K), of a transposed vector (compile-time chunks of four).
+template <int K, int S0>
+__device__ __forceinline__ void load_row(const float (&src)[kKP], float (&dst)[K]) {
+#pragma unroll
+    for (int t4 = S0 / 4; t4 <= (K - 1) / 4; ++t4) {
+        const float4 q = *reinterpret_cast<const float4*>(&src[4 * t4]);
+        if (4 * t4 + 0 >= S0 && 4 * t4 + 0 < K) dst[4 * t4 + 0] = q.x;
+        if (4 * t4 + 1 >= S0 && 4 * t4 + 1 < K) dst[4 * t4 + 1] = q.y;
+        if (4 * t4 + 2 >= S0 && 4 * t4 + 2 < K) dst[4 * t4 + 2] = q.z;
+        if (4 * t4 + 3 >= S0 && 4 * t4 + 3 < K) dst[4 * t4 + 3] = q.w;
+    }
 }
 
-// Householder vector element i of step j: v[j+1] = 1, v[i] = col[i] * sc below, 0 above.
-__device__ __forceinline__ float house_v(const float* col, int i, int j, float sc) {
-    return i > j + 1 ? col[i] * sc : (i == j + 1 ? 1.f : 0.f);
+// The reflector of column jn (local column S0 of the half-warp c = jn % 16), from its registers:
+// alpha = A[jn+1][jn], the tail A[jn+2:][jn]; v = (1, tail / (alpha - beta)) from row jn + 1 on.
+// Runs in the whole warp that holds the owners (the shuffles use all 32 lanes; the other half-warp
+// computes on its own column and stores nothing). For jn = n - 1 only d is written.
+template <int K, int S0>
+__device__ __forceinline__ void house_next(const float (&a)[K][K], RegShared& sh, int jn, int n, int r, int c,
+                                           float* __restrict__ Ag, int ld, float* __restrict__ dOut,
+                                           float* __restrict__ eOut, float* __restrict__ tqOut, bool& bad) {
+    const bool own = c == (jn & (kGrid - 1));
+    float      ss = 0.f, al = 0.f, dj = 0.f;
+#pragma unroll
+    for (int t = S0; t < K; ++t) {
+        const int   row = r + kGrid * t;
+        const float x   = a[t][S0];
+        if (row >= jn + 2) ss = fmaf(x, x, ss);
+        if (row == jn + 1) al = x;
+        if (row == jn) dj = x;
+    }
+    if (own && r == (jn & (kGrid - 1))) {
+        dOut[jn] = dj;
+        if (!isfinite(dj)) bad = true;
+    }
+    if (jn >= n - 1) {
+        if (own && r == 0) {
+            eOut[jn]  = 0.f;
+            tqOut[jn] = 0.f;
+        }
+        return;
+    }
+#pragma unroll
+    for (int o = 1; o < kGrid; o <<= 1) ss += __shfl_xor_sync(0xffffffffu, ss, o);
+    const float alpha = __shfl_sync(0xffffffffu, al, (jn + 1) & (kGrid - 1), kGrid);
+    // The divisions stay correctly rounded: with the approximate forms the biased tau of 136
+    // successive reflectors lost enough orthogonality to move the refined eigenvalues of the
+    // 2000-point Si path by 1e-5 eV.
+    float beta = alpha, tau = 0.f, sc = 0.f;
+    if (ss > num<float>::tiny()) {
+        beta = sqrtf(fmaf(alpha, alpha, ss));
+        if (alpha >= 0.f) beta = -beta;
+        tau = (beta - alpha) / beta;
+        sc  = 1.f / (alpha - beta);
+    }
+    if (!own) return;
+    float* vq = sh.v[jn & 1][r];
+    float* cg = Ag + (size_t)jn * ld;
+#pragma unroll
+    for (int t = S0; t < K; ++t) {
+        const int   row = r + kGrid * t;
+        const float x   = a[t][S0] * sc;
+        vq[t]           = row > jn + 1 ? x : (row == jn + 1 ? 1.f : 0.f);
+        if (row > jn + 1 && row < n) cg[row] = x;
+    }
+    if (r == ((jn + 1) & (kGrid - 1))) cg[jn + 1] = beta;
+    if (r == 0) {
+        eOut[jn]        = beta;
+        tqOut[jn]       = tau;
+        sh.tau[jn & 1]  = tau;
+        if (!isfinite(beta)) bad = true;
+    }
 }
 
 template <int K, int S0>
-__device__ __forceinline__ void reduce_block(float (&a)[K][K], RegShared<K>& sh, float* __restrict__ Ag, int n, int ld,
+__device__ __forceinline__ void reduce_block(float (&a)[K][K], RegShared& sh, float* __restrict__ Ag, int n, int ld,
                                              float* __restrict__ dOut, float* __restrict__ eOut,
                                              float* __restrict__ tqOut, bool& bad) {
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const int r = tid >> 4, c = tid & 15;
+    const int r = tid & (kGrid - 1), c = tid >> 4;
     const int jlo = max(kGrid * S0 - 1, 0), jhi = min(kGrid * S0 + kGrid - 2, n - 2);
     for (int j = jlo; j <= jhi; ++j) {
-        const float* col = sh.col[j & 1];
-        // ---- (a) Householder scalars of column j (every thread, same order of operations) ------
-        // The column's owners published the partial sums of squares of its tail with it. The
-        // divisions stay correctly rounded: with the approximate forms the biased tau of 136
-        // successive reflectors lost enough orthogonality to move the refined eigenvalues of the
-        // 2000-point Si path by 1e-5 eV.
-        const float tail2 = sum16(sh.nrm[j & 1]);
-        const float alpha = col[j + 1];
-        float       beta = alpha, tau = 0.f, sc = 0.f;
-        if (tail2 > num<float>::tiny()) {
-            beta = sqrtf(fmaf(alpha, alpha, tail2));
-            if (alpha >= 0.f) beta = -beta;
-            tau = (beta - alpha) / beta;
-            sc  = 1.f / (alpha - beta);
-        }
-        if (warp == 0) {
-            float* cg = Ag + (size_t)j * ld;
-            for (int i = j + 2 + lane; i < n; i += 32) cg[i] = col[i] * sc;
-            if (lane == 0) {
-                const float dj = col[j];
-                dOut[j]   = dj;
-                eOut[j]   = beta;
-                tqOut[j]  = tau;
-                cg[j + 1] = beta;
-                if (!isfinite(beta) || !isfinite(dj)) bad = true;
-            }
-        }
+        const int   b   = j & 1;
+        const float tau = sh.tau[b];
         if (tau != 0.f) {  // uniform over the CTA
-            float vc[K];
+            // ---- (a) column sums of A v over this thread's rows -----------------------------------
+            float vr[K], q[K];
+            load_row<K, S0>(sh.v[b][r], vr);
 #pragma unroll
-            for (int u = S0; u < K; ++u) vc[u] = house_v(col, c + kGrid * u, j, sc);
-            // ---- (b) p = A v, reduced over the 16 column owners of each row ---------------------
-            float p[K];
-#pragma unroll
-            for (int t = S0; t < K; ++t) {
+            for (int u = S0; u < K; ++u) {
                 float s = 0.f;
 #pragma unroll
-                for (int u = S0; u < K; ++u) s = fmaf(a[t][u], vc[u], s);
-                p[t] = s;
+                for (int t = S0; t < K; ++t) s = fmaf(a[t][u], vr[t], s);
+                q[u] = s;
             }
+            // sum over the 16 row groups of the half-warp: lane u ends with column c + 16u
+            float ysum = 0.f;
+            if constexpr (K - S0 <= 3) {
 #pragma unroll
-            for (int off = 1; off < kGrid; off <<= 1) {
+                for (int o = 1; o < kGrid; o <<= 1) {
 #pragma unroll
-                for (int t = S0; t < K; ++t) p[t] += __shfl_xor_sync(0xffffffffu, p[t], off);
+                    for (int u = S0; u < K; ++u) q[u] += __shfl_xor_sync(0xffffffffu, q[u], o);
+                }
+#pragma unroll
+                for (int u = S0; u < K; ++u)
+                    if (r == u) ysum = q[u];
+            } else {
+                float* pc = sh.part[c];
+#pragma unroll
+                for (int u = S0; u < K; ++u) pc[u * kPP + r] = q[u];
+                __syncwarp();
+                if (r >= S0 && r < K) {
+                    const float4* pr = reinterpret_cast<const float4*>(pc + r * kPP);
+                    const float4  p0 = pr[0], p1 = pr[1], p2 = pr[2], p3 = pr[3];
+                    ysum = (((p0.x + p0.y) + (p0.z + p0.w)) + ((p1.x + p1.y) + (p1.z + p1.w))) +
+                           (((p2.x + p2.y) + (p2.z + p2.w)) + ((p3.x + p3.y) + (p3.z + p3.w)));
+                }
             }
-            // every lane of the half-warp now holds p for rows r + 16t: v^T p over them (v is zero on
-            // the reduced rows), both halves combined; lane c publishes row r + 16c
-            float vtp = 0.f, mine = 0.f;
-#pragma unroll
-            for (int t = S0; t < K; ++t) {
-                vtp = fmaf(house_v(col, r + kGrid * t, j, sc), p[t], vtp);
-                if (c == t) mine = p[t];
+            float vty = 0.f;
+            if (r >= S0 && r < K) {
+                const int   i  = c + kGrid * r;
+                const float yv = i > j ? tau * ysum : 0.f;
+                sh.y[c][r]     = yv;
+                vty            = sh.v[b][c][r] * yv;
             }
-            vtp += __shfl_xor_sync(0xffffffffu, vtp, kGrid);
-            const int im = r + kGrid * c;
-            if (lane == 0) sh.red[warp] = vtp;
-            if (c >= S0 && c < K) sh.y[im] = im > j ? mine : 0.f;
+            vty = warp_sum(vty);
+            if (lane == 0) sh.red[warp] = vty;
         }
         __syncthreads();
         if (tau != 0.f) {
-            // ---- (c) rank-2 update on the registers ---------------------------------------------
+            // ---- (b) rank-2 update on the registers ---------------------------------------------
             const float4 r0 = reinterpret_cast<const float4*>(sh.red)[0], r1 = reinterpret_cast<const float4*>(sh.red)[1];
-            const float  vtp = ((r0.x + r0.y) + (r0.z + r0.w)) + ((r1.x + r1.y) + (r1.z + r1.w));
-            const float  al  = -0.5f * tau * tau * vtp;
-            float       vc[K], wc[K];
+            const float  vty = ((r0.x + r0.y) + (r0.z + r0.w)) + ((r1.x + r1.y) + (r1.z + r1.w));
+            const float  al  = -0.5f * tau * vty;
+            float        vc[K], wc[K], vr[K], wr[K];
+            load_row<K, S0>(sh.v[b][c], vc);
+            load_row<K, S0>(sh.y[c], wc);
+            load_row<K, S0>(sh.v[b][r], vr);
+            load_row<K, S0>(sh.y[r], wr);
 #pragma unroll
-            for (int u = S0; u < K; ++u) {
-                const int i = c + kGrid * u;
-                vc[u]       = house_v(col, i, j, sc);
-                wc[u]       = fmaf(tau, sh.y[i], al * vc[u]);
-            }
-#pragma unroll
-            for (int t = S0; t < K; ++t) {
-                const int   i  = r + kGrid * t;
-                const float vr = house_v(col, i, j, sc);
-                const float wr = fmaf(tau, sh.y[i], al * vr);
-#pragma unroll
-                for (int u = S0; u < K; ++u) a[t][u] = fmaf(-vr, wc[u], fmaf(-wr, vc[u], a[t][u]));
-            }
-        }
-        // column j + 1 (local column S0 of the owners) for the next step, with the partial sums of
-        // squares of its tail (rows >= j + 3)
-        if (c == ((j + 1) & (kGrid - 1))) {
-            float* nxt = sh.col[(j + 1) & 1];
-            float  ss  = 0.f;
+            for (int u = S0; u < K; ++u) wc[u] = fmaf(al, vc[u], wc[u]);
 #pragma unroll
             for (int t = S0; t < K; ++t) {
-                const float x = a[t][S0];
-                nxt[r + kGrid * t] = x;
-                if (r + kGrid * t >= j + 3) ss = fmaf(x, x, ss);
+                const float w = fmaf(al, vr[t], wr[t]);
+#pragma unroll
+                for (int u = S0; u < K; ++u) a[t][u] = fmaf(-vr[t], wc[u], fmaf(-w, vc[u], a[t][u]));
             }
-            sh.nrm[(j + 1) & 1][r] = ss;
         }
+        // ---- the reflector of column j + 1 (local column S0 of its owners) ----------------------
+        if (warp == (((j + 1) & (kGrid - 1)) >> 1)) house_next<K, S0>(a, sh, j + 1, n, r, c, Ag, ld, dOut, eOut, tqOut, bad);
         __syncthreads();
     }
-    if constexpr (S0 + 1 < K) reduce_block<K, S0 + 1>(a, sh, Ag, n, ld, dOut, eOut, tqOut, bad);
+    if constexpr (S0 + 1 < K) {
+        if (kGrid * (S0 + 1) - 1 <= n - 2) reduce_block<K, S0 + 1>(a, sh, Ag, n, ld, dOut, eOut, tqOut, bad);
+    }
 }
 
 template <int K>
 __global__ void __launch_bounds__(kThreads, K <= 9 ? 2 : 1)
     k_tridiag_reg(float* __restrict__ H, int n, int ld, size_t mstride, float* __restrict__ dOut,
                   float* __restrict__ eOut, float* __restrict__ tqOut, int* __restrict__ status, int batch) {
-    __shared__ RegShared<K> sh;
-    const int tid = threadIdx.x, r = tid >> 4, c = tid & 15;
+    __shared__ RegShared sh;
+    const int tid = threadIdx.x, r = tid & (kGrid - 1), c = tid >> 4;
     for (int b = blockIdx.x; b < batch; b += gridDim.x) {
         float* Ag = H + (size_t)b * mstride;
         float  a[K][K];
-        // a[t][u] = A[r+16t][c+16u], read as the (c+16u, r+16t) element of the column-major,
-        // exactly symmetric matrix so that consecutive lanes read consecutive addresses
+        // a[t][u] = A[r+16t][c+16u] (column-major: consecutive lanes read consecutive rows)
 #pragma unroll
         for (int t = 0; t < K; ++t) {
             const int i = r + kGrid * t;
 #pragma unroll
             for (int u = 0; u < K; ++u) {
                 const int jj = c + kGrid * u;
-                a[t][u]      = (i < n && jj < n) ? Ag[(size_t)i * ld + jj] : 0.f;
+                a[t][u]      = (i < n && jj < n) ? Ag[(size_t)jj * ld + i] : 0.f;
             }
         }
-        for (int i = tid; i < kGrid * K; i += kThreads) {
-            sh.col[0][i] = i < n ? Ag[i] : 0.f;
-            sh.col[1][i] = 0.f;
-        }
-        if (c == 0) {  // owners of column 0: partial sums of squares of its tail (rows >= 2)
-            float ss = 0.f;
-#pragma unroll
-            for (int t = 0; t < K; ++t)
-                if (r + kGrid * t >= 2) ss = fmaf(a[t][0], a[t][0], ss);
-            sh.nrm[0][r] = ss;
-        }
+        bool   bad = false;
+        float* dB  = dOut + (size_t)b * n;
+        float* eB  = eOut + (size_t)b * n;
+        float* tB  = tqOut + (size_t)b * n;
+        if (tid < 32) house_next<K, 0>(a, sh, 0, n, r, c, Ag, ld, dB, eB, tB, bad);  // column 0: warp 0
         __syncthreads();
-        bool bad = false;
-        reduce_block<K, 0>(a, sh, Ag, n, ld, dOut + (size_t)b * n, eOut + (size_t)b * n, tqOut + (size_t)b * n, bad);
-        if (tid == 0) {
-            const float dl = sh.col[(n - 1) & 1][n - 1];
-            dOut[(size_t)b * n + n - 1]  = dl;
-            eOut[(size_t)b * n + n - 1]  = 0.f;
-            tqOut[(size_t)b * n + n - 1] = 0.f;
-            if (!isfinite(dl)) bad = true;
-            if (bad && status) atomicOr(status + b, 2);  // UEPM_K_NONFINITE
-        }
-        __syncthreads();  // shared memory is reused by the CTA's next matrix
+        if (n >= 2) reduce_block<K, 0>(a, sh, Ag, n, ld, dB, eB, tB, bad);
+        bad = __syncthreads_or(bad);
+        if (tid == 0 && bad && status) atomicOr(status + b, 2);  // UEPM_K_NONFINITE
     }
 }
 
