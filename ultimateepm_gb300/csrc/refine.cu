@@ -206,7 +206,7 @@ __host__ __device__ inline size_t small_eigh_lowdin_offset(int m) {
 }
 template <typename S>
 __host__ __device__ inline size_t small_eigh_warp_bytes(int m) {
-    return (small_eigh_lowdin_offset<S>(m) + sizeof(typename Lower<S>::type) * 2 * (size_t)m * m + 15) & ~(size_t)15;
+    return (small_eigh_lowdin_offset<S>(m) + sizeof(typename Lower<S>::type) * 3 * (size_t)m * m + 15) & ~(size_t)15;
 }
 
 __device__ __forceinline__ float to_lower(double v) { return (float)v; }
@@ -244,10 +244,18 @@ __global__ void __launch_bounds__(32 * kSmallWarps) k_small_eigh(S* __restrict__
         VV(i, j)    = Ag[q];  // A, overwritten below
     }
     __syncwarp();
-    // FP32 eigenvectors are orthonormal to ~1e-6, so S = I + E with a small E and, to first order,
-    // S^-1/2 = I - E/2 (Loewdin): C = A - (E A + A E)/2 and W = (I - E/2) V, with an O(|E|^2 |A|)
-    // error (~1e-11 eV at |E| = 1e-6). When some |E_ij| exceeds 1e-4 the Cholesky route runs instead.
-    R emax2 = 0;
+    // FP32 eigenvectors are nearly orthonormal, so S = I + E with a small E (|E| up to ~1e-4 for
+    // close eigenvalues just outside the inverse iteration's clusters) and, to second order,
+    // S^-1/2 = I + F, F = -E/2 + 3E^2/8 (Loewdin):
+    //   C = (I + F) A (I + F) = A - (G + G^H)/2 + 3/8 (P + P^H) + E G^H / 4 + O(|E|^3 |A|),
+    //   G = E A, P = E G,     and W = (I + F) V,
+    // an error of ~1e-11 eV at |E| = 1e-4 (the first-order form left ~|E|^2 |A| ~ 1e-7 eV). When some
+    // |E_ij| exceeds 1e-4 the Cholesky route runs instead.
+    using F = typename Lower<S>::type;
+    F* Ef   = reinterpret_cast<F*>(smraw + (size_t)warp * small_eigh_warp_bytes<S>(m) + small_eigh_lowdin_offset<S>(m));
+    F* Af   = Ef + (size_t)m * m;  // A, then P
+    F* Gf   = Af + (size_t)m * m;  // G, then E V for the vectors
+    R  emax2 = 0;
     for (int q = lane; q < m * m; q += 32) {
         const int i = q / m, j = q - i * m;
         const S   e = (i == j) ? ST<S>::make(ST<S>::re(LL(i, j)) - 1.0, ST<S>::im(LL(i, j))) : LL(i, j);
@@ -256,11 +264,8 @@ __global__ void __launch_bounds__(32 * kSmallWarps) k_small_eigh(S* __restrict__
     emax2             = warp_max(emax2);
     const bool lowdin = emax2 <= 1e-8;  // max |E_ij| <= 1e-4
     if (lowdin) {
-        // the correction (E A + A E) / 2 is ~|E| |A| ~ 1e-4 eV and needs ~1e-5 relative accuracy:
-        // FP32 products (on copies converted once), subtracted from A in FP64
-        using F = typename Lower<S>::type;
-        F* Ef   = reinterpret_cast<F*>(smraw + (size_t)warp * small_eigh_warp_bytes<S>(m) + small_eigh_lowdin_offset<S>(m));
-        F* Af   = Ef + (size_t)m * m;
+        // the corrections are ~|E| |A| ~ 1e-3 eV and need ~1e-6 relative accuracy: FP32 products
+        // (on copies converted once), added to A in FP64
         for (int q = lane; q < m * m; q += 32) {
             const int i = q / m, c = q - i * m;
             const S   e = (i == c) ? ST<S>::make(ST<S>::re(LL(i, c)) - 1.0, ST<S>::im(LL(i, c))) : LL(i, c);
@@ -268,14 +273,28 @@ __global__ void __launch_bounds__(32 * kSmallWarps) k_small_eigh(S* __restrict__
             Af[q]       = to_lower(VV(i, c));
         }
         __syncwarp();
-        for (int q = lane; q < m * m; q += 32) {
+        for (int q = lane; q < m * m; q += 32) {  // G = E A
             const int i = q / m, c = q - i * m;
             F         acc = ST<F>::zero();
-            for (int j = 0; j < m; ++j) {
-                acc = cfma(Ef[i * m + j], Af[j * m + c], acc);
-                acc = cfma(Af[i * m + j], Ef[j * m + c], acc);
-            }
-            CC(i, c) = cfma(from_lower(acc), ST<S>::make(-0.5, 0.0), VV(i, c));
+            for (int j = 0; j < m; ++j) acc = cfma(Ef[i * m + j], Af[j * m + c], acc);
+            Gf[q] = acc;
+        }
+        __syncwarp();
+        for (int q = lane; q < m * m; q += 32) {  // P = E G, over A
+            const int i = q / m, c = q - i * m;
+            F         acc = ST<F>::zero();
+            for (int j = 0; j < m; ++j) acc = cfma(Ef[i * m + j], Gf[j * m + c], acc);
+            Af[q] = acc;
+        }
+        __syncwarp();
+        for (int q = lane; q < m * m; q += 32) {
+            const int i = q / m, c = q - i * m;
+            F         egh = ST<F>::zero();  // (E G^H)_ic
+            for (int j = 0; j < m; ++j) egh = cfma(Ef[i * m + j], ST<F>::conj(Gf[c * m + j]), egh);
+            const F g1 = cadd(Gf[i * m + c], ST<F>::conj(Gf[c * m + i]));
+            const F p2 = cadd(Af[i * m + c], ST<F>::conj(Af[c * m + i]));
+            const F corr = cfma(g1, ST<F>::make(-0.5f, 0.f), cfma(p2, ST<F>::make(0.375f, 0.f), cscale(egh, 0.25f)));
+            CC(i, c) = cadd(VV(i, c), from_lower(corr));
         }
         __syncwarp();
         for (int q = lane; q < m * m; q += 32) {
@@ -483,15 +502,26 @@ __global__ void __launch_bounds__(32 * kSmallWarps) k_small_eigh(S* __restrict__
     }
     // W = (I - E/2) V[:, ord[:nb]] (Loewdin) or L^-H V[:, ord[:nb]] (Cholesky)
     if (want_w && lowdin) {
+        // W = V - E V / 2 (FP64) + 3/8 E (E V) (FP32, ~|E|^2)
+        for (int q = lane; q < m * nb; q += 32) {
+            const int i = q / nb, c = q - i * nb;
+            const int oc = ord[c];
+            F         acc = ST<F>::zero();
+            for (int j = 0; j < m; ++j) acc = cfma(Ef[i * m + j], to_lower(VV(j, oc)), acc);
+            Gf[q] = acc;
+        }
+        __syncwarp();
         for (int q = lane; q < m * nb; q += 32) {
             const int i = q / nb, c = q - i * nb;
             const int oc = ord[c];
             S         acc = ST<S>::zero();
+            F         ac2 = ST<F>::zero();
             for (int j = 0; j < m; ++j) {
                 const S eij = (i == j) ? ST<S>::make(ST<S>::re(LL(i, j)) - 1.0, ST<S>::im(LL(i, j))) : LL(i, j);
                 acc         = cfma(eij, VV(j, oc), acc);
+                ac2         = cfma(Ef[i * m + j], Gf[j * nb + c], ac2);
             }
-            Wg[(size_t)i * nb + c] = cfma(acc, ST<S>::make(-0.5, 0.0), VV(i, oc));
+            Wg[(size_t)i * nb + c] = cadd(cfma(acc, ST<S>::make(-0.5, 0.0), VV(i, oc)), from_lower(cscale(ac2, 0.375f)));
         }
     }
     if (want_w && !lowdin) {
