@@ -238,10 +238,10 @@ void launch_bisect(const T* d, const T* e, int n, int nb, T* ev, int ev_ld, int 
 }
 
 // ------------------------------------------------------------------------------------------------
-// Inverse iteration. Per matrix the workspace holds 5 arrays of n x 32 values, interleaved by
-// lane ([i][lane]) so that the 32 lanes of a warp touch consecutive addresses at every step i:
-// U0, U1, U2 (the upper-triangular factor's three diagonals), Y (forward-eliminated right-hand
-// side) and Z (the current iterate).
+// Inverse iteration, one lane per eigenvalue (dstein's algorithm: LU of T - lam I with partial
+// pivoting, solves from a deterministic start vector, Gram-Schmidt inside clusters of close
+// eigenvalues). The per-lane arrays are interleaved by lane ([i][lane]) so that the lanes of a warp
+// touch consecutive addresses at every step i (layout below).
 
 __device__ __forceinline__ unsigned hash32(unsigned x) {
     x ^= x >> 16;
@@ -252,10 +252,10 @@ __device__ __forceinline__ unsigned hash32(unsigned x) {
     return x;
 }
 
-// Division in the LU of T - lam I: the FP32 kernel uses the fast form (inverse iteration only needs
-// a small backward error in its solves).
-__device__ __forceinline__ float idiv(float a, float b) { return __fdividef(a, b); }
-__device__ __forceinline__ double idiv(double a, double b) { return a / b; }
+// Pivot reciprocal in the LU of T - lam I: the FP32 kernel uses the fast form (inverse iteration
+// only needs a small backward error in its solves).
+__device__ __forceinline__ float irecip(float b) { return __fdividef(1.f, b); }
+__device__ __forceinline__ double irecip(double b) { return 1.0 / b; }
 __device__ __forceinline__ float isqrt_inv(float a) { return rsqrtf(a); }
 __device__ __forceinline__ double isqrt_inv(double a) { return 1.0 / sqrt(a); }
 
@@ -272,7 +272,7 @@ struct InvitIters<float> {
 };
 
 // Work arrays per matrix, each n x LS interleaved by lane (LS = lanes in use, min(nb, 32)): U0, U1
-// (the first two rows of U), Lm (the multipliers), Z (the vector; the forward sweep writes its
+// (the reciprocal diagonal and the first superdiagonal of U), Lm (the multipliers), Z (the vector; the forward sweep writes its
 // right-hand side into it, Y[i] landing after Z[i] was consumed, and the back substitution
 // overwrites it in place), then one word of row-interchange bits per 32 rows and lane (the third row
 // of U is e[i+1] where rows were interchanged, else 0), then copies of d and e. SMEM: all in shared
@@ -364,7 +364,7 @@ __global__ void k_invit(const T* __restrict__ dIn, const T* __restrict__ eIn, co
         // deterministic start vector in (-1, 1)
         if (active)
             for (int i = 0; i < n; ++i) {
-                const unsigned h = hash32((unsigned)(j * 7919 + 13) ^ hash32((unsigned)i + 0x9e3779b9U));
+                const unsigned h = hash32((unsigned)j * 0x9e3779b9U + (unsigned)i * 0x85ebca6bU + 0x27d4eb2fU);
                 AT(Z, i)         = T(2) * T(h & 0xffffff) / T(16777216) - T(1) + T(1e-3);
             }
         __syncwarp();
@@ -372,65 +372,58 @@ __global__ void k_invit(const T* __restrict__ dIn, const T* __restrict__ eIn, co
         T sc = T(1);  // pending scale of Z
         for (int it = 0; it < NIT; ++it) {
             if (active) {
-                T rp = AT(Z, 0) * sc, ulast;
+                T rp = AT(Z, 0) * sc;
                 if (it == 0) {
-                    // LU with partial pivoting of T - lam I (factors kept), applied to Z -> Y
+                    // LU with partial pivoting of T - lam I (factors kept), applied to Z -> Y. The
+                    // interchange is a select, not a branch (lanes pivot differently), and U0 holds
+                    // the reciprocal of the pivot (tiny pivots replaced by +-pivtiny, as dlagtf
+                    // perturbs them), so both solves multiply.
                     T        p0 = d[0] - lam, p1 = (n > 1) ? e[0] : T(0);
                     unsigned bits = 0;
                     for (int i = 0; i < n - 1; ++i) {
-                        const T s0 = e[i], s1 = d[i + 1] - lam, s2 = (i + 1 < n - 1) ? e[i + 1] : T(0);
-                        const T rs = AT(Z, i + 1) * sc;
-                        T       l;
-                        if (fabs(p0) >= fabs(s0)) {
-                            if (p0 == T(0)) p0 = pivtiny;
-                            l         = idiv(s0, p0);
-                            AT(U0, i) = p0;
-                            AT(U1, i) = p1;
-                            AT(Z, i)  = rp;
-                            p0        = s1 - l * p1;
-                            p1        = s2;
-                            rp        = rs - l * rp;
-                        } else {
-                            l         = idiv(p0, s0);
-                            AT(U0, i) = s0;
-                            AT(U1, i) = s1;
-                            AT(Z, i)  = rs;
-                            bits |= 1u << (i & 31);
-                            p0 = p1 - l * s1;
-                            p1 = -l * s2;
-                            rp = rp - l * rs;
-                        }
-                        AT(Lm, i) = l;
+                        const T    s0 = e[i], s1 = d[i + 1] - lam, s2 = (i + 1 < n - 1) ? e[i + 1] : T(0);
+                        const T    rs = AT(Z, i + 1) * sc;
+                        const bool sw = fabs(p0) < fabs(s0);
+                        T          den = sw ? s0 : p0;
+                        if (fabs(den) < pivtiny) den = (den < T(0)) ? -pivtiny : pivtiny;
+                        const T rd = irecip(den);
+                        const T l  = (sw ? p0 : s0) * rd;
+                        const T u1 = sw ? s1 : p1, zi = sw ? rs : rp;
+                        AT(U0, i)  = rd;
+                        AT(U1, i)  = u1;
+                        AT(Z, i)   = zi;
+                        AT(Lm, i)  = l;
+                        p0         = fma(-l, u1, sw ? p1 : s1);
+                        p1         = sw ? -l * s2 : s2;
+                        rp         = fma(-l, zi, sw ? rp : rs);
+                        bits |= (unsigned)sw << (i & 31);
                         if ((i & 31) == 31) {
                             AT(SW, i >> 5) = bits;
                             bits           = 0;
                         }
                     }
                     if (((n - 1) & 31) != 0) AT(SW, (n - 2) >> 5) = bits;
-                    ulast         = p0;
-                    AT(U0, n - 1) = p0;
+                    if (fabs(p0) < pivtiny) p0 = (p0 < T(0)) ? -pivtiny : pivtiny;
+                    AT(U0, n - 1) = irecip(p0);
                 } else {
                     // the same elimination on the new right-hand side
                     for (int i = 0; i < n - 1; ++i) {
-                        const T  rs = AT(Z, i + 1) * sc;
-                        const T  l  = AT(Lm, i);
+                        const T    rs = AT(Z, i + 1) * sc;
+                        const T    l  = AT(Lm, i);
                         const bool sw = (AT(SW, i >> 5) >> (i & 31)) & 1u;
-                        AT(Z, i)      = sw ? rs : rp;
-                        rp            = sw ? rp - l * rs : rs - l * rp;
+                        const T    zi = sw ? rs : rp;
+                        AT(Z, i)      = zi;
+                        rp            = fma(-l, zi, sw ? rp : rs);
                     }
-                    ulast = AT(U0, n - 1);
                 }
-                if (fabs(ulast) < pivtiny) ulast = (ulast < T(0)) ? -pivtiny : pivtiny;
                 // back substitution into Z with the 2-norm and the largest entry
-                T z2 = T(0), z1 = idiv(rp, ulast);
+                T z2 = T(0), z1 = rp * AT(U0, n - 1);
                 AT(Z, n - 1) = z1;
                 T ss = z1 * z1, zmax = fabs(z1);
                 for (int i = n - 2; i >= 0; --i) {
-                    T u0 = AT(U0, i);
-                    if (fabs(u0) < pivtiny) u0 = (u0 < T(0)) ? -pivtiny : pivtiny;
                     const bool sw = (AT(SW, i >> 5) >> (i & 31)) & 1u;
                     const T    u2 = (sw && i + 1 < n - 1) ? e[i + 1] : T(0);
-                    const T    zi = idiv(AT(Z, i) - AT(U1, i) * z1 - u2 * z2, u0);
+                    const T    zi = (AT(Z, i) - AT(U1, i) * z1 - u2 * z2) * AT(U0, i);
                     AT(Z, i)      = zi;
                     ss            = fma(zi, zi, ss);
                     zmax          = max(zmax, fabs(zi));
