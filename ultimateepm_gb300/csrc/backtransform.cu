@@ -43,11 +43,11 @@ __global__ void __launch_bounds__(32 * kBtMaxWarps) k_backtransform(const S* __r
     if (b >= batch) return;
     extern __shared__ __align__(16) unsigned char smraw[];
     // Reflector i is zero on rows <= i, i.e. on the row chunks t < tc(i) = (i + 1) / LPV of every
-    // lane, so it is staged packed: rows LPV tc(i) .. ldv - 1 only (ldv = n rounded up to LPV, the
-    // rows from n on zero), at packed_off(i) - packed_off(i0) in a block [i0, i1] of reflectors
-    // whose packed rows fit `cap` elements. At basis 137 (FP32) all 136 reflectors take 43 KB: one
-    // block, one wait.
-    const int ldv  = (n + LPV - 1) / LPV * LPV;
+    // lane, so it is staged packed: rows LPV tc(i) .. ldv - 1 only (ldv = LPV T, the rows from n on
+    // zero, so that every chunk t < T is valid and no per-chunk bound is needed), at
+    // packed_off(i) - packed_off(i0) in a block [i0, i1] of reflectors whose packed rows fit `cap`
+    // elements. At basis 137 (FP32, T = 18) all 136 reflectors take 43 KB: one block, one wait.
+    const int ldv  = LPV * T;
     S*        Vs   = reinterpret_cast<S*>(smraw);  // [cap] packed reflector rows
     S*        taus = Vs + cap;                     // [n]
     const int tid = threadIdx.x, nthr = blockDim.x;
@@ -113,7 +113,6 @@ __global__ void __launch_bounds__(32 * kBtMaxWarps) k_backtransform(const S* __r
             // the dead chunks are not issued at all
 #pragma unroll
             for (int tc = T - 1; tc >= 0; --tc) {
-                if (LPV * tc >= ldv) continue;  // uniform
                 const int ihi = min(i1, LPV * tc + LPV - 2), ilo = max(i0, LPV * tc - 1);
                 if (ihi < ilo) continue;
                 const int len  = ldv - LPV * tc;
@@ -124,10 +123,8 @@ __global__ void __launch_bounds__(32 * kBtMaxWarps) k_backtransform(const S* __r
                     S dot0 = ST<S>::zero(), dot1 = ST<S>::zero();
 #pragma unroll
                     for (int t = tc; t < T; ++t) {
-                        if (LPV * t < ldv) {  // uniform
-                            if ((t - tc) & 1) dot1 = cfmac(vrow[LPV * t], zr[t], dot1);
-                            else dot0 = cfmac(vrow[LPV * t], zr[t], dot0);
-                        }
+                        if ((t - tc) & 1) dot1 = cfmac(vrow[LPV * t], zr[t], dot1);
+                        else dot0 = cfmac(vrow[LPV * t], zr[t], dot0);
                     }
                     S dot = cadd(dot0, dot1);
 #pragma unroll
@@ -141,9 +138,7 @@ __global__ void __launch_bounds__(32 * kBtMaxWarps) k_backtransform(const S* __r
                     }
                     const S sdt = ST<S>::neg(cmul(tau, dot));
 #pragma unroll
-                    for (int t = tc; t < T; ++t) {
-                        if (LPV * t < ldv) zr[t] = cfma(vrow[LPV * t], sdt, zr[t]);
-                    }
+                    for (int t = tc; t < T; ++t) zr[t] = cfma(vrow[LPV * t], sdt, zr[t]);
                 }
             }
         }
@@ -193,7 +188,7 @@ static void bt_launch(const S* H, int n, int ld, size_t mstride, const S* tq, co
                       int batch, cudaStream_t s) {
     constexpr int GW    = 32 / LPV;
     const int     warps = std::min(kBtMaxWarps, (nb + GW - 1) / GW);
-    const int     ldv   = (n + LPV - 1) / LPV * LPV;
+    const int     ldv   = LPV * T;
     const int     total = packed_off<LPV>(std::max(n - 1, 0), ldv);  // all n - 1 reflectors
     const int     cap   = std::max(ldv, std::min(total, (int)(kBtStageBytes / sizeof(S))));
     const size_t  smem  = sizeof(S) * ((size_t)cap + n);
