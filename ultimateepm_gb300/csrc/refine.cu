@@ -365,19 +365,32 @@ __global__ void __launch_bounds__(32 * kSmallWarps) k_small_eigh(S* __restrict__
     const int nblk  = npair * (npair + 1) / 2;           // 2 x 2 blocks (k, l), k <= l, of C
     int*      pp    = reinterpret_cast<int*>(jq + me);  // pair table of the round: p, q
     int*      pq    = pp + npair;
+    // Without vectors only the near-degenerate pairs are rotated: a coupling b whose rotation angle
+    // b / gap is at most 1e-4 moves the Ritz values by b^2 / gap, which is added after the sweeps
+    // (second-order perturbation; the neglected third-order terms are ~b theta^2 < 1e-12 eV here).
+    // With vectors every pair above the threshold is rotated.
+    const R th0sq = want_w ? 0.0 : 1e-8;
+    R       dia   = 0;
+    for (int i = lane; i < m; i += 32) dia = fmax(dia, fabs(ST<S>::re(CC(i, i))));
+    dia = warp_max(dia);
+    // remaining off-diagonals move the Ritz values by at most ~off (degenerate pairs) or
+    // off^2 / gap: 1e-10 of the largest diagonal is ~2e-9 eV here
+    R thr2 = (1e-10 * dia) * (1e-10 * dia);
     for (int sweep = 0; sweep < 12; ++sweep) {
-        R off2 = 0, dia = 0;
-        for (int q = lane; q < m * m; q += 32) {
-            const int i = q / m, c = q - i * m;
-            if (i < c) off2 = fmax(off2, ST<S>::norm(CC(i, c)));
-            if (i == c) dia = fmax(dia, fabs(ST<S>::re(CC(i, i))));
+        if (want_w) {
+            R off2 = 0;
+            dia    = 0;
+            for (int q = lane; q < m * m; q += 32) {
+                const int i = q / m, c = q - i * m;
+                if (i < c) off2 = fmax(off2, ST<S>::norm(CC(i, c)));
+                if (i == c) dia = fmax(dia, fabs(ST<S>::re(CC(i, i))));
+            }
+            off2 = warp_max(off2);
+            dia  = warp_max(dia);
+            thr2 = (1e-10 * dia) * (1e-10 * dia);
+            if (off2 <= thr2 || off2 == 0.0) break;
         }
-        off2 = warp_max(off2);
-        dia  = warp_max(dia);
-        // remaining off-diagonals move the Ritz values by at most ~off (degenerate pairs) or
-        // off^2 / gap: 1e-10 of the largest diagonal is ~2e-9 eV here
-        const R thr2 = (1e-10 * dia) * (1e-10 * dia);
-        if (off2 <= thr2 || off2 == 0.0) break;
+        bool rotated = false;
         for (int round = 0; round < me - 1; ++round) {
             // tournament pairing: slot 0 fixed, slots 1..me-1 rotate
             bool act = false;
@@ -389,9 +402,9 @@ __global__ void __launch_bounds__(32 * kSmallWarps) k_small_eigh(S* __restrict__
                 if (q < m) {
                     const S bpq = CC(p, q);
                     const R b2  = ST<S>::norm(bpq);
-                    if (b2 > thr2) {
+                    const R a = ST<S>::re(CC(p, p)), d = ST<S>::re(CC(q, q));
+                    if (b2 > thr2 && b2 > th0sq * (d - a) * (d - a)) {
                         act               = true;
-                        const R     a = ST<S>::re(CC(p, p)), d = ST<S>::re(CC(q, q));
                         const float ib = rsqrtf((float)b2);  // 1 / |b|
                         const float t0 = 0.5f * (float)(d - a) * ib;
                         const float t  = copysignf(1.f, t0) / (fabsf(t0) + sqrtf(fmaf(t0, t0, 1.f)));
@@ -422,6 +435,7 @@ __global__ void __launch_bounds__(32 * kSmallWarps) k_small_eigh(S* __restrict__
                 jq[lane] = ST<S>::make(cc * ex, -cc * ey);
             }
             if (!__any_sync(0xffffffffu, act)) continue;  // warp-uniform: nothing to rotate
+            rotated = true;
             __syncwarp();
             // V <- V J, the accumulated rotations (only needed for the Ritz vectors)
             if (want_w) {
@@ -475,6 +489,33 @@ __global__ void __launch_bounds__(32 * kSmallWarps) k_small_eigh(S* __restrict__
             }
             __syncwarp();
         }
+        if (!want_w && !rotated) break;
+    }
+    if (!want_w) {
+        // lambda_p = C_pp + sum_q |C_pq|^2 / (C_pp - C_qq) over the couplings left above the
+        // threshold (all with angles below 1e-4); the small terms in FP32, the sum in FP64
+        R lam[2];
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            const int p = lane + 32 * h;
+            if (p >= m) continue;
+            const R cpp = ST<S>::re(CC(p, p));
+            float   cor = 0.f;
+            for (int q = 0; q < m; ++q) {
+                if (q == p) continue;
+                const R b2 = ST<S>::norm(CC(p, q));
+                const R g  = cpp - ST<S>::re(CC(q, q));
+                if (b2 > thr2 && g != 0.0) cor += __fdividef((float)b2, (float)g);
+            }
+            lam[h] = cpp + (R)cor;
+        }
+        __syncwarp();
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            const int p = lane + 32 * h;
+            if (p < m) CC(p, p) = ST<S>::make(lam[h], 0.0);
+        }
+        __syncwarp();
     }
     // ascending order of the Ritz values, nb smallest out: the rank of each value among all (ties
     // by index, i.e. a stable sort) from integer keys that order as the doubles do (-0 as +0)
