@@ -173,19 +173,32 @@ __global__ void __launch_bounds__(NT) k_tridiag(S* __restrict__ H, int n, int ld
         __syncthreads();
 
         // ---- A22 -= v w^H + w v^H: lower triangle computed, upper mirrored -------------------
-        for (int c = warp; c < m; c += NW) {
-            S*      ac = A + (size_t)(o + c) * ld + o;
-            const S vc = v[c], wc = w[c];
-            for (int r = c + lane; r < m; r += 32) {
-                S a = ldc(ac + r);
-                a   = cfms_conjb(v[r], wc, a);
-                a   = cfms_conjb(w[r], vc, a);
+        // The m (m + 1) / 2 lower elements in column-major order, element e to thread e mod NT:
+        // consecutive threads take consecutive rows of a column (coalesced), and only the last
+        // round has idle lanes (per-column 32-row chunks left ~16 idle lanes in every column).
+        {
+            const int tot = m * (m + 1) / 2;
+            int       c = 0, r = tid;  // (column, row) of element tid
+            while (r >= m && c < m) {
+                r = r - m + c + 1;
+                ++c;
+            }
+            for (int e = tid; e < tot; e += NT) {
+                S*      ac = A + (size_t)(o + c) * ld + o;
+                S       a  = ldc(ac + r);
+                a          = cfms_conjb(v[r], w[c], a);
+                a          = cfms_conjb(w[r], v[c], a);
                 if (r == c) {
                     a = ST<S>::make(ST<S>::re(a), R(0));
                 } else {
                     stc(A + (size_t)(o + r) * ld + (o + c), ST<S>::conj(a));
                 }
                 stc(ac + r, a);
+                r += NT;  // next element of this thread
+                while (r >= m && c < m) {
+                    r = r - m + c + 1;
+                    ++c;
+                }
             }
         }
         __syncthreads();
@@ -230,11 +243,12 @@ static void tridiag_launch_t(S* H, int n, int ld, size_t mstride, typename ST<S>
     if (smem > 48 * 1024) cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     int grid = batch;
     if (!SMEM) {
-        // automatic: keep the matrices in flight within ~96 MB so that they stay in the 129 MB L2, but
+        // automatic: keep the matrices in flight within ~120 MB so that they stay in the 129 MB L2
+        // (FP64 at n = 137: 5 per SM, 13.1 ms for 2000 matrices against 14.1 at 4 and 14.5 at 6), but
         // never below 4 CTAs per SM: for large (complex / spin-orbit) matrices, latency hiding wins
         // over L2 residency (measured 1.5-2x over 1 CTA per SM at n = 178..458, FP32)
         const size_t bytes  = sizeof(S) * (size_t)n * n;
-        int          per_sm = (int)std::max<size_t>(4, std::min<size_t>(8, (96u << 20) / (bytes * (size_t)sm_count())));
+        int          per_sm = (int)std::max<size_t>(4, std::min<size_t>(8, (120u << 20) / (bytes * (size_t)sm_count())));
         if (ctas_per_sm > 0) per_sm = std::min(ctas_per_sm, 8);
         grid = std::min(batch, per_sm * sm_count());
     }
