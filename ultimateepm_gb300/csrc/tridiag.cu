@@ -30,12 +30,22 @@
 
 namespace uepm {
 
+constexpr int kUpd = 4;  // elements per thread per round of the rank-2 update
+
 // SMEM = true: the matrix is copied into shared memory (leading dimension n | 1, odd, so that the
 // mirrored row-wise stores do not collide on banks), reduced there, and its reflector columns are
 // written back. Used where n x n fits (the FP32 reductions of the mixed path), because those are
 // bound by memory latency rather than by arithmetic.
+// Global-memory variant: CTAs per SM that must fit the register file (the persistent grid relies on
+// several to hide L2/DRAM latency): 5 for the real and complex-FP32 matrices up to n = 161, 4 above,
+// fewer for complex FP64 with many row chunks (whose accumulators alone take 4 MAXT registers).
+template <typename S, int MAXT>
+constexpr int tridiag_min_blocks() {
+    return sizeof(S) * MAXT <= 8 * 5 ? 5 : (sizeof(S) <= 8 || MAXT <= 5 ? 4 : (MAXT <= 8 ? 3 : 2));
+}
+
 template <typename S, int NT, int MAXT, bool SMEM>
-__global__ void __launch_bounds__(NT) k_tridiag(S* __restrict__ H, int n, int ldg, size_t mstride,
+__global__ void __launch_bounds__(NT, SMEM ? 1 : tridiag_min_blocks<S, MAXT>()) k_tridiag(S* __restrict__ H, int n, int ldg, size_t mstride,
                                                 typename ST<S>::R* __restrict__ dOut, typename ST<S>::R* __restrict__ eOut,
                                                 S* __restrict__ tqOut, int* __restrict__ status, int batch) {
     using R       = typename ST<S>::R;
@@ -176,6 +186,8 @@ __global__ void __launch_bounds__(NT) k_tridiag(S* __restrict__ H, int n, int ld
         // The m (m + 1) / 2 lower elements in column-major order, element e to thread e mod NT:
         // consecutive threads take consecutive rows of a column (coalesced), and only the last
         // round has idle lanes (per-column 32-row chunks left ~16 idle lanes in every column).
+        // Each thread takes its elements kUpd at a time, all loads first, so that kUpd loads per
+        // thread are in flight (one at a time left every element waiting a full L2/DRAM latency).
         {
             const int tot = m * (m + 1) / 2;
             int       c = 0, r = tid;  // (column, row) of element tid
@@ -183,21 +195,34 @@ __global__ void __launch_bounds__(NT) k_tridiag(S* __restrict__ H, int n, int ld
                 r = r - m + c + 1;
                 ++c;
             }
-            for (int e = tid; e < tot; e += NT) {
-                S*      ac = A + (size_t)(o + c) * ld + o;
-                S       a  = ldc(ac + r);
-                a          = cfms_conjb(v[r], w[c], a);
-                a          = cfms_conjb(w[r], v[c], a);
-                if (r == c) {
-                    a = ST<S>::make(ST<S>::re(a), R(0));
-                } else {
-                    stc(A + (size_t)(o + r) * ld + (o + c), ST<S>::conj(a));
+            for (int e0 = tid; e0 < tot; e0 += kUpd * NT) {
+                int cq[kUpd], rq[kUpd];
+                S   aq[kUpd];
+#pragma unroll
+                for (int q = 0; q < kUpd; ++q) {
+                    cq[q] = c;
+                    rq[q] = r;
+                    r += NT;  // next element of this thread
+                    while (r >= m && c < m) {
+                        r = r - m + c + 1;
+                        ++c;
+                    }
                 }
-                stc(ac + r, a);
-                r += NT;  // next element of this thread
-                while (r >= m && c < m) {
-                    r = r - m + c + 1;
-                    ++c;
+#pragma unroll
+                for (int q = 0; q < kUpd; ++q)
+                    if (e0 + q * NT < tot) aq[q] = ldc(A + (size_t)(o + cq[q]) * ld + o + rq[q]);
+#pragma unroll
+                for (int q = 0; q < kUpd; ++q) {
+                    if (e0 + q * NT >= tot) break;
+                    const int cc = cq[q], rr = rq[q];
+                    S         a  = cfms_conjb(v[rr], w[cc], aq[q]);
+                    a            = cfms_conjb(w[rr], v[cc], a);
+                    if (rr == cc) {
+                        a = ST<S>::make(ST<S>::re(a), R(0));
+                    } else {
+                        stc(A + (size_t)(o + rr) * ld + (o + cc), ST<S>::conj(a));
+                    }
+                    stc(A + (size_t)(o + cc) * ld + o + rr, a);
                 }
             }
         }
@@ -250,6 +275,9 @@ static void tridiag_launch_t(S* H, int n, int ld, size_t mstride, typename ST<S>
         const size_t bytes  = sizeof(S) * (size_t)n * n;
         int          per_sm = (int)std::max<size_t>(4, std::min<size_t>(8, (120u << 20) / (bytes * (size_t)sm_count())));
         if (ctas_per_sm > 0) per_sm = std::min(ctas_per_sm, 8);
+        int fit = 0;  // never more than are resident at once: the rest would wait as a tail
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&fit, kern, NT, smem) == cudaSuccess && fit > 0)
+            per_sm = std::min(per_sm, fit);
         grid = std::min(batch, per_sm * sm_count());
     }
     kern<<<grid, NT, smem, s>>>(H, n, ld, mstride, d, e, tq, status, batch);
