@@ -137,15 +137,32 @@ __global__ void __launch_bounds__(NT, SMEM ? 1 : tridiag_min_blocks<S, MAXT>()) 
 #pragma unroll
         for (int t = 0; t < MAXT; ++t) acc[t] = ST<S>::zero();
         const int tn = (m + 31) >> 5;
+        // FP32 matrices beyond the on-chip sizes reduce from L2/DRAM and wait on memory: there the
+        // column's chunks are all loaded before the first FMA (Ge SOC n = 362: 242 -> 220 ms per
+        // 2000 k). The FP64 kernel is FP64-pipe bound and keeps the interleaved form (11.2 vs
+        // 12.0 ms at n = 137), as do the shapes where the extra registers would spill.
+        constexpr bool kBatchLoads = sizeof(R) == 4 && MAXT <= 12;
         for (int c = warp; c < m; c += NW) {
             const S* ac = A + (size_t)(o + c) * ld + o;
             const S  vc = v[c];
+            if constexpr (kBatchLoads) {
+                S a[MAXT];
 #pragma unroll
-            for (int t = 0; t < MAXT; ++t) {
-                if (t < tn) {  // warp-uniform
+                for (int t = 0; t < MAXT; ++t) {
                     const int r = lane + 32 * t;
-                    const S   a = (r < m) ? ldc(ac + r) : ST<S>::zero();
-                    acc[t]      = cfma(a, vc, acc[t]);
+                    a[t]        = (t < tn && r < m) ? ldc(ac + r) : ST<S>::zero();
+                }
+#pragma unroll
+                for (int t = 0; t < MAXT; ++t)
+                    if (t < tn) acc[t] = cfma(a[t], vc, acc[t]);  // warp-uniform
+            } else {
+#pragma unroll
+                for (int t = 0; t < MAXT; ++t) {
+                    if (t < tn) {  // warp-uniform
+                        const int r = lane + 32 * t;
+                        const S   a = (r < m) ? ldc(ac + r) : ST<S>::zero();
+                        acc[t]      = cfma(a, vc, acc[t]);
+                    }
                 }
             }
         }
