@@ -179,8 +179,10 @@ int uepm_measure_peak(int precision, double* tflops);
  *   reduction     the Householder reduction kernel: 1 register-resident (FP32 real matrices, n <= 176),
  *                 2 one CTA per matrix (shared memory where the matrix fits, else global memory with
  *                 a persistent grid), 3 one thread-block cluster per matrix, the matrix spread over
- *                 the cluster's shared memory (orders beyond one SM); automatic: 1 where it applies,
- *                 3 for complex FP32 matrices just beyond one SM (n <= 300), else 2
+ *                 the cluster's shared memory (orders beyond one SM), 4 one CTA per matrix in global
+ *                 memory with each step's update fused into the next step's product (FP32 matrices
+ *                 beyond the on-chip sizes, n <= 512); automatic: 1 where it applies, 4 for the
+ *                 other FP32 matrices beyond the on-chip sizes, else 2
  *   ctas_per_sm   CTAs per SM of the global-memory reduction (its L2 working set), 1..8
  *   vector_lanes  lanes per eigenvector in the back-transformation: 8, 16 or 32
  *   chunk         k-points per pipeline pass (smaller keeps H(k) resident in L2 between the

@@ -265,6 +265,234 @@ __global__ void __launch_bounds__(NT, SMEM ? 1 : tridiag_min_blocks<S, MAXT>()) 
     }
 }
 
+// ------------------------------------------------------------------------------------------------
+// Fused variant for FP32 matrices reduced from L2/DRAM (beyond the on-chip sizes), where every
+// step streams the trailing matrix through memory. Step j (reflector v_j on rows/columns o = j+1..):
+//   (a) p_j = A v_j from the previous pass's per-warp partials; w_j = tau p_j - (tau/2)(w^H v_j) v_j
+//   (b) step j's update of column o alone, then the reflector of column o (d, e, tau, v_{j+1} and
+//       its tail in H)
+//   (c) ONE pass over the trailing block [o+1:, o+1:]: each element gets step j's update
+//       a -= v w^H + w v^H (both triangles, no mirror store) and enters p_{j+1} = A v_{j+1}
+//       before it is stored.
+// One read and one write per element and step, where the unfused kernel reads the block for the
+// product, reads and writes the lower triangle for the update, and scatters the mirror (32-byte
+// sectors for 8-byte elements). The two triangles are updated with the same products, so they stay
+// Hermitian to rounding; the diagonal is kept real.
+template <typename S, int NT>
+__device__ __forceinline__ void fused_reflector(const S (&colv)[2], S* __restrict__ A, int ld, int n, int col,
+                                                typename ST<S>::R* dB, typename ST<S>::R* eB, S* tB, S* vnext,
+                                                typename ST<S>::R* red, S* s_sc, S* s_th, S* s_alpha, bool& bad) {
+    using R          = typename ST<S>::R;
+    constexpr int NW = NT / 32;
+    const int     tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, m = n - col;
+    R             part = 0;
+#pragma unroll
+    for (int k = 0; k < 2; ++k) {
+        const int rr = threadIdx.x + NT * k;
+        if (rr >= m) continue;
+        if (rr >= 2) part += ST<S>::norm(colv[k]);
+        if (rr == 1) *s_alpha = colv[k];
+        if (rr == 0) {
+            const R dv = ST<S>::re(colv[k]);
+            dB[col]    = dv;
+            if (!isfinite(dv)) bad = true;
+        }
+    }
+    part = warp_sum(part);
+    if (lane == 0) red[warp] = part;
+    __syncthreads();
+    if (tid == 0) {
+        S th = ST<S>::zero(), sc = ST<S>::zero();
+        if (m >= 2) {
+            R tail2 = 0;
+#pragma unroll
+            for (int q = 0; q < NW; ++q) tail2 += red[q];
+            const S c0 = *s_alpha;
+            const R c0r = ST<S>::re(c0), c0i = ST<S>::im(c0);
+            R       beta;
+            if (tail2 <= num<R>::tiny() && c0i * c0i <= num<R>::tiny()) {
+                beta = c0r;
+            } else {
+                beta = sqrt(fma(c0r, c0r, fma(c0i, c0i, tail2)));
+                if (c0r >= 0) beta = -beta;
+                const R ib = R(1) / beta;
+                th         = ST<S>::make((beta - c0r) * ib, -c0i * ib);
+                const R ar = c0r - beta, ai = c0i;
+                const R den = R(1) / fma(ar, ar, ai * ai);
+                sc          = ST<S>::make(ar * den, -ai * den);  // 1 / (c0 - beta)
+            }
+            eB[col]                                = beta;
+            A[(size_t)col * ld + col + 1]          = ST<S>::make(beta, R(0));
+            if (!isfinite(beta)) bad = true;
+        } else {
+            eB[col] = R(0);
+        }
+        tB[col] = th;
+        *s_th   = th;
+        *s_sc   = sc;
+    }
+    __syncthreads();
+    const S sc = *s_sc;
+#pragma unroll
+    for (int k = 0; k < 2; ++k) {
+        const int rr = threadIdx.x + NT * k;
+        if (rr < 1 || rr >= m) continue;
+        if (rr == 1) {
+            vnext[0] = ST<S>::one();
+        } else {
+            const S x     = cmul(colv[k], sc);
+            vnext[rr - 1] = x;
+            stc(A + (size_t)col * ld + col + rr, x);
+        }
+    }
+    __syncthreads();
+}
+
+template <typename S, int NT, int MAXT>
+__global__ void __launch_bounds__(NT, 4) k_tridiag_fused(S* __restrict__ H, int n, int ld, size_t mstride,
+                                                        typename ST<S>::R* __restrict__ dOut,
+                                                        typename ST<S>::R* __restrict__ eOut, S* __restrict__ tqOut,
+                                                        int* __restrict__ status, int batch) {
+    using R          = typename ST<S>::R;
+    constexpr int NW = NT / 32;
+    extern __shared__ __align__(16) unsigned char smraw[];
+    S*        vb   = reinterpret_cast<S*>(smraw);            // [2][n] reflectors, by step parity
+    S*        w    = vb + 2 * (size_t)n;                      // [n]
+    S*        pacc = w + n;                                   // [NW][n] per-warp partials of A v
+    R*        red  = reinterpret_cast<R*>(pacc + (size_t)NW * n);  // [3 NW]: norms | dot re | dot im
+    __shared__ S s_sc, s_th, s_alpha;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    for (int b = blockIdx.x; b < batch; b += gridDim.x) {
+        __syncthreads();  // shared memory of the previous matrix consumed
+        S*   A   = H + (size_t)b * mstride;
+        R*   dB  = dOut + (size_t)b * n;
+        R*   eB  = eOut + (size_t)b * n;
+        S*   tB  = tqOut + (size_t)b * n;
+        bool bad = false;
+        // ---- the reflector of column 0, then p_0 = A[1:,1:] v_0 (pass without update) ----------
+        S colv[2];
+#pragma unroll
+        for (int k = 0; k < 2; ++k) {
+            const int rr = tid + NT * k;
+            colv[k]      = rr < n ? ldc(A + rr) : ST<S>::zero();
+        }
+        fused_reflector<S, NT>(colv, A, ld, n, 0, dB, eB, tB, vb, red, &s_sc, &s_th, &s_alpha, bad);
+        S th = s_th;
+        for (int j = 0; j <= n - 1; ++j) {
+            // pass over the block [o+1:, o+1:] (o = j for the prologue pass at j = 0, j + 1 after):
+            // prologue: product with v_0 only; step j: update with (v_j, w_j), product with v_{j+1}
+            const bool pro = j == 0;
+            const int  o   = pro ? 0 : j;  // the block starts at row/column o + 1
+            const int  mb  = n - 1 - o;
+            if (!pro && mb < 0) break;
+            const S* vcur = vb + (size_t)((j - 1) & 1) * n;  // v_{j-1}: offset rows o.. (step j-1's)
+            const S* vnx  = vb + (size_t)(j & 1) * n;        // v_j on rows o + 1..
+            if (mb >= 1) {
+                S         acc[MAXT];
+#pragma unroll
+                for (int t = 0; t < MAXT; ++t) acc[t] = ST<S>::zero();
+                const int tn = (mb + 31) >> 5;
+                // a column's chunks in groups of GS: the group's loads are issued together, then
+                // updated, stored and accumulated (smaller groups for the long columns, whose
+                // loads would otherwise spill)
+                constexpr int GS = MAXT > 12 ? 4 : (MAXT > 8 ? (MAXT + 1) / 2 : MAXT);
+                for (int C = warp; C < mb; C += NW) {
+                    S*      ac = A + (size_t)(o + 1 + C) * ld + o + 1;
+                    const S vn = vnx[C];
+                    const S wc = pro ? ST<S>::zero() : w[C + 1], vc = pro ? ST<S>::zero() : vcur[C + 1];
+#pragma unroll
+                    for (int g = 0; g < MAXT; g += GS) {
+                        S a[GS];
+#pragma unroll
+                        for (int q = 0; q < GS; ++q) {
+                            const int t = g + q, Rr = lane + 32 * t;
+                            a[q]        = (t < MAXT && t < tn && Rr < mb) ? ldc(ac + Rr) : ST<S>::zero();
+                        }
+#pragma unroll
+                        for (int q = 0; q < GS; ++q) {
+                            const int t = g + q, Rr = lane + 32 * t;
+                            if (t < MAXT && t < tn) {  // warp-uniform
+                                if (!pro && Rr < mb) {
+                                    S x = cfms_conjb(vcur[Rr + 1], wc, a[q]);
+                                    x   = cfms_conjb(w[Rr + 1], vc, x);
+                                    if (Rr == C) x = ST<S>::make(ST<S>::re(x), R(0));
+                                    stc(ac + Rr, x);
+                                    a[q] = x;
+                                }
+                                acc[t] = cfma(a[q], vn, acc[t]);
+                            }
+                        }
+                    }
+                }
+#pragma unroll
+                for (int t = 0; t < MAXT; ++t) {
+                    const int Rr = lane + 32 * t;
+                    if (t < tn && Rr < mb) pacc[(size_t)warp * n + Rr] = acc[t];
+                }
+            }
+            __syncthreads();
+            // ---- step j' = (pro ? 0 : j): p = A v_{j'} (rows o + 1..), w, then column o + 1 --------
+            const int col = o + 1;  // the next column to reduce
+            const int m   = n - col;
+            if (m < 1) break;
+            const S* v = vnx;  // v_{j'} on rows col..
+            S        wown[2];
+            S        dot = ST<S>::zero();
+#pragma unroll
+            for (int k = 0; k < 2; ++k) {
+                const int rr = tid + NT * k;
+                wown[k]      = ST<S>::zero();
+                if (rr < m) {
+                    S p = pacc[rr];
+#pragma unroll
+                    for (int q = 1; q < NW; ++q) p = cadd(p, pacc[(size_t)q * n + rr]);
+                    wown[k] = cmul(th, p);
+                    dot     = cfmac(wown[k], v[rr], dot);
+                }
+            }
+            dot = warp_sum(dot);
+            if (lane == 0) {
+                red[NW + warp]     = ST<S>::re(dot);
+                red[2 * NW + warp] = ST<S>::im(dot);
+            }
+            __syncthreads();
+            R dr = 0, di = 0;
+#pragma unroll
+            for (int q = 0; q < NW; ++q) {
+                dr += red[NW + q];
+                di += red[2 * NW + q];
+            }
+            const S alpha = cscale(cmul(th, ST<S>::make(dr, di)), R(-0.5));
+            S       p0    = pacc[0];
+#pragma unroll
+            for (int q = 1; q < NW; ++q) p0 = cadd(p0, pacc[(size_t)q * n]);
+            const S w0 = cfma(alpha, v[0], cmul(th, p0));
+#pragma unroll
+            for (int k = 0; k < 2; ++k) {
+                const int rr = tid + NT * k;
+                if (rr < m) {
+                    wown[k] = cfma(alpha, v[rr], wown[k]);
+                    w[rr]   = wown[k];
+                    // column col after the step: a -= v_r conj(w_0) + w_r conj(v_0)
+                    S x = ldc(A + (size_t)col * ld + col + rr);
+                    x   = cfms_conjb(v[rr], w0, x);
+                    x   = cfms_conjb(wown[k], v[0], x);
+                    if (rr == 0) x = ST<S>::make(ST<S>::re(x), R(0));
+                    colv[k] = x;
+                } else {
+                    colv[k] = ST<S>::zero();
+                }
+            }
+            // (w is read by the next pass after the reflector's barriers)
+            fused_reflector<S, NT>(colv, A, ld, n, col, dB, eB, tB, vb + (size_t)((j + 1) & 1) * n, red, &s_sc, &s_th,
+                                   &s_alpha, bad);
+            th = s_th;
+        }
+        bad = __syncthreads_or(bad);
+        if (tid == 0 && bad && status) atomicOr(status + b, 2);  // UEPM_K_NONFINITE
+    }
+}
+
 static int sm_count() {
     static int sms = 0;
     if (!sms) {
@@ -301,6 +529,27 @@ static void tridiag_launch_t(S* H, int n, int ld, size_t mstride, typename ST<S>
     count_launch();
 }
 
+template <typename S, int MAXT>
+static void fused_launch_t(S* H, int n, int ld, size_t mstride, typename ST<S>::R* d, typename ST<S>::R* e, S* tq,
+                           int* status, int batch, cudaStream_t s, int ctas_per_sm) {
+    using R           = typename ST<S>::R;
+    constexpr int NT  = 256;
+    const size_t  smem = sizeof(S) * (size_t)(3 + NT / 32) * n + sizeof(R) * 3 * (NT / 32);
+    auto          kern = k_tridiag_fused<S, NT, MAXT>;
+    if (smem > 48 * 1024) cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    // matrices in flight as for the unfused kernel (L2 budget, at least 4 per SM), capped at the
+    // kernel's occupancy
+    const size_t bytes  = sizeof(S) * (size_t)n * n;
+    int          per_sm = (int)std::max<size_t>(4, std::min<size_t>(8, (120u << 20) / (bytes * (size_t)sm_count())));
+    if (ctas_per_sm > 0) per_sm = std::min(ctas_per_sm, 8);
+    int fit = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&fit, kern, NT, smem) == cudaSuccess && fit > 0)
+        per_sm = std::min(per_sm, fit);
+    const int grid = std::min(batch, per_sm * sm_count());
+    kern<<<grid, NT, smem, s>>>(H, n, ld, mstride, d, e, tq, status, batch);
+    count_launch();
+}
+
 // Shared-memory residency: FP32 matrices whose n x n copy (plus vectors) fits in 200 KB.
 template <typename S>
 static bool use_smem(int n) {
@@ -324,14 +573,24 @@ void launch_tridiag(S* H, int n, int ld, size_t mstride, typename ST<S>::R* d, t
             return;
         }
     }
-    // automatic cluster reduction where it measured faster than the global-memory kernel: complex
-    // FP32 matrices just beyond one SM (orders 178..274: 1.15-1.25x); for larger orders and for FP64
-    // the global-memory kernel's 32 warps per SM hide more latency than the cluster's barriers allow
-    constexpr bool CX = !std::is_same<S, typename ST<S>::R>::value;
+    // the cluster reduction is a tuning choice: the fused kernel below beats it at every order it
+    // was automatic for (complex FP32, 2000 k: n = 178 22.5 vs 30.4 ms, 229 50.2 vs 79.7, 274 64.3
+    // vs 112.0)
     constexpr bool F32 = sizeof(typename ST<S>::R) == 4;
-    const bool auto_cluster = variant == 0 && CX && F32 && !use_smem<S>(n) && n <= 300;
-    if ((variant == 3 || auto_cluster) && launch_tridiag_cluster<S>(H, n, ld, mstride, d, e, tq, status, batch, s, cluster))
-        return;
+    if (variant == 3 && launch_tridiag_cluster<S>(H, n, ld, mstride, d, e, tq, status, batch, s, cluster)) return;
+    // FP32 matrices reduced from L2/DRAM: the fused kernel (one pass per step; Ge SOC n = 362:
+    // 142 vs 261 ms per 2000 k for the unfused kernel)
+    if constexpr (F32) {
+        const bool auto_fused = variant == 0 && !use_smem<S>(n);
+        if ((variant == 4 || auto_fused) && n <= 512) {
+            if (n <= 129) fused_launch_t<S, 4>(H, n, ld, mstride, d, e, tq, status, batch, s, ctas_per_sm);
+            else if (n <= 161) fused_launch_t<S, 5>(H, n, ld, mstride, d, e, tq, status, batch, s, ctas_per_sm);
+            else if (n <= 257) fused_launch_t<S, 8>(H, n, ld, mstride, d, e, tq, status, batch, s, ctas_per_sm);
+            else if (n <= 385) fused_launch_t<S, 12>(H, n, ld, mstride, d, e, tq, status, batch, s, ctas_per_sm);
+            else fused_launch_t<S, 16>(H, n, ld, mstride, d, e, tq, status, batch, s, ctas_per_sm);
+            return;
+        }
+    }
     // rows of the trailing matrix are at most n - 1 <= 32 * MAXT
     if (n <= 129) tridiag_pick<S, 4>(H, n, ld, mstride, d, e, tq, status, batch, s, ctas_per_sm);
     else if (n <= 161) tridiag_pick<S, 5>(H, n, ld, mstride, d, e, tq, status, batch, s, ctas_per_sm);

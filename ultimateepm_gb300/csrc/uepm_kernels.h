@@ -23,9 +23,11 @@ void launch_assemble(const DevParams& P, const cx<double>* Vloc, const double2* 
 // status: [batch] (ORed with UEPM_K_NONFINITE on NaN/Inf).
 // variant: 0 automatic, 1 register-resident (FP32 real, n <= tridiag_reg_max_n()), 2 one CTA per
 // matrix (shared memory where the matrix fits, else global memory with a persistent grid), 3 one
-// thread-block cluster per matrix (tridiag_cluster.cu). Automatic: 1 where it applies, 3 for complex
-// FP32 matrices just beyond one SM's shared memory (n <= 300), else 2. ctas_per_sm (0: automatic) caps the persistent grid
-// of the global-memory kernel; cluster (0: automatic) is the cluster size of variant 3.
+// thread-block cluster per matrix (tridiag_cluster.cu), 4 one CTA per matrix in global memory with
+// each step's update fused into the next step's product (FP32, n <= 512). Automatic: 1 where it
+// applies, 4 for the other FP32 matrices beyond the on-chip sizes, else 2. ctas_per_sm (0: automatic) caps the
+// persistent grid of the global-memory kernels; cluster (0: automatic) is the cluster size of
+// variant 3.
 template <typename S>
 void launch_tridiag(S* H, int n, int ld, size_t mstride, typename ST<S>::R* d, typename ST<S>::R* e, S* tq, int* status,
                     int batch, cudaStream_t s, int variant = 0, int ctas_per_sm = 0, int cluster = 0);
