@@ -236,6 +236,25 @@ uint64_t uepm_batch_kernels_per_run(const uepm_batch* b);
  * All pointers are device pointers; E is [.][nb], gradients [.][nb][3]; enqueued on `stream`. */
 int uepm_star_expand_device(const double* d_E_iw, const double* d_grad_iw, const int64_t* d_src, const uint16_t* d_op,
                             size_t n_full, int nb, double* d_E_full, double* d_grad_full, void* stream);
+
+/* Dielectric function from the eigenstates at k and k + q: the per-q body of
+ * DielectricFunction::compute_dielectric_function (src/EPP/DielectricFunction.cpp:92-150), and,
+ * with per-vertex weights (the volume / 4 of each tetrahedron holding the vertex), the tetrahedron
+ * sums of BZ_States::compute_dielectric_function (src/BZ_MESH/bz_states.cpp:101-140). For each of
+ * nk k-points, the P = (nb - first_cond) * first_cond squared overlaps
+ * O_cv = |sum_i u_c(k+q)_i u_v(k)_i|^2 (conduction c in [first_cond, nb) at k + q, valence
+ * v < first_cond at k; no factor conjugated, as the reference's Eigen expression
+ * col(c).adjoint().dot(col(v)) evaluates, which equals |<u_c|u_v>|^2 for a real H) and
+ * differences dE_cv = E_c(k+q) - E_v(k) give, at each of ne energies w,
+ *   s_k(w) = sum_{c,v} O_cv [(dE - w) / ((dE - w)^2 + eta^2) + (dE + w) / ((dE + w)^2 + eta^2)],
+ * and weights[k] * s_k(w) (weights NULL: 1) is ADDED to sums[w]. X_k, X_kq: [nk][nb][n] complex
+ * (re, im doubles: the layout uepm_solve writes), E_k, E_kq: [nk][nb], energies [ne], sums [ne];
+ * all device pointers, enqueued on `stream` with stream-ordered scratch (2 * SMs * ne doubles).
+ * ne <= 4096; nb * n complex must fit one CTA's shared memory (n <= ~780 at nb = 16). The sums are
+ * deterministic (fixed reduction order). */
+int uepm_dielectric_sums_device(const double* d_Xk, const double* d_Xkq, const double* d_Ek, const double* d_Ekq,
+                                size_t nk, int nb, int n, int first_cond, const double* d_energies, int ne, double eta,
+                                const double* d_weights, double* d_sums, void* stream);
 /* Host: the packed signed permutations op[q] mapping k_src[q] onto k_dst[q] (n pairs of reduced or
  * SI k-points, the rule of apply_same_symmetry_operation); found[q] = 0 (optional) where none
  * exists, with the identity written. */

@@ -346,3 +346,109 @@ def sample_first_bz(n: int, seed: int) -> np.ndarray:
         out.append(k[ok])
         have += int(ok.sum())
     return np.concatenate(out)[:n].copy()
+
+
+# ---- dielectric function (eigenvector consumer) ---------------------------------------------------
+def is_in_first_bz(k, one_eighth=False) -> bool:
+    """is_in_first_BZ (src/EPP/DielectricFunction.cpp:35-40)."""
+    x, y, z = (float(v) for v in k)
+    c1 = abs(x) <= 1.0 and abs(y) <= 1.0 and abs(z) <= 1.0
+    c2 = abs(x) + abs(y) + abs(z) <= 3.0 / 2.0
+    c8 = x >= 0.0 and y >= 0.0 and z >= 0.0
+    return c1 and c2 and (c8 if one_eighth else True)
+
+
+def is_in_irreducible_wedge_df(k) -> bool:
+    """is_in_irreducible_wedge (src/EPP/DielectricFunction.cpp:31-33)."""
+    x, y, z = (float(v) for v in k)
+    return z >= 0.0 and y >= z and x >= y and x <= 1.0 and x + y + z <= 3.0 / 2.0
+
+
+def dielectric_k_grid(nx: int, ny: int, nz: int, shift: float, irreducible_wedge: bool) -> np.ndarray:
+    """DielectricFunction::generate_k_points_grid (src/EPP/DielectricFunction.cpp:59-76): i, j, k
+    loops over N-1 points each of [-1 - shift, 1 + shift], kept in the first zone (and the wedge)."""
+    lo, hi = -1.0 - shift, 1.0 + shift
+    out = []
+    for i in range(nx - 1):
+        for j in range(ny - 1):
+            for k in range(nz - 1):
+                v = (lo + (hi - lo) * i / float(nx - 1), lo + (hi - lo) * j / float(ny - 1),
+                     lo + (hi - lo) * k / float(nz - 1))
+                if is_in_first_bz(v) and (not irreducible_wedge or is_in_irreducible_wedge_df(v)):
+                    out.append(v)
+    return np.array(out, dtype=np.float64).reshape(-1, 3)
+
+
+def dielectric_pair_sums(Ek, Xk, Ekq, Xkq, energies, eta, first_cond=4, weights=None) -> np.ndarray:
+    """The per-k sums of DielectricFunction::compute_dielectric_function
+    (src/EPP/DielectricFunction.cpp:122-143), from eigenstates at k and k + q ([nk][nb][n] vectors,
+    [nk][nb] energies): sum over k of weight_k * sum_{c >= first_cond > v} |sum_i u_c(k+q)_i u_v(k)_i|^2
+    [(dE - w) / ((dE - w)^2 + eta^2) + (dE + w) / ((dE + w)^2 + eta^2)], dE = E_c(k+q) - E_v(k)."""
+    en = np.asarray(energies, dtype=np.float64)
+    total = np.zeros(len(en))
+    nk, nb = Ek.shape
+    for b in range(nk):
+        ksum = np.zeros(len(en))
+        for c in range(first_cond, nb):
+            for v in range(first_cond):
+                # col(c).adjoint().dot(col(v)) in Eigen: dot() conjugates its first operand, already
+                # the adjoint, so the sum is unconjugated
+                ov = abs(np.dot(Xkq[b, c], Xk[b, v])) ** 2
+                d = Ekq[b, c] - Ek[b, v]
+                f1 = (d - en) / ((d - en) * (d - en) + eta * eta)
+                f2 = (d + en) / ((d + en) * (d + en) + eta * eta)
+                ksum += ov * (f1 + f2)
+        total += (1.0 if weights is None else float(weights[b])) * ksum
+    return total
+
+
+def dielectric_sums(mat: OrMaterial, G: np.ndarray, kpts: np.ndarray, q, nb: int, energies, eta: float, nl=False,
+                    first_cond=4, weights=None) -> np.ndarray:
+    """One q of DielectricFunction::compute_dielectric_function (src/EPP/DielectricFunction.cpp:
+    83-150): eigenstates at k and at k + q (q of length <= 1e-15 replaced by (1e-15, 1e-15, 1e-15),
+    :97-99), then the pair sums."""
+    q = np.asarray(q, dtype=np.float64)
+    if np.sqrt(np.dot(q, q)) <= 1e-15:
+        q = np.array([1e-15, 1e-15, 1e-15])
+    k = np.ascontiguousarray(kpts, dtype=np.float64).reshape(-1, 3)
+    a = band_structure(mat, G, k, nb, nl=nl, vectors=True)
+    b = band_structure(mat, G, k + q[None, :], nb, nl=nl, vectors=True)
+    return dielectric_pair_sums(a["E"], a["vecs"], b["E"], b["vecs"], energies, eta, first_cond, weights)
+
+
+def dielectric_merge(qpoints, results, nb_kpoints_per_instance) -> np.ndarray:
+    """DielectricFunction::merge_results (src/EPP/DielectricFunction.cpp:152-212): the instances'
+    [q][energy] sums added, divided by the total k count, then eps = 1 + (2 pi / |q|^2) * that
+    (|q|^2 = 0 taken as 1e-14)."""
+    if len(results) == 0:
+        raise RuntimeError("No results to merge")
+    if len(results) != len(nb_kpoints_per_instance):
+        raise RuntimeError("Number of results and number of k-points per instance do not match")
+    tot = np.array(results[0], dtype=np.float64).copy()
+    for r in results[1:]:
+        tot += np.array(r, dtype=np.float64)
+    ren = 1.0 / float(sum(nb_kpoints_per_instance))
+    out = np.empty_like(tot)
+    for iq, q in enumerate(qpoints):
+        q2 = float(np.sqrt(np.dot(q, q))) ** 2
+        if q2 == 0.0:
+            q2 = 1e-14
+        out[iq] = 1.0 + (2.0 * PI / q2) * (tot[iq] * ren)
+    return out
+
+
+def kramers_matrix(n: int) -> np.ndarray:
+    """create_kramers_matrix (src/EPP/DielectricFunction.cpp:214-228)."""
+    K = np.zeros((n, n))
+    for i in range(n):
+        for j in range(n):
+            if i != j:
+                K[i, j] = float(i) / float(j * j - i * i)
+    return K * (-2.0 / PI)
+
+
+def kramers_kronig(eps_real) -> np.ndarray:
+    """apply_kramers_kronig (src/EPP/DielectricFunction.cpp:230-251): Im = K (Re - 1) per q."""
+    e = np.atleast_2d(np.asarray(eps_real, dtype=np.float64))
+    K = kramers_matrix(e.shape[1])
+    return np.stack([K @ (row - 1.0) for row in e])

@@ -38,7 +38,7 @@ EXPORTED = [
     "uepm_ctx_get_tuning", "uepm_ctx_set_tuning", "uepm_ctx_autotune", "uepm_batch_create", "uepm_batch_destroy",
     "uepm_batch_add", "uepm_batch_clear", "uepm_batch_set_graph", "uepm_batch_run", "uepm_batch_kernels_per_run",
     "uepm_server_create", "uepm_server_destroy", "uepm_server_submit", "uepm_server_wait", "uepm_server_stats",
-    "uepm_server_reset_stats", "uepm_star_expand_device", "uepm_star_operations",
+    "uepm_server_reset_stats", "uepm_star_expand_device", "uepm_star_operations", "uepm_dielectric_sums_device",
 ]
 UEPM_SERVE_VELOCITY = 1
 NOALLOC_SCRATCH_BYTES = 16 << 20
@@ -143,6 +143,8 @@ def load():
             "uepm_server_reset_stats": (C.c_int, [vp]),
             "uepm_star_expand_device": (C.c_int, [vp, vp, vp, vp, C.c_size_t, C.c_int, vp, vp, vp]),
             "uepm_star_operations": (C.c_int, [dp, dp, C.c_size_t, C.POINTER(C.c_uint16), ip]),
+            "uepm_dielectric_sums_device": (C.c_int, [vp, vp, vp, vp, C.c_size_t, C.c_int, C.c_int, C.c_int, vp, C.c_int,
+                                                      C.c_double, vp, vp, vp]),
         }
         for name, (res, args) in sig.items():
             f = getattr(L, name)

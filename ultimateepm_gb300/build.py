@@ -30,7 +30,7 @@ PER_FILE = {"assemble.cu": ["--fmad=false"]}
 CXX_FLAGS = ["-O3", "-std=c++17", "-fPIC", "-Wall", "-I" + INCLUDE, "-I" + CSRC]
 
 CU_SOURCES = ["assemble.cu", "tridiag.cu", "tridiag_reg.cu", "tridiag_cluster.cu", "tridiag_eig.cu", "backtransform.cu", "refine.cu", "capi.cu", "batch.cu", "server.cu", "star.cu", "peak.cu",
-              "noalloc.cu"]
+              "noalloc.cu", "dielectric.cu"]
 CXX_SOURCES = ["host.cpp"]
 
 
