@@ -313,6 +313,7 @@ def run_ours(args):
     if ws == 1 and not args.no_extras:
         out["uneven_batch"] = run_uneven_batch(args)
         out["serve"] = run_serve()
+        out["dielectric"] = run_dielectric(cpu_budget=min(args.cpu_budget, 5.0))
     emit(out)
 
 
@@ -390,6 +391,96 @@ def run_serve(rate: float = 4.0, requests: int = 16, kmax: int = 1000, seed: int
                 "velocities": "central differences, h = 1e-4 (reduced units)", "precision": "mixed",
                 "slots": 4, "hbm_budget_gb": 16})
     return res
+
+
+def run_dielectric(nk: int = 8000, ne: int = 1001, seed: int = 20261203, cpu_budget: float = 5.0):
+    """The dielectric function from the band states (DielectricFunction::compute_dielectric_function
+    for one q): Si Cohen-Bergstresser, basis 137, 16 bands (4 valence x 12 conduction pairs), nk
+    seeded first-zone k-points, q = (0.01, 0, 0), ne energies over 0..10 eV, eta = 0.05, FP64 band
+    states with vectors at k and k + q. Reports k-points/s of the whole call (host k-points in, the
+    [ne] sums out), the sums kernel alone on resident states (CUDA events), and the oracle on a
+    bounded sample of the same workload."""
+    import torch
+
+    from oracle import oracle as O
+    from ultimateepm_gb300 import _native as N
+    from ultimateepm_gb300 import api
+    from ultimateepm_gb300.dielectric import DielectricFunction
+
+    L = N.load()
+    mats = api.Materials()
+    mats.load_material_parameters(PARAM_FILE)
+    si = mats.materials["Si"]
+    G = api.generate_basis_vectors(SHELLS)
+    k = O.sample_first_bz(nk, seed)
+    q = np.array([0.01, 0.0, 0.0])
+    en = np.linspace(0.0, 10.0, ne)
+    eta = 0.05
+    df = DielectricFunction(si, G, NB)
+    df.m_kpoints = k
+    df.set_qpoints([q])
+    df.set_energies(en)
+    df.set_nb_kpoints(nk)
+    df.compute_dielectric_function(eta)  # warm-up (builds, allocations)
+    times = []
+    for _ in range(3):
+        df.m_dielectric_function_real = []
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        df.compute_dielectric_function(eta)
+        torch.cuda.synchronize()
+        times.append(time.perf_counter() - t0)
+    call_s = min(times)
+    # the sums kernel alone, on resident states of the first 2000 k-points
+    m = 2000
+    ctx = api._Context(si, G, False, False, N.UEPM_PREC_FP64)
+    s = torch.cuda.current_stream()
+    sp = C.c_void_p(s.cuda_stream)
+    dev = "cuda"
+    p = lambda t: C.c_void_p(t.data_ptr())
+    dk = torch.from_numpy(k[:m]).to(dev)
+    dkq = dk + torch.from_numpy(q).to(dev)[None, :]
+    Ek = torch.zeros((m, NB), dtype=torch.float64, device=dev)
+    Ekq = torch.zeros_like(Ek)
+    Xk = torch.zeros((m, NB, len(G), 2), dtype=torch.float64, device=dev)
+    Xkq = torch.zeros_like(Xk)
+    st = torch.zeros(m, dtype=torch.int32, device=dev)
+    want = N.UEPM_WANT_VALUES | N.UEPM_WANT_VECTORS
+    N.check(L.uepm_solve_device(ctx.h, p(dk), m, NB, want, p(Ek), p(Xk), None, p(st), sp))
+    N.check(L.uepm_solve_device(ctx.h, p(dkq), m, NB, want, p(Ekq), p(Xkq), None, p(st), sp))
+    den = torch.from_numpy(en).to(dev)
+    sums = torch.zeros(ne, dtype=torch.float64, device=dev)
+    call = lambda: N.check(L.uepm_dielectric_sums_device(p(Xk), p(Xkq), p(Ek), p(Ekq), m, NB, len(G), 4, p(den), ne, eta,
+                                                          None, p(sums), sp))
+    for _ in range(3):
+        call()
+    kt = []
+    for _ in range(5):
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(s)
+        call()
+        b.record(s)
+        b.synchronize()
+        kt.append(a.elapsed_time(b))
+    kernel_ms = min(kt)
+    ctx.close()
+    pairs = 4 * (NB - 4)
+    # the oracle (eigenstates on all host cores, the pair sums in numpy) on a bounded sample
+    mat = O.load_materials(PARAM_FILE)["Si"]
+    Go = O.generate_basis(SHELLS)
+    done, t0 = 0, time.perf_counter()
+    while time.perf_counter() - t0 < cpu_budget and done < nk:
+        O.dielectric_sums(mat, Go, k[done:done + 64], q, NB, en, eta)
+        done += 64
+    cpu_dt = time.perf_counter() - t0
+    return {
+        "value": nk / call_s, "unit": "k-points/s", "ms_per_call": call_s * 1e3,
+        "workload": f"Si Cohen-Bergstresser basis {len(G)}, {NB} bands ({pairs} valence-conduction pairs), {nk} seeded "
+                    f"first-zone k, q = (0.01, 0, 0), {ne} energies 0..10 eV, eta = {eta}, FP64 band states",
+        "sums_kernel": {"ms_per_2000_k": kernel_ms, "pair_energy_terms_per_s": 2000 * pairs * ne / (kernel_ms * 1e-3)},
+        "cpu_baseline": {"value": done / cpu_dt, "unit": "k-points/s", "cores": os.cpu_count() or 1, "kind": "port",
+                         "sample": f"{done} k-points, {cpu_dt:.1f} s (oracle eigenstates on all cores, numpy pair sums)"},
+    }
 
 
 def run_reference(args):
