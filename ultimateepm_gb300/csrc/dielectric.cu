@@ -9,11 +9,12 @@
 //   for each k:  O_cv = |sum_i u_c(k+q)_i u_v(k)_i|^2,  dE_cv = E_c(k+q) - E_v(k)   (c >= first_cond > v)
 //   s_k(w) = sum_{c, v} O_cv [ (dE_cv - w) / ((dE_cv - w)^2 + eta^2) + (dE_cv + w) / ((dE_cv + w)^2 + eta^2) ]
 //   sums(w) += weight_k s_k(w)
-// in FP64, pairs in the reference's order (conduction outer, valence inner). The overlap is the
-// reference's Eigen expression col(c).adjoint().dot(col(v)): dot() conjugates its first operand,
-// which is already the adjoint, so no factor is conjugated. For a real H (the elemental crystals the
-// reference's epsilon driver runs) this equals |<u_c|u_v>|^2; it is kept as written so that complex
-// H gives the reference's numbers too.
+// in FP64, pairs in the reference's order (conduction outer, valence inner), each pair's two
+// fractions over one denominator (rounding-level differences from the reference's two divisions).
+// The overlap is the reference's Eigen expression col(c).adjoint().dot(col(v)): dot() conjugates
+// its first operand, which is already the adjoint, so no factor is conjugated. For a real H (the
+// elemental crystals the reference's epsilon driver runs) this equals |<u_c|u_v>|^2; it is kept as
+// written so that complex H gives the reference's numbers too.
 //
 // Layout. A persistent grid of CTAs takes k-points b, b + grid, ...: the CTA stages the valence rows
 // of X(k) and the conduction rows of X(k+q) in shared memory (coalesced), one warp per overlap
@@ -84,10 +85,11 @@ __global__ void __launch_bounds__(kDfThreads) k_dielectric_sums(const double2* _
                 const double om = en[e];
                 double       s  = 0.0;
                 for (int p = 0; p < P; ++p) {
-                    const double d  = sd[p];
-                    const double f1 = (d - om) / ((d - om) * (d - om) + eta2);
-                    const double f2 = (d + om) / ((d + om) * (d + om) + eta2);
-                    s += so[p] * (f1 + f2);
+                    // the pair over one denominator (one FP64 division instead of two):
+                    // a / (a^2 + eta^2) + b / (b^2 + eta^2) = (a B + b A) / (A B)
+                    const double d = sd[p], a = d - om, b = d + om;
+                    const double A = fma(a, a, eta2), B = fma(b, b, eta2);
+                    s += so[p] * (fma(a, B, b * A) / (A * B));
                 }
                 acc[t] += w * s;
             }
