@@ -452,3 +452,28 @@ def kramers_kronig(eps_real) -> np.ndarray:
     e = np.atleast_2d(np.asarray(eps_real, dtype=np.float64))
     K = kramers_matrix(e.shape[1])
     return np.stack([K @ (row - 1.0) for row in e])
+
+
+def bz_states_dielectric(Ek, Xk, Ekq, Xkq, tetra, signed_volumes, energies, eta, q_si, first_cond=4) -> np.ndarray:
+    """BZ_States::compute_dielectric_function (src/BZ_MESH/bz_states.cpp:93-150) from the vertex
+    eigenstates at k and k + q: per tetrahedron, the four vertices' pair sums times |volume| / 4,
+    then eps = 1 + q_e^2 / (eps_0 |q|^2) / q_e * 2 / (2 pi)^3 * sum (q in SI)."""
+    eps_0 = 8.8541878128e-12  # src/Common/physical_constants.hpp:31
+    en = np.asarray(energies, dtype=np.float64)
+    total = np.zeros(len(en))
+    nb = Ek.shape[1]
+    for t, vol in zip(tetra, signed_volumes):
+        tsum = np.zeros(len(en))
+        for idx in t:
+            for c in range(first_cond, nb):
+                for v in range(first_cond):
+                    ov = abs(np.dot(Xkq[idx, c], Xk[idx, v])) ** 2
+                    d = Ekq[idx, c] - Ek[idx, v]
+                    f1 = (d - en) / ((d - en) * (d - en) + eta * eta)
+                    f2 = (d + en) / ((d + en) * (d + en) + eta * eta)
+                    tsum += ov * (f1 + f2)
+        total += tsum * abs(vol) * 0.25
+    q = np.asarray(q_si, dtype=np.float64)
+    q2 = float(np.sqrt(np.dot(q, q))) ** 2
+    pref = (Q_E * Q_E) / (eps_0 * q2) / Q_E * (2.0 / (2.0 * PI) ** 3)
+    return 1.0 + pref * total

@@ -76,6 +76,59 @@ def read_msh_nodes(path: str) -> tuple[np.ndarray, np.ndarray]:
     raise ValueError(f"{path}: no $Nodes section")
 
 
+def read_msh_tetrahedra(path: str) -> np.ndarray:
+    """Node tags (n x 4) of the 4-node tetrahedra (element type 4) of an ASCII MSH 4.1 or 2.2 file, in
+    file order: the elements gmsh::model::mesh::getElements(dim = 3) returns to MeshBZ
+    (bz_mesh.cpp:106-120)."""
+    with open(path, "r") as f:
+        lines = f.read().splitlines()
+    ver = None
+    i = 0
+    while i < len(lines):
+        t = lines[i].strip()
+        if t == "$MeshFormat":
+            parts = lines[i + 1].split()
+            ver, ftype = float(parts[0]), int(parts[1])
+            if ftype != 0:
+                raise ValueError("binary MSH files are not supported; save the mesh as ASCII")
+            i += 2
+            continue
+        if t == "$Elements":
+            if ver is None:
+                raise ValueError("$Elements before $MeshFormat")
+            i += 1
+            out = []
+            if ver >= 4.0:
+                nblocks = int(lines[i].split()[0])
+                i += 1
+                for _ in range(nblocks):
+                    dim, _, etype, nin = (int(x) for x in lines[i].split()[:4])
+                    i += 1
+                    if dim == 3 and etype == 4:
+                        out.extend([int(x) for x in lines[i + q].split()[1:5]] for q in range(nin))
+                    i += nin
+            else:
+                n = int(lines[i])
+                i += 1
+                for q in range(n):
+                    p = [int(x) for x in lines[i + q].split()]
+                    if p[1] == 4:
+                        out.append(p[3 + p[2]:3 + p[2] + 4])
+            return np.array(out, dtype=np.int64).reshape(-1, 4)
+        i += 1
+    raise ValueError(f"{path}: no $Elements section")
+
+
+def tetra_signed_volumes(positions: np.ndarray, tetra: np.ndarray) -> np.ndarray:
+    """Tetra::compute_signed_volume (mesh_tetra.cpp:128-132): (1/6) e0 . (e1 x e2) with
+    e_j = v_{j+1} - v_0."""
+    p = positions[tetra]
+    e0, e1, e2 = p[:, 1] - p[:, 0], p[:, 2] - p[:, 0], p[:, 3] - p[:, 0]
+    c = np.stack([e1[:, 1] * e2[:, 2] - e1[:, 2] * e2[:, 1], e1[:, 2] * e2[:, 0] - e1[:, 0] * e2[:, 2],
+                  e1[:, 0] * e2[:, 1] - e1[:, 1] * e2[:, 0]], axis=1)
+    return (1.0 / 6.0) * np.einsum("ij,ij->i", e0, c)
+
+
 def _fold_key(kr: np.ndarray, digits: int) -> list[tuple]:
     f = -np.sort(-np.abs(kr), axis=1)  # |k| sorted descending: the wedge representative
     return [tuple(r) for r in np.round(f, digits)]
@@ -91,6 +144,8 @@ class MeshBZ:
         self.iw_vertices: list[int] = []
         self.energies = None
         self.gradients = None
+        self.tetra = np.zeros((0, 4), dtype=np.int64)
+        self.tetra_volumes = np.zeros(0)
 
     # ---- geometry --------------------------------------------------------------------------------
     def si_to_reduced_scale(self) -> float:
@@ -102,6 +157,23 @@ class MeshBZ:
         self.node_tags = tags
         self.positions = xyz * f
         self.filename = filename
+        try:
+            self.set_tetrahedra(read_msh_tetrahedra(filename) - 1)  # vertex = node tag - 1 (bz_mesh.cpp:135-138)
+        except ValueError:
+            self.tetra = np.zeros((0, 4), dtype=np.int64)
+            self.tetra_volumes = np.zeros(0)
+        return self
+
+    def set_tetrahedra(self, vertex_indices: np.ndarray):
+        """Tetrahedra as vertex indices (m x 4); those with |signed volume| < 1e-12 are dropped, as
+        MeshBZ does when it reads them (bz_mesh.cpp:130-146)."""
+        t = np.asarray(vertex_indices, dtype=np.int64).reshape(-1, 4)
+        if len(t) and (t.min() < 0 or t.max() >= len(self.positions)):
+            raise ValueError("tetrahedron vertex index out of range")
+        vol = tetra_signed_volumes(self.positions, t) if len(t) else np.zeros(0)
+        keep = np.abs(vol) >= 1e-12
+        self.tetra = t[keep]
+        self.tetra_volumes = vol[keep]
         return self
 
     def set_vertices(self, k_reduced: np.ndarray):
