@@ -380,16 +380,23 @@ def run_serve(rate: float = 4.0, requests: int = 16, kmax: int = 1000, seed: int
 
     ctxs = make_contexts(N.UEPM_PREC_MIXED)
     srv = Server(ctxs, hbm_budget=16 << 30, slots=4, max_chunk=512)
+    sweep = []
     try:
         run_load(srv, poisson_requests(4, 50.0, seed + 7, len(ctxs), 1, 64), seed=seed + 7)  # warm-up
         res = run_load(srv, poisson_requests(requests, rate, seed, len(ctxs), 1, kmax), seed=seed)
+        # the same request mix at rising offered load (24 requests each): latency against load
+        for q, r in enumerate((16.0, 64.0, 256.0)):
+            s = run_load(srv, poisson_requests(24, r, seed + 11 + q, len(ctxs), 1, kmax), seed=seed + 11 + q)
+            sweep.append({"rate_req_per_s": r, "offered_req_per_s": s["offered_req_per_s"], "p50_ms": s["p50_ms"],
+                          "p99_ms": s["p99_ms"], "k_points_per_s": s["k_points_per_s"], "requests": s["requests"],
+                          "requests_with_nonzero_status": s["requests_with_nonzero_status"]})
     finally:
         srv.close()
         for c in ctxs:
             c.close()
     res.update({"rate_req_per_s": rate, "k_per_request": f"log-uniform 1..{kmax}", "bands": "8..16",
                 "velocities": "central differences, h = 1e-4 (reduced units)", "precision": "mixed",
-                "slots": 4, "hbm_budget_gb": 16})
+                "slots": 4, "hbm_budget_gb": 16, "sweep": sweep})
     return res
 
 
