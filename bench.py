@@ -314,6 +314,7 @@ def run_ours(args):
         out["uneven_batch"] = run_uneven_batch(args)
         out["serve"] = run_serve()
         out["dielectric"] = run_dielectric(cpu_budget=min(args.cpu_budget, 5.0))
+        out["configs_2_3"] = run_configs_2_3()
     emit(out)
 
 
@@ -488,6 +489,63 @@ def run_dielectric(nk: int = 8000, ne: int = 1001, seed: int = 20261203, cpu_bud
         "cpu_baseline": {"value": done / cpu_dt, "unit": "k-points/s", "cores": os.cpu_count() or 1, "kind": "port",
                          "sample": f"{done} k-points, {cpu_dt:.1f} s (oracle eigenstates on all cores, numpy pair sums)"},
     }
+
+
+def run_configs_2_3(seed: int = 20261203):
+    """The other precision cases at bounded sizes, each with FP64 and mixed throughput and the mixed
+    path's per-band max error against the FP64 path: Si with the nonlocal d-channel (basis 137,
+    12 bands, 20000 seeded first-zone k) and Ge with nonlocal wells and spin-orbit (12 shells, order
+    362 complex, 16 bands = 8 Kramers pairs, 2000 k)."""
+    import torch
+
+    from ultimateepm_gb300 import _native as N
+    from ultimateepm_gb300 import api
+    from ultimateepm_gb300.serve import sample_bz
+
+    L = N.load()
+    s = torch.cuda.current_stream()
+    sp = C.c_void_p(s.cuda_stream)
+    p = lambda t: C.c_void_p(t.data_ptr())
+
+    def solve_timed(ctx, k, nb):
+        nk = len(k)
+        dk = torch.from_numpy(np.ascontiguousarray(k)).cuda()
+        dE = torch.zeros((nk, nb), dtype=torch.float64, device="cuda")
+        st = torch.zeros(nk, dtype=torch.int32, device="cuda")
+        call = lambda: N.check(L.uepm_solve_device(ctx.h, p(dk), nk, nb, N.UEPM_WANT_VALUES, p(dE), None, None, p(st), sp))
+        call()
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(s)
+        call()
+        b.record(s)
+        b.synchronize()
+        assert not st.any().item(), "a k-point reported a non-zero status"
+        return dE.cpu().numpy(), a.elapsed_time(b)
+
+    rng = np.random.default_rng(seed)
+    out = {}
+    for name, yaml, sym, shells, nl, soc, nb, nk in (
+            ("config_2", "si-nonlocal-d.yaml", "Si", 10, True, False, 12, 20000),
+            ("config_3", "materials.yaml", "Ge", 12, True, True, 16, 2000)):
+        mats = api.Materials()
+        mats.load_material_parameters(os.path.join(ROOT, "params", yaml))
+        m = mats.materials[sym]
+        G = api.generate_basis_vectors(shells)
+        k = sample_bz(nk, rng)
+        res = {}
+        for prec, tag in ((N.UEPM_PREC_FP64, "fp64"), (N.UEPM_PREC_MIXED, "mixed")):
+            ctx = api._Context(m, G, nl, soc, prec)
+            res[tag] = solve_timed(ctx, k, nb) + (ctx.n,)
+            ctx.close()
+        err = np.abs(res["mixed"][0] - res["fp64"][0]).max(axis=0)
+        out[name] = {
+            "workload": f"{sym} ({yaml}, nonlocal{', spin-orbit' if soc else ''}), {shells} shells, order {res['fp64'][2]}, "
+                        f"{nb} bands, {nk} seeded first-zone k",
+            "fp64_k_points_per_s": nk / (res["fp64"][1] * 1e-3), "mixed_k_points_per_s": nk / (res["mixed"][1] * 1e-3),
+            "mixed_max_err_ev": float(err.max()), "mixed_max_err_ev_per_band": [float(x) for x in err],
+        }
+    return out
 
 
 def run_reference(args):

@@ -7,11 +7,14 @@
 //             LAPACK dstebz's pivot guard and absolute/relative stopping tolerances. Each value is
 //             the j-th smallest eigenvalue of T to about eps * ||T||.
 //   k_invit   inverse iteration (one warp per matrix, one lane per eigenvalue): LU with partial
-//             pivoting of T - lambda I, three solves from a deterministic pseudo-random start,
-//             LAPACK dstein's shift perturbation for (near-)equal eigenvalues and modified
-//             Gram-Schmidt inside clusters (consecutive gaps <= 1e-3 ||T||_1), so degenerate
-//             bands (Kramers pairs with SOC, the Gamma-point triplets) get an orthonormal basis of
-//             their eigenspace. Iteration counts are fixed: nothing here can spin.
+//             pivoting of T - lambda I, three solves (FP64; two in FP32) from a deterministic
+//             pseudo-random start, LAPACK dstein's shift perturbation for close eigenvalues and
+//             modified Gram-Schmidt inside clusters (consecutive gaps <= 1e-3 ||T||_1), so
+//             degenerate bands (Kramers pairs with SOC, the Gamma-point triplets) get an
+//             orthonormal basis of their eigenspace. Groups that are degenerate to rounding
+//             (consecutive gaps below 8 eps ||T||_1) share one shift placed just below the group
+//             instead, and a Gram-Schmidt step that leaves less than 2% of a vector adds two
+//             solves (see k_invit). Iteration counts are bounded: nothing here can spin.
 #include <algorithm>
 
 #include "uepm_common.cuh"
@@ -270,6 +273,7 @@ template <>
 struct InvitIters<float> {
     static constexpr int value = 2;
 };
+constexpr double kGsKeep = 0.02;  // Gram-Schmidt remainder below which two more solves follow
 
 // Work arrays per matrix, each n x LS interleaved by lane (LS = lanes in use, min(nb, 32)): U0, U1
 // (the reciprocal diagonal and the first superdiagonal of U), Lm (the multipliers), Z (the vector; the forward sweep writes its
@@ -323,37 +327,59 @@ __global__ void k_invit(const T* __restrict__ dIn, const T* __restrict__ eIn, co
     const T eps     = num<T>::eps();
     const T ortol   = T(1e-3) * onenrm;
     const T pivtiny = eps * onenrm;
+    // Eigenvalues closer than ptight are one eigenvalue to the working precision (the two members
+    // of a Kramers pair differ by rounding in T). dstein's shifts (the eigenvalue, then + 10 eps
+    // |lambda|) would put every member's shift inside the rounding band of the factorisation, where
+    // the solve returns one rounding-chosen direction of the eigenspace whatever the start vector;
+    // the second member then differs from the first only by rounding and Gram-Schmidt keeps noise
+    // (seen in FP32 as Ritz errors up to 1e-5 eV on the second band of a pair at about one k-point
+    // in a thousand). Instead every member of such a group takes one shift p = ptight below the
+    // group (at most half-way to the eigenvalue below): the solve then stretches the group's
+    // eigenspace evenly, the start vectors keep their directions inside it, Gram-Schmidt keeps
+    // them orthogonal, and the rest of the spectrum still shrinks by p / gap per solve.
+    const T ptight = T(8) * eps * onenrm;
     // largest |z| for which sum z^2 stays finite
     const T zsafe = sizeof(T) == 4 ? T(1e17) : T(1e150);
     bool    bad   = false;
 
-    // carried across groups of 32: the previous (perturbed) shift and cluster start
-    T   prev_lam = T(0);
+    // carried across groups of 32: the previous shift, eigenvalue and cluster start
+    T   prev_lam = T(0), prev_ev = T(0);
     int prev_gs  = 0;
     for (int g0 = 0; g0 < nb; g0 += 32) {
         const int gn = min(32, nb - g0);
         if (lane == 0) {
-            T   pl = prev_lam;
+            T   pl = prev_lam, pe = prev_ev;
             int pg = prev_gs;
             for (int q = 0; q < gn; ++q) {
-                const int j  = g0 + q;
-                T         xj = ev[(size_t)b * ev_ld + j];
-                if (j > 0) {
-                    const T pertol = T(10) * fabs(eps * xj);
-                    if (xj - pl < pertol) xj = pl + pertol;
-                    if (xj - pl > ortol) pg = j;
+                const int  j     = g0 + q;
+                const T    x     = ev[(size_t)b * ev_ld + j];
+                const bool tprev = j > 0 && x - pe < ptight;
+                const bool tnext = j + 1 < nb && ev[(size_t)b * ev_ld + j + 1] - x < ptight;
+                T          xj    = x;
+                if (tprev) {
+                    xj = pl;  // a later member of a degenerate group: the group's shift and cluster
                 } else {
-                    pg = 0;
+                    if (tnext) xj = x - (j > 0 ? min(ptight, T(0.5) * (x - pe)) : ptight);
+                    if (j > 0) {
+                        const T pertol = T(10) * fabs(eps * xj);
+                        if (xj - pl < pertol) xj = pl + pertol;
+                        if (xj - pl > ortol) pg = j;
+                    } else {
+                        pg = 0;
+                    }
                 }
                 s_lam[warp][q] = xj;
                 s_gs[warp][q]  = pg;
                 pl             = xj;
+                pe             = x;
             }
             prev_lam = pl;
+            prev_ev  = pe;
             prev_gs  = pg;
         }
         __syncwarp();
         prev_lam = __shfl_sync(0xffffffffu, prev_lam, 0);
+        prev_ev  = __shfl_sync(0xffffffffu, prev_ev, 0);
         prev_gs  = __shfl_sync(0xffffffffu, prev_gs, 0);
         const bool active = lane < gn;
         const T    lam    = active ? s_lam[warp][lane] : T(0);
@@ -369,8 +395,9 @@ __global__ void k_invit(const T* __restrict__ dIn, const T* __restrict__ eIn, co
             }
         __syncwarp();
 
-        T sc = T(1);  // pending scale of Z
-        for (int it = 0; it < NIT; ++it) {
+        T   sc   = T(1);  // pending scale of Z
+        int need = NIT;   // solves to run (raised after a Gram-Schmidt step that kept little)
+        for (int it = 0; it < need; ++it) {
             if (active) {
                 T rp = AT(Z, 0) * sc;
                 if (it == 0) {
@@ -453,6 +480,7 @@ __global__ void k_invit(const T* __restrict__ dIn, const T* __restrict__ eIn, co
                     for (int i = 0; i < n; ++i) AT(Z, i) *= sc;
                 sc = T(1);
                 __syncwarp();
+                T kept2 = T(1);  // smallest squared norm left by the projections (unit vectors in)
                 for (int q = 0; q < gn; ++q) {
                     const int jq = g0 + q;
                     const int gs = s_gs[warp][q];
@@ -474,10 +502,17 @@ __global__ void k_invit(const T* __restrict__ dIn, const T* __restrict__ eIn, co
                     T ss = T(0);
                     for (int i = lane; i < n; i += 32) ss = fma(Z[(size_t)i * LS + q], Z[(size_t)i * LS + q], ss);
                     ss        = warp_sum(ss);
+                    kept2     = min(kept2, ss);
                     const T r = (ss > T(0)) ? T(1) / sqrt(ss) : T(0);
                     for (int i = lane; i < n; i += 32) Z[(size_t)i * LS + q] *= r;
                     __syncwarp();
                 }
+                // A vector that came out of its solve nearly parallel to an earlier one (the start
+                // vectors' components in a degenerate eigenspace can nearly coincide) keeps only a
+                // small remainder, in which rounding and the components outside the eigenspace are
+                // magnified by 1 / remainder: give it two more solves (at most NIT + 2 in all).
+                // kept2 is warp-uniform (warp sums), so the trip count stays uniform.
+                if (kept2 < T(kGsKeep * kGsKeep)) need = min(NIT + 2, max(need, it + 3));
             }
         }
         // write this group's vectors ([j][i], coalesced over i), with the pending scale
