@@ -493,6 +493,208 @@ __global__ void __launch_bounds__(NT, 4) k_tridiag_fused(S* __restrict__ H, int 
     }
 }
 
+// Deferred variant: every other rank-2 update is held back one step. The pass after an odd step j
+// (reflector v_j formed from column j with both pending updates) is read-only: it accumulates
+// S v_j from the stored matrix S, which still lacks update j-1, and the vector phase corrects it,
+// p_j = S v_j - v_{j-1} (w_{j-1}^H v_j) - w_{j-1} (v_{j-1}^H v_j), with the two dots formed in the
+// previous vector phase. The pass after an even step applies updates j-2 and j-1 together (rank 4)
+// and accumulates the exact product. Per two steps the trailing matrix is read three times and
+// written once instead of read and written twice.
+template <typename S, int NT, int MAXT>
+__global__ void __launch_bounds__(NT, 4)
+    k_tridiag_fused_deferred(S* __restrict__ H, int n, int ld, size_t mstride, typename ST<S>::R* __restrict__ dOut,
+                             typename ST<S>::R* __restrict__ eOut, S* __restrict__ tqOut, int* __restrict__ status,
+                             int batch) {
+    using R          = typename ST<S>::R;
+    constexpr int NW = NT / 32;
+    extern __shared__ __align__(16) unsigned char smraw[];
+    S*        vb   = reinterpret_cast<S*>(smraw);            // [3][n]: v_j in slot j % 3 (v_j[i] <-> row j + 1 + i)
+    S*        wb   = vb + 3 * (size_t)n;                      // [2][n]: w_j in slot j % 2
+    S*        pacc = wb + 2 * (size_t)n;                      // [NW][n] per-warp partials of S v
+    R*        red  = reinterpret_cast<R*>(pacc + (size_t)NW * n);  // [3 NW]: norms | dot re | dot im
+    R*        red2 = red + 3 * NW;                            // [4 NW]: w^H v' re, im | v^H v' re, im
+    __shared__ S s_sc, s_th, s_alpha;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    for (int b = blockIdx.x; b < batch; b += gridDim.x) {
+        __syncthreads();  // shared memory of the previous matrix consumed
+        S*   A   = H + (size_t)b * mstride;
+        R*   dB  = dOut + (size_t)b * n;
+        R*   eB  = eOut + (size_t)b * n;
+        S*   tB  = tqOut + (size_t)b * n;
+        bool bad = false;
+        S    colv[2];
+#pragma unroll
+        for (int k = 0; k < 2; ++k) {
+            const int rr = tid + NT * k;
+            colv[k]      = rr < n ? ldc(A + rr) : ST<S>::zero();
+        }
+        fused_reflector<S, NT>(colv, A, ld, n, 0, dB, eB, tB, vb, red, &s_sc, &s_th, &s_alpha, bad);
+        S th = s_th;
+        for (int j = 0; j <= n - 1; ++j) {
+            const int  mb  = n - 1 - j;  // the block [j+1:, j+1:]
+            const bool odd = (j & 1) != 0;
+            const bool rw  = j >= 2 && !odd;  // apply updates j-2 and j-1
+            const S*   vj  = vb + (size_t)(j % 3) * n;
+            const S*   v1  = vb + (size_t)((j + 2) % 3) * n;  // v_{j-1}
+            const S*   v2  = vb + (size_t)((j + 1) % 3) * n;  // v_{j-2}
+            const S*   w1  = wb + (size_t)((j + 1) & 1) * n;  // w_{j-1}
+            const S*   w2  = wb + (size_t)(j & 1) * n;        // w_{j-2}
+            if (mb >= 1) {
+                S         acc[MAXT];
+#pragma unroll
+                for (int t = 0; t < MAXT; ++t) acc[t] = ST<S>::zero();
+                const int     tn = (mb + 31) >> 5;
+                constexpr int GS = MAXT > 12 ? 4 : (MAXT > 8 ? (MAXT + 1) / 2 : MAXT);
+                for (int C = warp; C < mb; C += NW) {
+                    S*      ac = A + (size_t)(j + 1 + C) * ld + j + 1;
+                    const S vn = vj[C];
+                    S       c2w = ST<S>::zero(), c2v = ST<S>::zero(), c1w = ST<S>::zero(), c1v = ST<S>::zero();
+                    if (rw) {
+                        c2w = w2[C + 2];
+                        c2v = v2[C + 2];
+                        c1w = w1[C + 1];
+                        c1v = v1[C + 1];
+                    }
+#pragma unroll
+                    for (int g = 0; g < MAXT; g += GS) {
+                        S a[GS];
+#pragma unroll
+                        for (int q = 0; q < GS; ++q) {
+                            const int t = g + q, Rr = lane + 32 * t;
+                            a[q]        = (t < MAXT && t < tn && Rr < mb) ? ldc(ac + Rr) : ST<S>::zero();
+                        }
+#pragma unroll
+                        for (int q = 0; q < GS; ++q) {
+                            const int t = g + q, Rr = lane + 32 * t;
+                            if (t < MAXT && t < tn) {  // warp-uniform
+                                if (rw && Rr < mb) {
+                                    S x = cfms_conjb(v2[Rr + 2], c2w, a[q]);
+                                    x   = cfms_conjb(w2[Rr + 2], c2v, x);
+                                    x   = cfms_conjb(v1[Rr + 1], c1w, x);
+                                    x   = cfms_conjb(w1[Rr + 1], c1v, x);
+                                    if (Rr == C) x = ST<S>::make(ST<S>::re(x), R(0));
+                                    stc(ac + Rr, x);
+                                    a[q] = x;
+                                }
+                                acc[t] = cfma(a[q], vn, acc[t]);
+                            }
+                        }
+                    }
+                }
+#pragma unroll
+                for (int t = 0; t < MAXT; ++t) {
+                    const int Rr = lane + 32 * t;
+                    if (t < tn && Rr < mb) pacc[(size_t)warp * n + Rr] = acc[t];
+                }
+            }
+            __syncthreads();
+            const int col = j + 1, m = n - col;
+            if (m < 1) break;
+            // p_j (corrected for the held-back update j-1 after a read-only pass), w_j
+            S d1 = ST<S>::zero(), d2 = ST<S>::zero();
+            if (odd) {
+                R a1 = 0, b1 = 0, a2 = 0, b2 = 0;
+#pragma unroll
+                for (int q = 0; q < NW; ++q) {
+                    a1 += red2[q];
+                    b1 += red2[NW + q];
+                    a2 += red2[2 * NW + q];
+                    b2 += red2[3 * NW + q];
+                }
+                d1 = ST<S>::make(a1, b1);
+                d2 = ST<S>::make(a2, b2);
+            }
+            S wown[2];
+            S dot = ST<S>::zero();
+#pragma unroll
+            for (int k = 0; k < 2; ++k) {
+                const int rr = tid + NT * k;
+                wown[k]      = ST<S>::zero();
+                if (rr < m) {
+                    S p = pacc[rr];
+#pragma unroll
+                    for (int q = 1; q < NW; ++q) p = cadd(p, pacc[(size_t)q * n + rr]);
+                    if (odd) {
+                        p = cfma(ST<S>::neg(v1[rr + 1]), d1, p);
+                        p = cfma(ST<S>::neg(w1[rr + 1]), d2, p);
+                    }
+                    wown[k] = cmul(th, p);
+                    dot     = cfmac(wown[k], vj[rr], dot);
+                }
+            }
+            dot = warp_sum(dot);
+            if (lane == 0) {
+                red[NW + warp]     = ST<S>::re(dot);
+                red[2 * NW + warp] = ST<S>::im(dot);
+            }
+            __syncthreads();
+            R dr = 0, di = 0;
+#pragma unroll
+            for (int q = 0; q < NW; ++q) {
+                dr += red[NW + q];
+                di += red[2 * NW + q];
+            }
+            const S alpha = cscale(cmul(th, ST<S>::make(dr, di)), R(-0.5));
+            S       p0    = pacc[0];
+#pragma unroll
+            for (int q = 1; q < NW; ++q) p0 = cadd(p0, pacc[(size_t)q * n]);
+            if (odd) {
+                p0 = cfma(ST<S>::neg(v1[1]), d1, p0);
+                p0 = cfma(ST<S>::neg(w1[1]), d2, p0);
+            }
+            const S w0  = cfma(alpha, vj[0], cmul(th, p0));
+            const S c1w = odd ? w1[1] : ST<S>::zero(), c1v = odd ? v1[1] : ST<S>::zero();
+            S*      wj  = wb + (size_t)(j & 1) * n;
+#pragma unroll
+            for (int k = 0; k < 2; ++k) {
+                const int rr = tid + NT * k;
+                if (rr < m) {
+                    wown[k] = cfma(alpha, vj[rr], wown[k]);
+                    wj[rr]  = wown[k];
+                    // column col: the held-back update j-1 (odd j), then update j
+                    S x = ldc(A + (size_t)col * ld + col + rr);
+                    if (odd) {
+                        x = cfms_conjb(v1[rr + 1], c1w, x);
+                        x = cfms_conjb(w1[rr + 1], c1v, x);
+                    }
+                    x = cfms_conjb(vj[rr], w0, x);
+                    x = cfms_conjb(wown[k], vj[0], x);
+                    if (rr == 0) x = ST<S>::make(ST<S>::re(x), R(0));
+                    colv[k] = x;
+                } else {
+                    colv[k] = ST<S>::zero();
+                }
+            }
+            S* vnext = vb + (size_t)((j + 1) % 3) * n;
+            fused_reflector<S, NT>(colv, A, ld, n, col, dB, eB, tB, vnext, red, &s_sc, &s_th, &s_alpha, bad);
+            th = s_th;
+            if (!odd && m >= 2) {
+                // the dots the next (odd) step corrects with: w_j^H v_{j+1} and v_j^H v_{j+1} over rows >= j + 2
+                S e1 = ST<S>::zero(), e2 = ST<S>::zero();
+#pragma unroll
+                for (int k = 0; k < 2; ++k) {
+                    const int rr = tid + NT * k;
+                    if (rr >= 1 && rr < m) {
+                        const S vn = vnext[rr - 1];
+                        e1         = cfmac(wown[k], vn, e1);
+                        e2         = cfmac(vj[rr], vn, e2);
+                    }
+                }
+                e1 = warp_sum(e1);
+                e2 = warp_sum(e2);
+                if (lane == 0) {
+                    red2[warp]          = ST<S>::re(e1);
+                    red2[NW + warp]     = ST<S>::im(e1);
+                    red2[2 * NW + warp] = ST<S>::re(e2);
+                    red2[3 * NW + warp] = ST<S>::im(e2);
+                }
+            }
+        }
+        bad = __syncthreads_or(bad);
+        if (tid == 0 && bad && status) atomicOr(status + b, 2);  // UEPM_K_NONFINITE
+    }
+}
+
 static int sm_count() {
     static int sms = 0;
     if (!sms) {
@@ -529,13 +731,14 @@ static void tridiag_launch_t(S* H, int n, int ld, size_t mstride, typename ST<S>
     count_launch();
 }
 
-template <typename S, int MAXT>
+template <typename S, int MAXT, bool DEFER = false>
 static void fused_launch_t(S* H, int n, int ld, size_t mstride, typename ST<S>::R* d, typename ST<S>::R* e, S* tq,
                            int* status, int batch, cudaStream_t s, int ctas_per_sm) {
     using R           = typename ST<S>::R;
     constexpr int NT  = 256;
-    const size_t  smem = sizeof(S) * (size_t)(3 + NT / 32) * n + sizeof(R) * 3 * (NT / 32);
-    auto          kern = k_tridiag_fused<S, NT, MAXT>;
+    const size_t  smem = DEFER ? sizeof(S) * (size_t)(5 + NT / 32) * n + sizeof(R) * 7 * (NT / 32)
+                               : sizeof(S) * (size_t)(3 + NT / 32) * n + sizeof(R) * 3 * (NT / 32);
+    auto          kern = DEFER ? k_tridiag_fused_deferred<S, NT, MAXT> : k_tridiag_fused<S, NT, MAXT>;
     if (smem > 48 * 1024) cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     // matrices in flight as for the unfused kernel (L2 budget, at least 4 per SM), capped at the
     // kernel's occupancy
@@ -578,16 +781,25 @@ void launch_tridiag(S* H, int n, int ld, size_t mstride, typename ST<S>::R* d, t
     // vs 112.0)
     constexpr bool F32 = sizeof(typename ST<S>::R) == 4;
     if (variant == 3 && launch_tridiag_cluster<S>(H, n, ld, mstride, d, e, tq, status, batch, s, cluster)) return;
-    // FP32 matrices reduced from L2/DRAM: the fused kernel (one pass per step; Ge SOC n = 362:
-    // 142 vs 261 ms per 2000 k for the unfused kernel)
+    // FP32 matrices reduced from L2/DRAM: the fused kernels (one pass per step, 4; every other
+    // update deferred, 3 passes per two steps, 5 and automatic). Reduction time per 2000 k: Ge SOC
+    // n = 362 222 ms unfused, 102.7 fused, 81.3 deferred; GaP SOC n = 458 115.3 -> 99.2 ms.
     if constexpr (F32) {
         const bool auto_fused = variant == 0 && !use_smem<S>(n);
-        if ((variant == 4 || auto_fused) && n <= 512) {
+        if (variant == 4 && n <= 512) {
             if (n <= 129) fused_launch_t<S, 4>(H, n, ld, mstride, d, e, tq, status, batch, s, ctas_per_sm);
             else if (n <= 161) fused_launch_t<S, 5>(H, n, ld, mstride, d, e, tq, status, batch, s, ctas_per_sm);
             else if (n <= 257) fused_launch_t<S, 8>(H, n, ld, mstride, d, e, tq, status, batch, s, ctas_per_sm);
             else if (n <= 385) fused_launch_t<S, 12>(H, n, ld, mstride, d, e, tq, status, batch, s, ctas_per_sm);
             else fused_launch_t<S, 16>(H, n, ld, mstride, d, e, tq, status, batch, s, ctas_per_sm);
+            return;
+        }
+        if ((variant == 5 || auto_fused) && n <= 512) {
+            if (n <= 129) fused_launch_t<S, 4, true>(H, n, ld, mstride, d, e, tq, status, batch, s, ctas_per_sm);
+            else if (n <= 161) fused_launch_t<S, 5, true>(H, n, ld, mstride, d, e, tq, status, batch, s, ctas_per_sm);
+            else if (n <= 257) fused_launch_t<S, 8, true>(H, n, ld, mstride, d, e, tq, status, batch, s, ctas_per_sm);
+            else if (n <= 385) fused_launch_t<S, 12, true>(H, n, ld, mstride, d, e, tq, status, batch, s, ctas_per_sm);
+            else fused_launch_t<S, 16, true>(H, n, ld, mstride, d, e, tq, status, batch, s, ctas_per_sm);
             return;
         }
     }

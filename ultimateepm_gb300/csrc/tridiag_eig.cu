@@ -13,8 +13,8 @@
 //             degenerate bands (Kramers pairs with SOC, the Gamma-point triplets) get an
 //             orthonormal basis of their eigenspace. Groups that are degenerate to rounding
 //             (consecutive gaps below 8 eps ||T||_1) share one shift placed just below the group
-//             instead, and a Gram-Schmidt step that leaves less than 2% of a vector adds two
-//             solves (see k_invit). Iteration counts are bounded: nothing here can spin.
+//             instead, and a Gram-Schmidt step that leaves little of a vector adds solves (see
+//             k_invit). Iteration counts are bounded: nothing here can spin.
 #include <algorithm>
 
 #include "uepm_common.cuh"
@@ -273,7 +273,8 @@ template <>
 struct InvitIters<float> {
     static constexpr int value = 2;
 };
-constexpr double kGsKeep = 0.02;  // Gram-Schmidt remainder below which two more solves follow
+constexpr double kGsKeep   = 0.02;  // Gram-Schmidt remainder below which two more solves follow
+constexpr double kGsSettle = 0.5;   // remainder of the last step below which one more follows
 
 // Work arrays per matrix, each n x LS interleaved by lane (LS = lanes in use, min(nb, 32)): U0, U1
 // (the reciprocal diagonal and the first superdiagonal of U), Lm (the multipliers), Z (the vector; the forward sweep writes its
@@ -333,11 +334,15 @@ __global__ void k_invit(const T* __restrict__ dIn, const T* __restrict__ eIn, co
     // the solve returns one rounding-chosen direction of the eigenspace whatever the start vector;
     // the second member then differs from the first only by rounding and Gram-Schmidt keeps noise
     // (seen in FP32 as Ritz errors up to 1e-5 eV on the second band of a pair at about one k-point
-    // in a thousand). Instead every member of such a group takes one shift p = ptight below the
-    // group (at most half-way to the eigenvalue below): the solve then stretches the group's
-    // eigenspace evenly, the start vectors keep their directions inside it, Gram-Schmidt keeps
-    // them orthogonal, and the rest of the spectrum still shrinks by p / gap per solve.
-    const T ptight = T(8) * eps * onenrm;
+    // in a thousand). Instead every member of such a group takes one shift p below the group,
+    // p = max(8 eps ||T||_1, 2 x the group's spread) and at most half-way to the eigenvalue
+    // below: the solve then stretches the group's eigenspace nearly evenly (by at most 1.5x
+    // between members), the start vectors keep their directions inside it, Gram-Schmidt keeps
+    // them orthogonal, and the rest of the spectrum still shrinks by p / gap per solve. (Detecting
+    // groups up to 64 eps ||T||_1 was tried: it also grouped the genuinely split pairs of
+    // zinc-blende crystals with spin-orbit, whose larger shared offsets left up to 2e-8 eV.)
+    const T ptight = T(8) * eps * onenrm;  // consecutive gaps below this form a group
+    const T poff   = ptight;               // smallest offset of a group's shared shift
     // largest |z| for which sum z^2 stays finite
     const T zsafe = sizeof(T) == 4 ? T(1e17) : T(1e150);
     bool    bad   = false;
@@ -359,7 +364,12 @@ __global__ void k_invit(const T* __restrict__ dIn, const T* __restrict__ eIn, co
                 if (tprev) {
                     xj = pl;  // a later member of a degenerate group: the group's shift and cluster
                 } else {
-                    if (tnext) xj = x - (j > 0 ? min(ptight, T(0.5) * (x - pe)) : ptight);
+                    if (tnext) {  // the first member: the group's spread, then its shift
+                        int jl = j + 1;
+                        while (jl + 1 < nb && ev[(size_t)b * ev_ld + jl + 1] - ev[(size_t)b * ev_ld + jl] < ptight) ++jl;
+                        const T p = max(poff, T(2) * (ev[(size_t)b * ev_ld + jl] - x));
+                        xj        = x - (j > 0 ? min(p, T(0.5) * (x - pe)) : p);
+                    }
                     if (j > 0) {
                         const T pertol = T(10) * fabs(eps * xj);
                         if (xj - pl < pertol) xj = pl + pertol;
@@ -510,9 +520,12 @@ __global__ void k_invit(const T* __restrict__ dIn, const T* __restrict__ eIn, co
                 // A vector that came out of its solve nearly parallel to an earlier one (the start
                 // vectors' components in a degenerate eigenspace can nearly coincide) keeps only a
                 // small remainder, in which rounding and the components outside the eigenspace are
-                // magnified by 1 / remainder: give it two more solves (at most NIT + 2 in all).
-                // kept2 is warp-uniform (warp sums), so the trip count stays uniform.
+                // magnified by 1 / remainder: give it two more solves. A last step that still
+                // removes most of a vector (close groups still turning into each other) gets one
+                // more. At most NIT + 2 solves in all; kept2 is warp-uniform (warp sums), so the
+                // trip count stays uniform.
                 if (kept2 < T(kGsKeep * kGsKeep)) need = min(NIT + 2, max(need, it + 3));
+                else if (it == need - 1 && kept2 < T(kGsSettle * kGsSettle)) need = min(NIT + 2, it + 2);
             }
         }
         // write this group's vectors ([j][i], coalesced over i), with the pending scale

@@ -24,8 +24,9 @@ void launch_assemble(const DevParams& P, const cx<double>* Vloc, const double2* 
 // variant: 0 automatic, 1 register-resident (FP32 real, n <= tridiag_reg_max_n()), 2 one CTA per
 // matrix (shared memory where the matrix fits, else global memory with a persistent grid), 3 one
 // thread-block cluster per matrix (tridiag_cluster.cu), 4 one CTA per matrix in global memory with
-// each step's update fused into the next step's product (FP32, n <= 512). Automatic: 1 where it
-// applies, 4 for the other FP32 matrices beyond the on-chip sizes, else 2. ctas_per_sm (0: automatic) caps the
+// each step's update fused into the next step's product (FP32, n <= 512), 5 the same with every
+// other update deferred to the next pass. Automatic: 1 where it applies, 5 for the other FP32
+// matrices beyond the on-chip sizes, else 2. ctas_per_sm (0: automatic) caps the
 // persistent grid of the global-memory kernels; cluster (0: automatic) is the cluster size of
 // variant 3.
 template <typename S>
