@@ -494,8 +494,9 @@ def run_dielectric(nk: int = 8000, ne: int = 1001, seed: int = 20261203, cpu_bud
 def run_configs_2_3(seed: int = 20261203):
     """The other precision cases at bounded sizes, each with FP64 and mixed throughput and the mixed
     path's per-band max error against the FP64 path: Si with the nonlocal d-channel (basis 137,
-    12 bands, 20000 seeded first-zone k) and Ge with nonlocal wells and spin-orbit (12 shells, order
-    362 complex, 16 bands = 8 Kramers pairs, 2000 k)."""
+    12 bands, 20000 seeded first-zone k), InP with square d-wells (basis 113, complex) and Ge with
+    the gaussian d-well (basis 181, real) at the same sizes, and Ge with nonlocal wells and
+    spin-orbit (12 shells, order 362 complex, 16 bands = 8 Kramers pairs, 2000 k)."""
     import torch
 
     from ultimateepm_gb300 import _native as N
@@ -527,6 +528,8 @@ def run_configs_2_3(seed: int = 20261203):
     out = {}
     for name, yaml, sym, shells, nl, soc, nb, nk in (
             ("config_2", "si-nonlocal-d.yaml", "Si", 10, True, False, 12, 20000),
+            ("config_2_inp", "materials.yaml", "InP", 9, True, False, 12, 20000),
+            ("config_2_ge", "materials.yaml", "Ge", 12, True, False, 12, 20000),
             ("config_3", "materials.yaml", "Ge", 12, True, True, 16, 2000)):
         mats = api.Materials()
         mats.load_material_parameters(os.path.join(ROOT, "params", yaml))

@@ -126,15 +126,15 @@ __global__ void k_rows(const DevParams P, const double* __restrict__ kpts, const
     R[RF_KY] = K[1];
     R[RF_KZ] = K[2];
     R[RF_NK] = nK;
-    if (P.nl) {
+    if (P.nl) {  // the cation's values only where its parameters differ (nl_element reads them then)
         if (P.has_R0a) sph_triple(0, nK * P.R0a, R + RF_J0A);
-        if (P.has_R0c) sph_triple(0, nK * P.R0c, R + RF_J0C);
+        if (P.has_R0c && !P.same_nl) sph_triple(0, nK * P.R0c, R + RF_J0C);
         if (P.square) {
             if (P.has_A2a) sph_triple(2, nK * P.R2a, R + RF_J2A);
-            if (P.has_A2c) sph_triple(2, nK * P.R2c, R + RF_J2C);
+            if (P.has_A2c && !P.same_nl) sph_triple(2, nK * P.R2c, R + RF_J2C);
         } else {
             R[RF_GEA] = exp(-0.25 * (nK * nK) * P.R2a * P.R2a);
-            R[RF_GEC] = exp(-0.25 * (nK * nK) * P.R2c * P.R2c);
+            if (!P.same_nl) R[RF_GEC] = exp(-0.25 * (nK * nK) * P.R2c * P.R2c);
         }
     }
     if (P.soc) {
@@ -143,12 +143,17 @@ __global__ void k_rows(const DevParams P, const double* __restrict__ kpts, const
     }
 }
 
-// F_l_function (Material.cpp:87-109) from per-row Bessel triples ja (row i) and jb (row j).
-__device__ __forceinline__ double F_l(int l, double n1, double n2, const double* ja, const double* jb, double R2,
-                                      double R3h, double R3t) {
+// F_l_function (Material.cpp:87-109) from per-row Bessel triples ja (row i) and jb (row j). The
+// branch (|n1 - n2| > 1e-4, evaluated on bit-identical |K|) is the reference's; in the first branch
+// R^2 / (n1^2 - n2^2) is taken as R^2 times the reciprocal inv = 1 / (n1^2 - n2^2) that all F_l
+// terms of the element share (one FP64 division instead of one per term; the product differs from
+// the quotient by at most an ulp).
+__device__ __forceinline__ bool F_l_far(double n1, double n2) { return fabs(n1 - n2) > 1.0e-4; }
+__device__ __forceinline__ double F_l(int l, double n1, double n2, bool far, double inv, const double* ja, const double* jb,
+                                      double R2, double R3h, double R3t) {
     constexpr double EPSILON = 1.0e-4;
-    if (fabs(n1 - n2) > EPSILON) {
-        const double pre = R2 / (n1 * n1 - n2 * n2);
+    if (far) {
+        const double pre = R2 * inv;
         const double F   = n1 * ja[2] * jb[1] - n2 * jb[2] * ja[1];
         return pre * F;
     } else if (n1 > EPSILON) {
@@ -159,7 +164,9 @@ __device__ __forceinline__ double F_l(int l, double n1, double n2, const double*
 }
 
 // compute_pseudopotential_non_local_correction (Material.cpp:139-208); (pc, ps) = cos, sin of the
-// structure phase 2 pi (tau/a).(G_i - G_j).
+// structure phase 2 pi (tau/a).(G_i - G_j). Where anion and cation carry the same parameters their
+// two terms are equal bit for bit (the same operations on the same values), so the cation's is not
+// recomputed: Vs = (Va + Va) / 2 = Va and Vas = 0 exactly.
 __device__ cx<double> nl_element(const DevParams& P, const double* Ri, const double* Rj, double pc, double ps) {
     const double n1  = Ri[RF_NK], n2 = Rj[RF_NK];
     const double dp  = Ri[RF_KX] * Rj[RF_KX] + Ri[RF_KY] * Rj[RF_KY] + Ri[RF_KZ] * Rj[RF_KZ];
@@ -167,15 +174,17 @@ __device__ cx<double> nl_element(const DevParams& P, const double* Ri, const dou
     const double ca  = (np < 1.0e-13) ? 1.0 : dp / (n1 * n2);
     const double lg2 = 0.5 * (3 * ca * ca - 1);
     const double t   = n1 * n2 - P.kF2;
+    const bool   far = F_l_far(n1, n2);
+    const double inv = far ? 1.0 / (n1 * n1 - n2 * n2) : 0.0;
 
     double       Va  = 0.0;
     const double A0a = P.alpha0a + P.nl_df * P.beta0a * t;
-    const double F0a = P.has_R0a ? F_l(0, n1, n2, Ri + RF_J0A, Rj + RF_J0A, P.R0a2, P.R0a3h, P.R0a3t) : 0.0;
+    const double F0a = P.has_R0a ? F_l(0, n1, n2, far, inv, Ri + RF_J0A, Rj + RF_J0A, P.R0a2, P.R0a3h, P.R0a3t) : 0.0;
     Va               = Va + P.Vpre * A0a * F0a;
     if (P.has_A2a) {
         double V2;
         if (P.square) {
-            const double F2 = F_l(2, n1, n2, Ri + RF_J2A, Rj + RF_J2A, P.R2a2, P.R2a3h, 0.0);
+            const double F2 = F_l(2, n1, n2, far, inv, Ri + RF_J2A, Rj + RF_J2A, P.R2a2, P.R2a3h, 0.0);
             V2              = P.Vpre * P.A2a * 5 * lg2 * F2;
         } else {
             const double arg = 0.5 * (P.R2a * P.R2a) * n1 * n2;
@@ -184,14 +193,15 @@ __device__ cx<double> nl_element(const DevParams& P, const double* Ri, const dou
         }
         Va = Va + V2;
     }
+    if (P.same_nl) return mk(pc * Va, ps * 0.0);
     double       Vc  = 0.0;
-    const double F0c = P.has_R0c ? F_l(0, n1, n2, Ri + RF_J0C, Rj + RF_J0C, P.R0c2, P.R0c3h, P.R0c3t) : 0.0;
+    const double F0c = P.has_R0c ? F_l(0, n1, n2, far, inv, Ri + RF_J0C, Rj + RF_J0C, P.R0c2, P.R0c3h, P.R0c3t) : 0.0;
     const double A0c = P.alpha0c + P.beta0c * P.nl_df * t;
     Vc               = Vc + P.Vpre * A0c * F0c;
     if (P.has_A2c) {
         double V2;
         if (P.square) {
-            const double F2 = F_l(2, n1, n2, Ri + RF_J2C, Rj + RF_J2C, P.R2c2, P.R2c3h, 0.0);
+            const double F2 = F_l(2, n1, n2, far, inv, Ri + RF_J2C, Rj + RF_J2C, P.R2c2, P.R2c3h, 0.0);
             V2              = P.Vpre * P.A2c * 5 * lg2 * F2;
         } else {
             const double arg = 0.5 * (P.R2c * P.R2c) * n1 * n2;

@@ -443,6 +443,7 @@ int uepm_ctx_create(const uepm_material* mat, const int32_t* G, int N, uint32_t 
     P.has_R0c = (mat->R0_cation != 0.0);
     P.has_A2a = (mat->A2_anion != 0.0);
     P.has_A2c = (mat->A2_cation != 0.0);
+    P.same_nl = same_nl ? 1 : 0;
     P.R0a2 = pow(P.R0a, 2.0);
     P.R0c2 = pow(P.R0c, 2.0);
     P.R2a2 = pow(P.R2a, 2.0);

@@ -785,7 +785,11 @@ void launch_tridiag(S* H, int n, int ld, size_t mstride, typename ST<S>::R* d, t
     // update deferred, 3 passes per two steps, 5 and automatic). Reduction time per 2000 k: Ge SOC
     // n = 362 222 ms unfused, 102.7 fused, 81.3 deferred; GaP SOC n = 458 115.3 -> 99.2 ms.
     if constexpr (F32) {
-        const bool auto_fused = variant == 0 && !use_smem<S>(n);
+        // automatic: the deferred kernel for every FP32 order beyond the register kernel, also where
+        // the matrix would fit shared memory (2000 k: Ge nonlocal n = 181 real 5.85 ms against 14.3
+        // for the shared-memory kernel; InP n = 113 complex 2.37 against 3.27; GaAs n = 89 complex
+        // 1.45 against 1.70)
+        const bool auto_fused = variant == 0;
         if (variant == 4 && n <= 512) {
             if (n <= 129) fused_launch_t<S, 4>(H, n, ld, mstride, d, e, tq, status, batch, s, ctas_per_sm);
             else if (n <= 161) fused_launch_t<S, 5>(H, n, ld, mstride, d, e, tq, status, batch, s, ctas_per_sm);

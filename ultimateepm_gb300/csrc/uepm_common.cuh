@@ -264,6 +264,7 @@ struct DevParams {
     int soc;      // spin-orbit blocks on
     int square;   // nonlocal well: 1 square, 0 gaussian
     int has_R0a, has_R0c, has_A2a, has_A2c;
+    int same_nl;  // anion and cation carry the same nonlocal parameters (their terms are equal)
     double kin_pref;      // two_pi_over_a * two_pi_over_a * diag_factor      (Hamiltonian.cpp:68-72)
     double grad_pref;     // 2 * diag_factor * (2pi/a)^2                      (Hamiltonian.cpp:167)
     double frac_to_phys;  // 1 / (2pi/a)                                      (Hamiltonian.cpp:190)

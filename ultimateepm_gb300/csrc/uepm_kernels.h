@@ -26,7 +26,7 @@ void launch_assemble(const DevParams& P, const cx<double>* Vloc, const double2* 
 // thread-block cluster per matrix (tridiag_cluster.cu), 4 one CTA per matrix in global memory with
 // each step's update fused into the next step's product (FP32, n <= 512), 5 the same with every
 // other update deferred to the next pass. Automatic: 1 where it applies, 5 for the other FP32
-// matrices beyond the on-chip sizes, else 2. ctas_per_sm (0: automatic) caps the
+// matrices up to n = 512, else 2. ctas_per_sm (0: automatic) caps the
 // persistent grid of the global-memory kernels; cluster (0: automatic) is the cluster size of
 // variant 3.
 template <typename S>
