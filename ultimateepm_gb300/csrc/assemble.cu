@@ -234,32 +234,11 @@ __device__ void soc_element(const DevParams& P, const double* Ri, const double* 
     s[3] = mk((-cz) * phr - 0.0 * phi, (-cz) * phi + 0.0 * phr);
 }
 
-// Element writers: the real path stores only the real part (its imaginary part is exactly zero).
-__device__ __forceinline__ void put(double* p, cx<double> h) { *p = h.x; }
-__device__ __forceinline__ void put(cx<double>* p, cx<double> h) { *p = h; }
-__device__ __forceinline__ void put(float* p, cx<double> h) { *p = (float)h.x; }
-__device__ __forceinline__ void put(cx<float>* p, cx<double> h) { *p = mk((float)h.x, (float)h.y); }
 __device__ __forceinline__ ds2 split_fp32(double v) {
     const float hi = __double2float_rn(v);
     return ds2{hi, __double2float_rn(v - (double)hi)};
 }
-__device__ __forceinline__ void put(ds2* p, cx<double> h) { *p = split_fp32(h.x); }
-__device__ __forceinline__ void put(ds4* p, cx<double> h) {
-    const ds2 r = split_fp32(h.x), i = split_fp32(h.y);
-    *p = ds4{r.hi, r.lo, i.hi, i.lo};
-}
 __device__ __forceinline__ cx<double> conjd(cx<double> a) { return mk(a.x, -a.y); }
-
-// Writes element (r, c) of the full matrix and, when r != c, its Hermitian mirror (c, r).
-template <typename SO, typename SF>
-__device__ __forceinline__ void put_pair(SO* Hb, SF* Fb, int ld, int r, int c, cx<double> h) {
-    put(Hb + (size_t)c * ld + r, h);
-    if (Fb) put(Fb + (size_t)c * ld + r, h);
-    if (r != c) {
-        put(Hb + (size_t)r * ld + c, conjd(h));
-        if (Fb) put(Fb + (size_t)r * ld + c, conjd(h));
-    }
-}
 
 // Element (i, j), i >= j, of the scalar N x N problem: local form factor, kinetic diagonal and the
 // nonlocal correction, in the reference's order of operations.
@@ -305,6 +284,23 @@ __device__ __forceinline__ float copy32(ds2 v) { return v.hi; }
 __device__ __forceinline__ cx<float> copy32(ds4 v) { return mk(v.rhi, v.ihi); }
 __device__ __forceinline__ float copy32(double v) { return (float)v; }
 __device__ __forceinline__ cx<float> copy32(cx<double> v) { return mk((float)v.x, (float)v.y); }
+
+// Writes element (r, c) of the full matrix and, when r != c, its Hermitian mirror (c, r). The
+// element is converted to its stored form once; the mirror and the FP32 copy are taken from that
+// form (a sign flip, the hi parts), the same values as converting each separately, since rounding
+// commutes with negation (conversions run at the FP64 rate).
+template <typename SO, typename SF>
+__device__ __forceinline__ void put_pair(SO* Hb, SF* Fb, int ld, int r, int c, cx<double> h) {
+    const SO v = stored(Hb, h);
+    Hb[(size_t)c * ld + r] = v;
+    if (Fb) Fb[(size_t)c * ld + r] = copy32(v);
+    if (r != c) {
+        const SO w = conj_stored(v);
+        Hb[(size_t)r * ld + c] = w;
+        if (Fb) Fb[(size_t)r * ld + c] = copy32(w);
+    }
+}
+
 
 // Without spin-orbit coupling: one CTA per 32 x 32 tile of the lower triangle, 32 x 8 threads, four
 // elements per thread. The tile is written directly (coalesced down its columns) and, through a

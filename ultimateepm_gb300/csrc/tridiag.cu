@@ -783,7 +783,7 @@ void launch_tridiag(S* H, int n, int ld, size_t mstride, typename ST<S>::R* d, t
     if (variant == 3 && launch_tridiag_cluster<S>(H, n, ld, mstride, d, e, tq, status, batch, s, cluster)) return;
     // FP32 matrices reduced from L2/DRAM: the fused kernels (one pass per step, 4; every other
     // update deferred, 3 passes per two steps, 5 and automatic). Reduction time per 2000 k: Ge SOC
-    // n = 362 222 ms unfused, 102.7 fused, 81.3 deferred; GaP SOC n = 458 115.3 -> 99.2 ms.
+    // n = 362 222 ms unfused, 102.7 fused, 81.3 deferred; GaP SOC n = 458 230.6 -> 198.3 ms.
     if constexpr (F32) {
         // automatic: the deferred kernel for every FP32 order beyond the register kernel, also where
         // the matrix would fit shared memory (2000 k: Ge nonlocal n = 181 real 5.85 ms against 14.3
