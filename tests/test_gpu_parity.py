@@ -60,6 +60,7 @@ CASES = {
     "alas_local_169": ("AlAs", 11, False, False),
     "sn_nl_229": ("Sn", 13, True, False),
     "gap_soc_89": ("GaP", 8, False, True),
+    "ge_nl_181": ("Ge", 12, True, False),
 }
 
 
@@ -94,7 +95,8 @@ def test_assembly_matches_oracle(gpu, oracle, mats, case):
 @pytest.mark.parametrize("case,nb,nk", [("si_cb_local_137", 16, 40), ("si_cb_local_137_cx", 16, 40),
                                         ("si_d_nonlocal_137", 12, 24), ("si_d_nonlocal_137_cx", 12, 24),
                                         ("ge_nl_soc_181", 16, 6), ("gaas_nl_soc_89", 16, 12), ("inp_nl_113", 12, 16),
-                                        ("alas_local_169", 16, 12), ("sn_nl_229", 12, 6), ("gap_soc_89", 16, 12)])
+                                        ("alas_local_169", 16, 12), ("sn_nl_229", 12, 6), ("gap_soc_89", 16, 12),
+                                        ("ge_nl_181", 12, 6)])
 def test_fp64_eigenvalues_match_oracle(gpu, oracle, mats, case, nb, nk):
     key, shells, nl, soc, fcx = _case(case)
     G = oracle.generate_basis(shells)
@@ -148,11 +150,12 @@ def test_fp64_vectors_and_gradients_match_oracle(gpu, oracle, mats, case, nb):
 
 @pytest.mark.parametrize("case,nb,nk", [("si_cb_local_137", 16, 60), ("si_cb_local_137_cx", 16, 60),
                                         ("si_d_nonlocal_137", 12, 30), ("ge_nl_soc_181", 16, 8), ("gaas_nl_soc_89", 16, 12),
-                                        ("alas_local_169", 16, 12), ("sn_nl_229", 16, 10)])
+                                        ("alas_local_169", 16, 12), ("sn_nl_229", 16, 10), ("ge_nl_181", 12, 10)])
 def test_mixed_precision_eigenvalues_within_1e6(gpu, oracle, mats, case, nb, nk):
     """Covers the automatic FP32 reductions: register-resident (Si, AlAs 169) and the deferred
-    global-memory kernel for complex (Ge SOC n = 362, GaAs SOC 178) and real (Sn 229) matrices;
-    the shared-memory and plain fused kernels are tuning choices, covered in test_batch."""
+    global-memory kernel for complex (Ge SOC n = 362, GaAs SOC 178) and real (Ge 181, which would
+    fit shared memory, and Sn 229) matrices; the other kernels are tuning choices (below and in
+    test_batch)."""
     key, shells, nl, soc, fcx = _case(case)
     G = oracle.generate_basis(shells)
     ks = _kset(oracle, 31, nk)
@@ -161,6 +164,22 @@ def test_mixed_precision_eigenvalues_within_1e6(gpu, oracle, mats, case, nb, nk)
     assert not st.any()
     err = np.abs(E - Eo).max()
     assert err <= MIXED_TOL, f"{case}: mixed max |dE| = {err:.3e} eV"
+
+
+@pytest.mark.parametrize("reduction", [2, 3, 4, 5])
+def test_mixed_precision_complex_reductions(gpu, oracle, mats, reduction):
+    """Every FP32 reduction kernel on a complex matrix (InP with nonlocal wells, n = 113, which fits
+    shared memory): 2 shared memory, 3 cluster, 4 fused, 5 deferred."""
+    key, shells, nl, soc, _ = _case("inp_nl_113")
+    G = oracle.generate_basis(shells)
+    ks = _kset(oracle, 37, 10)
+    ctx = _ctx(mats[key], G, nl, soc, N.UEPM_PREC_MIXED)
+    N.check(gpu.uepm_ctx_set_tuning(ctx.h, C.byref(N.UepmTuning(reduction=reduction))))
+    E, _, _, st = ctx.solve(ks, 12)
+    Eo = oracle.band_structure(mats[key], G, ks, 12, nl=nl, soc=soc)["E"]
+    assert not st.any()
+    err = np.abs(E - Eo).max()
+    assert err <= MIXED_TOL, f"reduction {reduction}: mixed max |dE| = {err:.3e} eV"
 
 
 def test_mixed_precision_on_the_2000_point_path(gpu, oracle, mats):
