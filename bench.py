@@ -251,7 +251,7 @@ def run_ours(args):
     pipe_of = {"tridiag_fp32": "fp32", "backtransform": "fp32"}
     # DRAM bytes per launch of the reduction on this 2000-matrix workload: dram__bytes_read.sum +
     # dram__bytes_write.sum from one ncu capture of the same kernels (ncu cannot run inside a bench)
-    traffic = {"tridiag_fp32": 192.3e6, "tridiag_fp64": 9.108e9}
+    traffic = {"tridiag_fp32": 83.66e6, "tridiag_fp64": 9.108e9}
     peak64 = C.c_double()
     peak32 = C.c_double()
     N.check(L.uepm_measure_peak(N.UEPM_PREC_FP64, C.byref(peak64)))

@@ -15,6 +15,7 @@
 #include <cstring>
 #include <mutex>
 #include <string>
+#include <type_traits>
 #include <vector>
 
 #include "ctx_internal.h"
@@ -256,7 +257,12 @@ void run_chunk(uepm_ctx* ctx, const Layout& L, char* ws, const double* kk, int c
     using SP  = typename Split<S>::type;
     auto* H32 = reinterpret_cast<S32*>(ws + L.H32);
     auto* Hs  = reinterpret_cast<SP*>(ws + L.H);
-    {
+    // Real local-potential matrices reduced in registers: the reduction forms H(k) itself from the
+    // resident V and the kinetic diagonal (the same FP32 values), so nothing is assembled.
+    constexpr bool kReal32 = std::is_same<S32, float>::value;
+    const bool     reg_local = kReal32 && ctx->sparse_local && (ctx->tune.reduction == 0 || ctx->tune.reduction == 1) &&
+                           n <= tridiag_reg_max_n();
+    if (!reg_local) {
         ProfScope p(ctx, s, KK_ASSEMBLE);
         // the FP64 matrix is kept only for the Rayleigh-Ritz products: stored as FP32 pairs in place;
         // with a local potential only, those products use the resident sparse V instead
@@ -276,8 +282,16 @@ void run_chunk(uepm_ctx* ctx, const Layout& L, char* ws, const double* kk, int c
     auto* small = reinterpret_cast<S*>(ws + L.small);
     {
         ProfScope p(ctx, s, KK_TRIDIAG32);
-        launch_tridiag<S32>(H32, n, n, mstride, d, e, tq, st, c, s, ctx->tune.reduction, ctx->tune.ctas_per_sm,
+        if constexpr (kReal32) {
+            if (reg_local)
+                launch_tridiag_reg_local(ctx->d_V32, ctx->d_Vloc, rows, H32, n, n, mstride, d, e, tq, st, c, s);
+            else
+                launch_tridiag<S32>(H32, n, n, mstride, d, e, tq, st, c, s, ctx->tune.reduction, ctx->tune.ctas_per_sm,
+                                    ctx->tune.cluster);
+        } else {
+            launch_tridiag<S32>(H32, n, n, mstride, d, e, tq, st, c, s, ctx->tune.reduction, ctx->tune.ctas_per_sm,
                                 ctx->tune.cluster);
+        }
     }
     {
         ProfScope p(ctx, s, KK_BISECT);
@@ -553,6 +567,13 @@ int uepm_ctx_create(const uepm_material* mat, const int32_t* G, int N, uint32_t 
             (e = cudaMemcpy(ctx->d_ell_re, re.data(), sizeof(float2) * cnt, cudaMemcpyHostToDevice)) != cudaSuccess ||
             (e = cudaMemcpy(ctx->d_ell_im, im.data(), sizeof(float2) * cnt, cudaMemcpyHostToDevice)) != cudaSuccess)
             return fail(e, "copy ell");
+        // the FP32 off-diagonal of a real local H is k-independent: the register reduction reads it
+        // from this table (rounded as the assembly's FP32 copy rounds it) instead of an assembled copy
+        std::vector<float> v32((size_t)N * N);
+        for (size_t q = 0; q < v32.size(); ++q) v32[q] = (float)V[q].x;
+        if ((e = cudaMalloc(&ctx->d_V32, sizeof(float) * v32.size())) != cudaSuccess) return fail(e, "cudaMalloc(V32)");
+        if ((e = cudaMemcpy(ctx->d_V32, v32.data(), sizeof(float) * v32.size(), cudaMemcpyHostToDevice)) != cudaSuccess)
+            return fail(e, "copy V32");
         ctx->sparse_local = true;
     }
     *out = ctx;
@@ -568,6 +589,7 @@ int uepm_ctx_destroy(uepm_ctx* ctx) {
     if (ctx->d_ell_col) cudaFree(ctx->d_ell_col);
     if (ctx->d_ell_re) cudaFree(ctx->d_ell_re);
     if (ctx->d_ell_im) cudaFree(ctx->d_ell_im);
+    if (ctx->d_V32) cudaFree(ctx->d_V32);
     if (ctx->d_ws) cudaFree(ctx->d_ws);
     if (ctx->d_io) cudaFree(ctx->d_io);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);

@@ -34,6 +34,7 @@ struct uepm_ctx {
     int*          d_ell_col = nullptr;  // [ell_w][N]
     float2*       d_ell_re  = nullptr;  // [ell_w][N] FP32 pairs of Re V
     float2*       d_ell_im  = nullptr;  // [ell_w][N] FP32 pairs of Im V
+    float*        d_V32     = nullptr;  // [N][N] Re V rounded to FP32 (the diagonal is formed per k)
     void*         d_ws      = nullptr;
     size_t        ws_bytes  = 0;
     // buffers of the host-pointer entry point

@@ -204,10 +204,15 @@ __device__ __forceinline__ void reduce_block(float (&a)[K][K], RegShared& sh, fl
     }
 }
 
-template <int K>
+// LOCAL: the matrix is not read from H but formed from the k-independent local potential: off the
+// diagonal its FP32 rounding V32 ([N][N] column-major), on it the FP64 V (complex storage of a real
+// matrix) plus the rows table's kinetic term, rounded once, exactly as the assembly's FP32 copy is;
+// H then only receives the reflector tails. V32 (75 KB at N = 137) stays in L2 across the batch.
+template <int K, bool LOCAL>
 __global__ void __launch_bounds__(kThreads, K <= 9 ? 2 : 1)
     k_tridiag_reg(float* __restrict__ H, int n, int ld, size_t mstride, float* __restrict__ dOut,
-                  float* __restrict__ eOut, float* __restrict__ tqOut, int* __restrict__ status, int batch) {
+                  float* __restrict__ eOut, float* __restrict__ tqOut, int* __restrict__ status, int batch,
+                  const float* __restrict__ V32, const double* __restrict__ Vre, const double* __restrict__ rows) {
     __shared__ RegShared sh;
     const int tid = threadIdx.x, r = tid & (kGrid - 1), c = tid >> 4;
     for (int b = blockIdx.x; b < batch; b += gridDim.x) {
@@ -220,7 +225,19 @@ __global__ void __launch_bounds__(kThreads, K <= 9 ? 2 : 1)
 #pragma unroll
             for (int u = 0; u < K; ++u) {
                 const int jj = c + kGrid * u;
-                a[t][u]      = (i < n && jj < n) ? Ag[(size_t)jj * ld + i] : 0.f;
+                if constexpr (LOCAL) {
+                    float x = 0.f;
+                    if (i < n && jj < n) {
+                        if (i == jj)  // Re V[i][i] + kinetic, rounded once
+                            x = __double2float_rn(Vre[2 * ((size_t)i * n + i)] +
+                                                  rows[((size_t)b * n + i) * ROW_STRIDE + RF_KIN]);
+                        else
+                            x = V32[(size_t)jj * n + i];
+                    }
+                    a[t][u] = x;
+                } else {
+                    a[t][u] = (i < n && jj < n) ? Ag[(size_t)jj * ld + i] : 0.f;
+                }
             }
         }
         bool   bad = false;
@@ -235,19 +252,34 @@ __global__ void __launch_bounds__(kThreads, K <= 9 ? 2 : 1)
     }
 }
 
-template <int K>
+template <int K, bool LOCAL>
 void launch_k(float* H, int n, int ld, size_t mstride, float* d, float* e, float* tq, int* status, int batch,
-              cudaStream_t s) {
+              cudaStream_t s, const float* V32, const double* Vre, const double* rows) {
     static int grid_cap = 0;
     if (!grid_cap) {
         int dev = 0, sms = 0, per_sm = 0;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_tridiag_reg<K>, kThreads, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_tridiag_reg<K, LOCAL>, kThreads, 0);
         grid_cap = std::max(1, sms) * std::max(1, per_sm);
     }
-    k_tridiag_reg<K><<<std::min(batch, grid_cap), kThreads, 0, s>>>(H, n, ld, mstride, d, e, tq, status, batch);
+    k_tridiag_reg<K, LOCAL>
+        <<<std::min(batch, grid_cap), kThreads, 0, s>>>(H, n, ld, mstride, d, e, tq, status, batch, V32, Vre, rows);
     count_launch();
+}
+
+template <bool LOCAL>
+void launch_reg(float* H, int n, int ld, size_t mstride, float* d, float* e, float* tq, int* status, int batch,
+                cudaStream_t s, const float* V32, const double* Vre, const double* rows) {
+    switch ((n + kGrid - 1) / kGrid) {
+        case 1: case 2: case 3: case 4: case 5:
+        case 6: launch_k<6, LOCAL>(H, n, ld, mstride, d, e, tq, status, batch, s, V32, Vre, rows); break;
+        case 7: launch_k<7, LOCAL>(H, n, ld, mstride, d, e, tq, status, batch, s, V32, Vre, rows); break;
+        case 8: launch_k<8, LOCAL>(H, n, ld, mstride, d, e, tq, status, batch, s, V32, Vre, rows); break;
+        case 9: launch_k<9, LOCAL>(H, n, ld, mstride, d, e, tq, status, batch, s, V32, Vre, rows); break;
+        case 10: launch_k<10, LOCAL>(H, n, ld, mstride, d, e, tq, status, batch, s, V32, Vre, rows); break;
+        default: launch_k<11, LOCAL>(H, n, ld, mstride, d, e, tq, status, batch, s, V32, Vre, rows); break;
+    }
 }
 
 }  // namespace
@@ -256,15 +288,12 @@ int tridiag_reg_max_n() { return kGrid * 11; }
 
 void launch_tridiag_reg(float* H, int n, int ld, size_t mstride, float* d, float* e, float* tq, int* status, int batch,
                         cudaStream_t s) {
-    switch ((n + kGrid - 1) / kGrid) {
-        case 1: case 2: case 3: case 4: case 5:
-        case 6: launch_k<6>(H, n, ld, mstride, d, e, tq, status, batch, s); break;
-        case 7: launch_k<7>(H, n, ld, mstride, d, e, tq, status, batch, s); break;
-        case 8: launch_k<8>(H, n, ld, mstride, d, e, tq, status, batch, s); break;
-        case 9: launch_k<9>(H, n, ld, mstride, d, e, tq, status, batch, s); break;
-        case 10: launch_k<10>(H, n, ld, mstride, d, e, tq, status, batch, s); break;
-        default: launch_k<11>(H, n, ld, mstride, d, e, tq, status, batch, s); break;
-    }
+    launch_reg<false>(H, n, ld, mstride, d, e, tq, status, batch, s, nullptr, nullptr, nullptr);
+}
+
+void launch_tridiag_reg_local(const float* V32, const cx<double>* Vloc, const double* rows, float* H, int n, int ld,
+                              size_t mstride, float* d, float* e, float* tq, int* status, int batch, cudaStream_t s) {
+    launch_reg<true>(H, n, ld, mstride, d, e, tq, status, batch, s, V32, reinterpret_cast<const double*>(Vloc), rows);
 }
 
 }  // namespace uepm

@@ -44,6 +44,11 @@ bool launch_tridiag_cluster(S* H, int n, int ld, size_t mstride, typename ST<S>:
 int  tridiag_reg_max_n();
 void launch_tridiag_reg(float* H, int n, int ld, size_t mstride, float* d, float* e, float* tq, int* status, int batch,
                         cudaStream_t s);
+// The same for real local-potential matrices formed in the kernel from the k-independent local V
+// ([N][N], N = n: its FP32 rounding V32 off the diagonal, FP64 Vloc plus the rows table's kinetic term
+// on it), bit-identical to reducing the assembly's FP32 copy; H receives only the reflector tails.
+void launch_tridiag_reg_local(const float* V32, const cx<double>* Vloc, const double* rows, float* H, int n, int ld,
+                              size_t mstride, float* d, float* e, float* tq, int* status, int batch, cudaStream_t s);
 
 // tridiag_eig.cu
 template <typename T>
