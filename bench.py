@@ -11,6 +11,7 @@ One step = one solve of the whole 2000-point batch. Reported:
   e2e          the same metric through the C ABI uepm_solve with pinned host buffers (k in, E out)
   roofline     the dominant kernel of the headline path, timed with CUDA events on its stream
   cpu_baseline the oracle (CPU restatement of the reference path) on this host's cores
+  cpu_cli_as_shipped  the same on one thread with gradients on, as the reference CLI runs it
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 """
@@ -84,6 +85,30 @@ def cpu_time_oracle(nthreads: int, budget_s: float):
             break
     dt = time.perf_counter() - t0
     return done / dt, done, dt
+
+
+def cpu_time_cli_as_shipped(budget_s: float):
+    """The reference CLI as shipped runs BandStructure::Compute_parallel on one thread with
+    gradients on: apps/EmpiricalPseudoPotentialMain.cpp:75,122,174 call Compute_parallel(nrThreads),
+    whose first parameter is the gradient flag (BandStructure.h:58). The oracle timed that way on
+    growing prefixes of the path until budget_s elapsed."""
+    from oracle import oracle as O
+
+    O.build()
+    mat = O.load_materials(PARAM_FILE)["Si"]
+    G = O.generate_basis(SHELLS)
+    k, _ = O.generate_path(PATH, NPOINTS)
+    O.band_structure(mat, G, k[:4], NB, grad=True, nthreads=1)  # warm-up
+    done, m, t0 = 0, 8, time.perf_counter()
+    while True:
+        O.band_structure(mat, G, k[:m], NB, grad=True, nthreads=1)
+        done += m
+        dt = time.perf_counter() - t0
+        if dt >= budget_s or m >= len(k):
+            break
+        m = min(2 * m, len(k))
+    return {"value": done / dt, "unit": "k-points/s", "cores": 1, "kind": "port",
+            "sample": f"{done} path k-points, {dt:.1f} s, FP64 eigenvalues and gradients, one thread"}
 
 
 class Clocks:
@@ -308,6 +333,7 @@ def run_ours(args):
         "cpu_baseline": {"value": cpu_v, "unit": "k-points/s", "cores": cores, "kind": "port",
                          "sample": f"{cpu_done} k-points ({cpu_done // nk} passes over the 2000-point path), "
                                    f"{cpu_dt:.1f} s, FP64 eigenvalues only"},
+        "cpu_cli_as_shipped": cpu_time_cli_as_shipped(min(args.cpu_budget, 3.0)) if ws == 1 else None,
         "clocks": clk,
     }
     if ws == 1 and not args.no_extras:

@@ -41,3 +41,11 @@ def test_reference_arm_other_ranks_exit_quietly():
     r = _run({"RANK": "1", "LOCAL_RANK": "1", "WORLD_SIZE": "2"})
     assert r.returncode == 0, r.stderr[-2000:]
     assert not [ln for ln in r.stdout.splitlines() if ln.strip().startswith("{")]
+
+
+def test_cli_as_shipped_baseline_is_one_thread_with_gradients():
+    sys.path.insert(0, ROOT)
+    import bench
+
+    d = bench.cpu_time_cli_as_shipped(0.5)
+    assert d["value"] > 0 and d["cores"] == 1 and d["kind"] == "port" and "gradients" in d["sample"]
