@@ -337,7 +337,8 @@ __global__ void k_invit(const T* __restrict__ dIn, const T* __restrict__ eIn, co
     // in a thousand). Instead every member of such a group takes one shift p below the group,
     // p = max(8 eps ||T||_1, 2 x the group's spread) and at most half-way to the eigenvalue
     // below: the solve then stretches the group's eigenspace nearly evenly (by at most 1.5x
-    // between members), the start vectors keep their directions inside it, Gram-Schmidt keeps
+    // between members where the eigenvalue below does not cap the offset), the start vectors keep
+    // their directions inside it, Gram-Schmidt keeps
     // them orthogonal, and the rest of the spectrum still shrinks by p / gap per solve. (Detecting
     // groups up to 64 eps ||T||_1 was tried: it also grouped the genuinely split pairs of
     // zinc-blende crystals with spin-orbit, whose larger shared offsets left up to 2e-8 eV.)
