@@ -166,6 +166,39 @@ def test_mixed_precision_eigenvalues_within_1e6(gpu, oracle, mats, case, nb, nk)
     assert err <= MIXED_TOL, f"{case}: mixed max |dE| = {err:.3e} eV"
 
 
+FIXTURES = {  # tests/golden/oracle_bands.npz entries: (material key, shells, nl, soc, bands)
+    "si_cb_local": ("Si-CB", 10, False, False, 16),
+    "si_d_nonlocal": ("Si-d", 10, True, False, 12),
+    "inp_nonlocal": ("InP", 9, True, False, 12),
+    "gaas_nonlocal_soc": ("GaAs", 8, True, True, 16),
+    "ge_nonlocal_soc": ("Ge", 12, True, True, 16),
+}
+
+
+@pytest.mark.parametrize("name", list(FIXTURES))
+def test_fp64_path_matches_the_committed_band_fixtures(gpu, oracle, mats, name):
+    """The committed oracle fixtures (tests/golden/oracle_bands.npz: symmetry points and two seeded
+    k) without an oracle solve at test time: eigenvalues within 1e-10 eV, gradients of bands more
+    than 1e-3 eV from both neighbours (the top band excluded) within 1e-8 of the gradient scale."""
+    import os
+
+    from conftest import GOLDEN
+
+    fx = np.load(os.path.join(GOLDEN, "oracle_bands.npz"))
+    key, shells, nl, soc, nb = FIXTURES[name]
+    G = oracle.generate_basis(shells)
+    E, _, g, st = _ctx(mats[key], G, nl, soc).solve(fx["k"], nb, gradient=True)
+    assert not st.any()
+    Ef, gf = fx[name + "_E"], fx[name + "_grad"]
+    err = np.abs(E - Ef).max()
+    assert err <= EV_TOL, f"{name}: max |dE| = {err:.3e} eV"
+    scale = np.abs(gf).max()
+    for q in range(len(Ef)):
+        gaps = np.diff(Ef[q])
+        iso = (np.r_[np.inf, gaps] > 1e-3) & (np.r_[gaps, 0.0] > 1e-3)
+        np.testing.assert_allclose(g[q][iso], gf[q][iso], rtol=0, atol=1e-8 * scale, err_msg=name)
+
+
 @pytest.mark.parametrize("precision", [N.UEPM_PREC_FP64, N.UEPM_PREC_MIXED])
 def test_vectors_at_size_are_orthonormal_eigenvectors(gpu, oracle, mats, precision):
     """Ge with spin-orbit (all bands exact Kramers pairs), 400 seeded first-zone k, 16 bands with

@@ -194,3 +194,30 @@ def test_unsupported_soc_period_is_rejected(oracle, mats):
     G = oracle.generate_basis(4)
     with pytest.raises(RuntimeError):
         oracle.assemble(mats["Sn"], G, [0.1, 0.0, 0.0], soc=True)  # Sn has atomic period 5
+
+
+def _isolated(E, tol=1e-3):
+    """Bands separated from both neighbours by more than tol eV, the top band excluded (its upper
+    neighbour is not in the fixture): their gradients are well defined."""
+    gaps = np.diff(E)
+    iso = (np.r_[np.inf, gaps] > tol) & (np.r_[gaps, 0.0] > tol)
+    return iso
+
+
+def test_oracle_reproduces_its_band_fixtures(oracle):
+    """tests/golden/oracle_bands.npz (make_oracle_golden.py): eigenvalues and, for isolated bands,
+    Hellmann-Feynman gradients at the symmetry points and two seeded k, for five configurations."""
+    import sys
+
+    sys.path.insert(0, GOLDEN)
+    import make_oracle_golden as MG
+
+    fx = np.load(os.path.join(GOLDEN, "oracle_bands.npz"))
+    np.testing.assert_array_equal(fx["k"], MG.k_points())
+    for name in MG.CONFIGS:
+        E, g = MG.compute(name)
+        np.testing.assert_allclose(E, fx[name + "_E"], rtol=0, atol=1e-10, err_msg=name)
+        scale = np.abs(fx[name + "_grad"]).max()
+        for q in range(len(E)):
+            iso = _isolated(fx[name + "_E"][q])
+            np.testing.assert_allclose(g[q][iso], fx[name + "_grad"][q][iso], rtol=0, atol=1e-8 * scale, err_msg=name)
