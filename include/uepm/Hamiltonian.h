@@ -33,8 +33,11 @@ class Hamiltonian {
     const RealVector&    get_eigenvalues() const { return m_values; }
     const ComplexMatrix& get_eigenvectors() const { return m_vectors; }
     const RealVector&    eigenvalues() const { return m_values; }
-    // H(k) is Hermitian by construction on the GPU (the reference compares H with its transpose)
-    bool check_matrix_is_symmetric() const { return true; }
+    // The reference compares the stored H(k) with its transpose (Hamiltonian.h:22), so it answers
+    // true for a real H(k) and false for a complex one (spin-orbit, antisymmetric form factors,
+    // unequal anion / cation nonlocal parameters); the same answer here, from the context's type.
+    // True before the first SetMatrix.
+    bool check_matrix_is_symmetric() const;
     // Hellmann-Feynman kinetic gradient of band level_index at k_point, from the kept eigenvectors
     // (src/EPP/Hamiltonian.cpp:146-194); throws std::runtime_error / std::out_of_range like the reference.
     Vector3D<double> compute_gradient_at_level(const Vector3D<double>& k_point, unsigned int level_index) const;
@@ -44,10 +47,10 @@ class Hamiltonian {
     const std::vector<Vector3D<int>>& m_basisVectors;
 
  private:
-    uepm_ctx* context(bool nl, bool soc);
-    uepm_ctx*        m_ctx[4] = {nullptr, nullptr, nullptr, nullptr};  // per (nl, soc)
-    Vector3D<double> m_k;
-    bool             m_nl = false, m_soc = false;
+    uepm_ctx*         context(bool nl, bool soc) const;
+    mutable uepm_ctx* m_ctx[4] = {nullptr, nullptr, nullptr, nullptr};  // per (nl, soc)
+    Vector3D<double>  m_k;
+    bool              m_nl = false, m_soc = false, m_set = false;
     RealVector       m_values;
     ComplexMatrix    m_vectors;
 };

@@ -19,7 +19,11 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "lib", "liboracle.so")
+FAST_LIB_PATH = os.path.join(HERE, "lib", "liboracle_fast.so")
 REF_PATH = os.path.join(HERE, "_ref", "libref.so")
+# Root of the reference source tree (read only by the checker build and the fixture script; absent
+# on machines that only run the committed fixtures).
+REFERENCE_ROOT = os.environ.get("UEPM_REFERENCE_ROOT", "/root/reference")
 
 # src/Common/physical_constants.hpp:18-44
 H_PLANCK = 6.62607015e-34
@@ -151,11 +155,17 @@ _lib = None
 _ref = None
 
 
+def reference_present() -> bool:
+    return os.path.isdir(os.path.join(REFERENCE_ROOT, "src", "EPP"))
+
+
 def build():
-    """Compile liboracle.so (and libref.so when the reference tree is present)."""
-    subprocess.run(["make", "-s", "-C", HERE, "oracle"], check=True)
-    if os.path.isdir("/root/reference/src/EPP"):
-        subprocess.run(["make", "-s", "-C", HERE, "ref"], check=True)
+    """Compile liboracle.so, liboracle_fast.so (the timed baseline build) and, when the reference
+    tree is present, libref.so."""
+    env = dict(os.environ, UEPM_REFERENCE_ROOT=REFERENCE_ROOT)
+    subprocess.run(["make", "-s", "-C", HERE, "oracle", "fast"], check=True, env=env)
+    if reference_present():
+        subprocess.run(["make", "-s", "-C", HERE, "ref"], check=True, env=env)
 
 
 def lib():
@@ -218,6 +228,17 @@ def ref_lib():
         L.ref_pp_value.argtypes = [dp, C.c_int, C.c_int, C.c_int, dp, C.c_double, dp]
         L.ref_generate_path.argtypes = [C.c_char_p, C.c_uint, dp, C.c_int, C.POINTER(C.c_uint32), C.c_int]
         L.ref_generate_path.restype = C.c_int
+        cp = C.c_char_p
+        ip = C.POINTER(C.c_int32)
+        L.ref_material.argtypes = [cp, cp, C.POINTER(OrMaterial)]
+        L.ref_hamiltonian.argtypes = [cp, cp, ip, C.c_int, dp, C.c_int, C.c_int, C.c_int, dp]
+        L.ref_nl_correction.argtypes = [cp, cp, dp, dp, dp, dp]
+        L.ref_soc_block.argtypes = [cp, cp, dp, dp, dp, dp, dp, dp]
+        L.ref_band_file.argtypes = [cp, cp, C.c_int, cp, C.c_uint, C.c_uint, C.c_int, C.c_int, C.c_int, cp, dp,
+                                    C.c_int]
+        L.ref_gradient_shape.argtypes = [cp, cp, C.c_int, dp, C.c_int, C.c_uint, C.POINTER(C.c_int),
+                                         C.POINTER(C.c_int), dp, C.c_int]
+        assert L.ref_material_size() == C.sizeof(OrMaterial)
         _ref = L
     return _ref
 

@@ -7,6 +7,8 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 sys.path.insert(0, ROOT)
 PARAMS = os.path.join(ROOT, "params")
 GOLDEN = os.path.join(ROOT, "tests", "golden")
+# the reference source tree (UEPM_REFERENCE_ROOT), present only where fixtures are made
+from oracle.oracle import REFERENCE_ROOT  # noqa: E402
 
 
 def pytest_configure(config):

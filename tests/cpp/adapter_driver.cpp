@@ -42,8 +42,11 @@ int main(int argc, char** argv) {
     // one k-point through Hamiltonian directly, all eigenvalues and vectors
     Hamiltonian h(mat, bs.get_basis_vectors());
     const Vector3D<double> k0(0.11, 0.27, -0.05);
+    const bool sym_before = h.check_matrix_is_symmetric();
     h.SetMatrix(k0, nl, soc);
     h.Diagonalize(true);
+    std::printf("symmetric %d %d\n", sym_before ? 1 : 0, h.check_matrix_is_symmetric() ? 1 : 0);
+    std::printf("gradrows %zu %zu\n", g.size(), g.empty() ? (size_t)0 : g.front().size());
     FILE* fh = std::fopen((out + "_ham.txt").c_str(), "w");
     const auto& ev = h.eigenvalues();
     for (long i = 0; i < ev.size(); ++i) std::fprintf(fh, "E %.17g\n", ev(i));

@@ -12,10 +12,29 @@ Outputs (all small, committed):
                      G_i - G_j of the 10-shell basis, for two form-factor sets.
   ref_paths.json     SymmetryPoints::GeneratePoints (the reference's SymmetryPoints.cpp) for several
                      paths and sizes, including the 2000-point L-G-X-W-K-U-L-W-X-K-G path.
+
+From the reference's Material.cpp, SpinOrbitFunctional.cpp, Hamiltonian.cpp and BandStructure.cpp,
+compiled against the project-written Eigen / yaml-cpp subsets in oracle/shim:
+  ref_materials.json the fields Materials::load_material_parameters leaves in each Material of every
+                     parameter file under params/ (units as the reference holds them).
+  ref_hamiltonian.npz H(k) after Hamiltonian::SetMatrix and Diagonalize's hermitisation, for seven
+                     material / nonlocal / spin-orbit cases at the eight fixed k (Gamma, L, X, W, K,
+                     U and two seeded generic points): the lower triangles at basis 15 (3 shells),
+                     and SHA-256 digests of the full column-major complex128 matrices at the
+                     production bases (89 to 229 plane waves, orders up to 458), zeros unsigned.
+  ref_elements.npz   Material::compute_pseudopotential_non_local_correction and
+                     SpinOrbitCorrection::compute_soc_contribution on seeded (K1, K2) pairs, with
+                     equal-norm and equal pairs for the reference's |K1| = |K2| branches.
+  ref_band_*.txt     BandStructure::export_result_in_file after Initialize (path), Compute and
+                     AdjustValues, for Si local and Ge nonlocal with spin-orbit; their energies in
+                     ref_bands.npz.
+  ref_gradients.npz  the shape of get_band_energy_gradients() after Compute_parallel(true, 1)
+                     ([nk * nb] rows of nb) and its first nk rows.
 """
 from __future__ import annotations
 
 import ctypes as C
+import hashlib
 import json
 import os
 import re
@@ -47,8 +66,123 @@ def parse_bessel_table(ref_root: str) -> dict:
     return out
 
 
+PARAMS = os.path.join(ROOT, "params")
+# (key, parameter file, symbol, nonlocal, spin-orbit, production shells)
+HAM_CASES = [("si_local", "si-cohen-bergstresser.yaml", "Si", 0, 0, 10),
+             ("si_nl", "materials.yaml", "Si", 1, 0, 10),
+             ("si_d", "si-nonlocal-d.yaml", "Si", 1, 0, 10),
+             ("inp_nl", "materials.yaml", "InP", 1, 0, 9),
+             ("ge_nl_soc", "materials.yaml", "Ge", 1, 1, 12),
+             ("gaas_nl_soc", "materials.yaml", "GaAs", 1, 1, 8),
+             ("gap_soc", "materials.yaml", "GaP", 0, 1, 13)]
+# Gamma, L, X, W, K, U, then two seeded generic points
+FIXED_K = np.array([[0, 0, 0], [0.5, 0.5, 0.5], [1, 0, 0], [1, 0.5, 0], [0.75, 0.75, 0], [1, 0.25, 0.25],
+                    [0.1237, -0.3318, 0.2871], [-0.4419, 0.0963, 0.6027]], dtype=np.float64)
+BAND_FILES = [("si_local", "si-cohen-bergstresser.yaml", "Si", 16, "LGXWKULWXKG", 40, 10, 0, 0),
+              ("ge_nl_soc", "materials.yaml", "Ge", 8, "LGX", 20, 8, 1, 1)]
+
+
+def ref_hamiltonians(R, path, sym, G, k, nl, soc):
+    N = len(G)
+    n = 2 * N if soc else N
+    H = np.zeros((len(k), n, n), dtype=np.complex128)  # [q][column][row]: column-major per k
+    rc = R.ref_hamiltonian(path.encode(), sym.encode(), O._ip(np.ascontiguousarray(G, dtype=np.int32)), N,
+                           O._dp(np.ascontiguousarray(k)), len(k), nl, soc, O._dp(H))
+    assert rc == n, (path, sym, rc)
+    return H
+
+
+def make_reference_hamiltonians(R):
+    small = O.generate_basis(3)
+    out = {"k": FIXED_K, "G_small": small}
+    for key, fname, sym, nl, soc, shells in HAM_CASES:
+        path = os.path.join(PARAMS, fname)
+        H = ref_hamiltonians(R, path, sym, small, FIXED_K, nl, soc)
+        n = H.shape[1]
+        r, c = np.tril_indices(n)
+        out[key + "_lower"] = np.stack([H[q][c, r] for q in range(len(FIXED_K))])  # H(r, c), r >= c
+        Gp = O.generate_basis(shells)
+        Hp = ref_hamiltonians(R, path, sym, Gp, FIXED_K, nl, soc)
+        # zeros are hashed unsigned (x + 0.0): the sign of a zero element depends on how the matrix
+        # library scales a complex by a real (Diagonalize's 0.5 * (H + H^H)), not on the reference
+        out[key + "_sha256"] = np.array([hashlib.sha256((Hp[q] + 0.0).tobytes()).hexdigest()
+                                         for q in range(len(FIXED_K))])
+        out[key + "_shells"] = np.array(shells)
+    np.savez_compressed(os.path.join(HERE, "ref_hamiltonian.npz"), **out)
+
+
+def make_reference_elements(R):
+    rng = np.random.default_rng(20261204)
+    K1 = rng.uniform(-3.0, 3.0, (96, 3))
+    K2 = rng.uniform(-3.0, 3.0, (96, 3))
+    # the reference's |K1| = |K2| branches: equal vectors, and signed permutations (equal norms)
+    K2[:16] = K1[:16]
+    K2[16:32] = -K1[16:32, ::-1]
+    K1[32:36] = 0.0
+    G1 = rng.integers(-3, 4, (96, 3)).astype(np.float64)
+    G2 = rng.integers(-3, 4, (96, 3)).astype(np.float64)
+    out = {"K1": K1, "K2": K2, "G1": G1, "G2": G2}
+    for key, fname, sym, nl, soc, _ in HAM_CASES:
+        path = os.path.join(PARAMS, fname).encode()
+        mat = O.load_materials(os.path.join(PARAMS, fname))[sym]
+        tau = np.full(3, (1.0 / 8.0) * 1e-10 * mat.lattice_constant)
+        if nl:
+            v = np.zeros((96, 2))
+            for q in range(96):
+                assert R.ref_nl_correction(path, sym.encode(), O._dp(K1[q]), O._dp(K2[q]), O._dp(tau), O._dp(v[q])) == 0
+            out[key + "_nl"] = v
+        if soc:
+            b = np.zeros((96, 8))
+            for q in range(96):
+                assert R.ref_soc_block(path, sym.encode(), O._dp(K1[q]), O._dp(K2[q]), O._dp(G1[q]), O._dp(G2[q]),
+                                       O._dp(tau), O._dp(b[q])) == 0
+            out[key + "_soc"] = b
+    np.savez_compressed(os.path.join(HERE, "ref_elements.npz"), **out)
+
+
+def make_reference_materials(R):
+    out = {}
+    for fname in sorted(os.listdir(PARAMS)):
+        if not fname.endswith(".yaml"):
+            continue
+        path = os.path.join(PARAMS, fname)
+        for sym in O.load_materials(path):
+            m = O.OrMaterial()
+            assert R.ref_material(path.encode(), sym.encode(), C.byref(m)) == 0
+            out.setdefault(fname, {})[sym] = {f: getattr(m, f) for f, _ in O.OrMaterial._fields_}
+    with open(os.path.join(HERE, "ref_materials.json"), "w") as f:
+        json.dump(out, f, indent=1)
+
+
+def make_reference_band_files(R):
+    out = {}
+    for key, fname, sym, nb, labels, npts, shells, nl, soc in BAND_FILES:
+        dst = os.path.join(HERE, f"ref_band_{key}.txt")
+        cap = 4 * npts * nb
+        E = np.zeros(cap)
+        cnt = R.ref_band_file(os.path.join(PARAMS, fname).encode(), sym.encode(), nb, labels.encode(), npts, shells, nl,
+                              soc, 0, dst.encode(), O._dp(E), cap)
+        assert cnt > 0, (key, cnt)
+        out[key] = E[:cnt].reshape(-1, nb * (2 if soc else 1))
+    np.savez_compressed(os.path.join(HERE, "ref_bands.npz"), **out)
+
+
+def make_reference_gradients(R):
+    k = FIXED_K[[1, 6, 7]].copy()
+    nb = 4
+    G = O.generate_basis(4)
+    rows, row_len = C.c_int(), C.c_int()
+    g = np.zeros((len(k), nb, 3))
+    assert R.ref_gradient_shape(os.path.join(PARAMS, "si-cohen-bergstresser.yaml").encode(), b"Si", nb,
+                                O._dp(k), len(k), 4, C.byref(rows), C.byref(row_len), O._dp(g), len(k)) == 0
+    np.savez(os.path.join(HERE, "ref_gradients.npz"), k=k, nb=nb, shells=4, rows=rows.value, row_len=row_len.value,
+             grad=g, G=G)
+
+
 def main():
-    ref_root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    ref_root = sys.argv[1] if len(sys.argv) > 1 else O.REFERENCE_ROOT
+    os.environ["UEPM_REFERENCE_ROOT"] = ref_root
+    O.REFERENCE_ROOT = ref_root
     O.build()
     R = O.ref_lib()
     if R is None:
@@ -105,6 +239,12 @@ def main():
         paths.append(entry)
     with open(os.path.join(HERE, "ref_paths.json"), "w") as f:
         json.dump(paths, f)
+
+    make_reference_materials(R)
+    make_reference_hamiltonians(R)
+    make_reference_elements(R)
+    make_reference_band_files(R)
+    make_reference_gradients(R)
     print("golden fixtures written to", HERE)
 
 

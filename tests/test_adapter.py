@@ -8,11 +8,11 @@ import subprocess
 import numpy as np
 import pytest
 
-from conftest import PARAMS, ROOT
+from conftest import GOLDEN, PARAMS, REFERENCE_ROOT, ROOT
 
 LIB = os.path.join(ROOT, "ultimateepm_gb300", "lib")
 INC = [f"-I{os.path.join(ROOT, 'include')}", f"-I{os.path.join(ROOT, 'include', 'uepm')}"]
-REF = "/root/reference"
+REF = REFERENCE_ROOT
 
 
 def _compile_driver(tmp_path):
@@ -79,9 +79,48 @@ def test_adapter_matches_oracle(gpu, oracle, mats, tmp_path, yaml, mat, key, nl,
     vals = np.array([[float(x) for x in l.split(",")] for l in lines[6:]])
     # 6 significant digits, like the reference's default stream output
     np.testing.assert_allclose(vals, Eo, rtol=1e-5, atol=1e-9)
+    # the reference's [nk * nb] x nb gradient array (BandStructure.cpp:158-166), first nk rows filled
+    rows, rlen = [int(x) for x in [l for l in r.stdout.splitlines() if l.startswith("gradrows")][0].split()[1:]]
+    assert (rows, rlen) == (len(k) * nb, nb)
+    # H compared with its transpose (Hamiltonian.h:22): true before SetMatrix, then true only for real H
+    sym = [int(x) for x in [l for l in r.stdout.splitlines() if l.startswith("symmetric")][0].split()[1:]]
+    assert sym == [1, 0 if soc else 1]
     # Hamiltonian path: all n eigenvalues at one k (up to ~400 eV: 1e-10 eV or 1e-12 relative)
     ham = open(out + "_ham.txt").read().split("\n")
     Eh = np.array([float(l.split()[1]) for l in ham if l.startswith("E ")])
     H = oracle.assemble(mats[key], G, [0.11, 0.27, -0.05], nl=bool(nl), soc=bool(soc))
     Eoh = oracle.eigh(H)
     assert (np.abs(Eh - Eoh) <= np.maximum(1e-10, 1e-12 * np.abs(Eoh))).all()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("key,yaml,mat,nb,labels,npts,shells,nl,soc", [
+    ("si_local", "si-cohen-bergstresser.yaml", "Si", 16, "LGXWKULWXKG", 40, 10, 0, 0),
+    ("ge_nl_soc", "materials.yaml", "Ge", 8, "LGX", 20, 8, 1, 1)])
+def test_adapter_band_file_matches_the_reference_file(gpu, tmp_path, key, yaml, mat, nb, labels, npts, shells, nl, soc):
+    """The adapter's export_result_in_file after Compute_parallel and AdjustValues, against the file the
+    reference itself wrote (tests/golden/ref_band_*.txt, BandStructure.cpp:290-314): the header and
+    layout byte-identical, and every value the same 6-digit string, except the last digit where the
+    two solvers' 1e-10 eV difference crosses a rounding boundary and the rounding noise of values
+    that AdjustValues brings to ~0 (degenerate valence tops, |E| < 1e-6 eV)."""
+    exe = _compile_driver(tmp_path)
+    out = str(tmp_path / "run")
+    r = subprocess.run([exe, os.path.join(PARAMS, yaml), mat, labels, str(npts), str(nb), str(shells), str(nl), str(soc),
+                        "fp64", out], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr[-2000:]
+    got = open(out + "_bands.txt").read().splitlines()
+    want = open(os.path.join(GOLDEN, f"ref_band_{key}.txt")).read().splitlines()
+    assert len(got) == len(want)
+    assert got[:6] == want[:6]
+    same = total = 0
+    for lg, lw in zip(got[6:], want[6:]):
+        fg, fw = lg.split(","), lw.split(",")
+        assert len(fg) == len(fw)
+        for a, b in zip(fg, fw):
+            total += 1
+            if a == b:
+                same += 1
+                continue
+            va, vb = float(a), float(b)
+            assert abs(vb) < 1e-6 and abs(va) < 1e-6 or abs(va - vb) <= 1.01e-5 * max(abs(vb), 1.0), (a, b)
+    assert same >= 0.98 * total

@@ -111,3 +111,37 @@ def test_no_cpu_fallback_when_library_missing(monkeypatch, tmp_path):
     with pytest.raises(RuntimeError, match="no CPU fallback"):
         nat.load()
     # monkeypatch restores the path and the loaded library afterwards
+
+
+def test_product_loader_equals_the_reference_loader(native):
+    """uepm_materials_load against Materials::load_material_parameters of the reference itself
+    (Material.cpp:33-71 compiled against oracle/shim; fixture tests/golden/ref_materials.json)."""
+    from ultimateepm_gb300 import Materials
+
+    ref = json.load(open(os.path.join(GOLDEN, "ref_materials.json")))
+    for fname, mats in ref.items():
+        m = Materials()
+        m.load_material_parameters(os.path.join(PARAMS, fname))
+        assert set(m.materials) == set(mats), fname
+        for sym, fields in mats.items():
+            for f, v in fields.items():
+                assert getattr(m.materials[sym].raw, f) == v, (fname, sym, f)
+
+
+@pytest.mark.parametrize("key,fname,sym,nb,labels,npts,shells,nl,soc", [
+    ("si_local", "si-cohen-bergstresser.yaml", "Si", 16, "LGXWKULWXKG", 40, 10, 0, 0),
+    ("ge_nl_soc", "materials.yaml", "Ge", 8, "LGX", 20, 8, 1, 1)])
+def test_band_file_byte_identical_to_the_reference(native, tmp_path, key, fname, sym, nb, labels, npts, shells, nl,
+                                                   soc):
+    """BandStructure::export_result_in_file (BandStructure.cpp:290-314): the Python mirror's band file
+    for the reference's own energies is byte-identical to the file the reference wrote."""
+    from ultimateepm_gb300 import BandStructure, Materials
+
+    mats = Materials()
+    mats.load_material_parameters(os.path.join(PARAMS, fname))
+    bs = BandStructure()
+    bs.Initialize(mats.materials[sym], nb, list(labels), shells, bool(nl), bool(soc), nrPoints=npts)
+    bs.m_energies = np.load(os.path.join(GOLDEN, "ref_bands.npz"))[key]
+    out = tmp_path / "bands.txt"
+    bs.export_result_in_file(str(out))
+    assert out.read_bytes() == open(os.path.join(GOLDEN, f"ref_band_{key}.txt"), "rb").read()

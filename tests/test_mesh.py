@@ -10,12 +10,12 @@ import os
 import numpy as np
 import pytest
 
-from conftest import PARAMS
+from conftest import PARAMS, REFERENCE_ROOT
 from ultimateepm_gb300 import _native as N
 from ultimateepm_gb300 import api
 from ultimateepm_gb300.mesh import MeshBZ, read_msh_nodes
 
-REF_MESH = "/root/reference/examples/meshes/bz_mesh.msh"
+REF_MESH = os.path.join(REFERENCE_ROOT, "examples", "meshes", "bz_mesh.msh")
 
 
 def _si():

@@ -55,7 +55,7 @@ Hamiltonian::~Hamiltonian() {
         if (c) uepm_ctx_destroy(c);
 }
 
-uepm_ctx* Hamiltonian::context(bool nl, bool soc) {
+uepm_ctx* Hamiltonian::context(bool nl, bool soc) const {
     uepm_ctx*& c = m_ctx[(nl ? 1 : 0) + (soc ? 2 : 0)];
     if (!c) c = make_context(m_material, m_basisVectors, nl, soc);
     return c;
@@ -65,6 +65,13 @@ void Hamiltonian::SetMatrix(const Vector3D<double>& k, bool add_non_local_correc
     m_k   = k;
     m_nl  = add_non_local_correction;
     m_soc = enable_soc;
+    m_set = true;
+}
+
+bool Hamiltonian::check_matrix_is_symmetric() const {
+    if (!m_set) return true;
+    // uepm_ctx_force_complex(ctx, 0) leaves the automatic choice and reports whether H(k) is real
+    return uepm_ctx_force_complex(context(m_nl, m_soc), 0) == 1;
 }
 
 void Hamiltonian::Diagonalize(bool keep_eigenvectors) {
@@ -191,8 +198,9 @@ void BandStructure::run(bool compute_gradient) {
     if (rc == UEPM_ERR_NOT_CONVERGED) throw std::runtime_error("Eigenvalue decomposition failed");
     throw_for(rc, "BandStructure::Compute");
     m_energies.assign(nk, std::vector<double>((size_t)nb));
-    m_energies_gradient.clear();
-    if (compute_gradient) m_energies_gradient.assign(nk, std::vector<Vector3D<double>>((size_t)nb));
+    // The reference sizes the gradient array [nk * nb] rows of nb and fills the first nk rows
+    // (BandStructure.cpp:158-166, :186-187); kept, so get_band_energy_gradients().size() matches.
+    if (compute_gradient) m_energies_gradient.assign(nk * m_nb_bands, std::vector<Vector3D<double>>((size_t)m_nb_bands));
     for (size_t i = 0; i < nk; ++i)
         for (int b = 0; b < nb; ++b) {
             m_energies[i][(size_t)b] = E[i * nb + b];
