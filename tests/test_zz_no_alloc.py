@@ -25,8 +25,7 @@ def test_noalloc_assembly_matches_regular_entry_point(gpu, oracle, mats, key, sh
     G = oracle.generate_basis(shells)
     ctx = api._Context(api.Material(key, raw=N.UepmMaterial.from_buffer_copy(bytes(mats[key]))), G, nl, soc)
     n = ctx.n
-    # the tolerance of the assembly parity tests: exact formulas, device special functions
-    rtol = 1e-12 if (nl or soc) else 1e-14
+    # both entry points run the same kernels on the same inputs: the results are bit-identical
     # two calls in a row, with different k-points, each compared with the regular entry point
     for seed in (3, 4):
         ks = np.concatenate([np.zeros((1, 3)), oracle.sample_first_bz(7, seed)])
@@ -40,8 +39,41 @@ def test_noalloc_assembly_matches_regular_entry_point(gpu, oracle, mats, key, sh
         r = ref.cpu().numpy()
         o = out.cpu().numpy()
         assert np.isfinite(o).all()
-        assert np.abs(o - r).max() <= rtol * np.abs(r).max()
+        np.testing.assert_array_equal(o, r)
     ctx.close()
+
+
+def test_noalloc_allocates_nothing_on_a_fresh_context(gpu, oracle, mats):
+    """Two no-alloc calls on a context that has never solved or assembled (its workspace is still
+    unallocated) leave the device's free memory unchanged, then match the regular entry point bit
+    for bit. A call on another context first does the once-per-device set-up (module load, address
+    lookup)."""
+    import torch
+
+    G = oracle.generate_basis(9)
+    raw = N.UepmMaterial.from_buffer_copy(bytes(mats["Ge"]))
+    warm = api._Context(api.Material("Ge", raw=raw), G, True, True)
+    ks = oracle.sample_first_bz(5, 9)
+    dk = torch.from_numpy(ks).cuda()
+    n = warm.n
+    out = torch.zeros((len(ks), n, n), dtype=torch.complex128, device="cuda")
+    N.check(gpu.uepm_assemble_device_noalloc(warm.h, C.c_void_p(dk.data_ptr()), len(ks), C.c_void_p(out.data_ptr()), None))
+    ctx = api._Context(api.Material("Ge", raw=raw), G, True, True)
+    out2 = torch.zeros_like(out)
+    ref = torch.zeros_like(out)
+    torch.cuda.synchronize()
+    free0 = torch.cuda.mem_get_info()[0]
+    for o in (out, out2):
+        N.check(gpu.uepm_assemble_device_noalloc(ctx.h, C.c_void_p(dk.data_ptr()), len(ks), C.c_void_p(o.data_ptr()),
+                                                 None))
+    torch.cuda.synchronize()
+    assert torch.cuda.mem_get_info()[0] == free0
+    N.check(gpu.uepm_assemble_device(ctx.h, C.c_void_p(dk.data_ptr()), len(ks), C.c_void_p(ref.data_ptr()), None))
+    torch.cuda.synchronize()
+    np.testing.assert_array_equal(out.cpu().numpy(), ref.cpu().numpy())
+    np.testing.assert_array_equal(out2.cpu().numpy(), ref.cpu().numpy())
+    ctx.close()
+    warm.close()
 
 
 def test_noalloc_rejects_requests_beyond_its_scratch(gpu, oracle, mats):
@@ -56,4 +88,15 @@ def test_noalloc_rejects_requests_beyond_its_scratch(gpu, oracle, mats):
     rc = gpu.uepm_assemble_device_noalloc(ctx.h, C.c_void_p(dk.data_ptr()), too_many, C.c_void_p(dH.data_ptr()), None)
     assert rc == N.UEPM_ERR_INVALID
     assert "limit" in N.last_error()
+    # more k-points than one assembly launch takes, with a one-plane-wave basis small enough for the
+    # scratch to admit them
+    G2 = np.zeros((1, 3), dtype=np.int32)
+    small = api._Context(api.Material("Si", raw=N.UepmMaterial.from_buffer_copy(bytes(mats["Si-CB"]))), G2, False, False)
+    nk = 32769
+    assert nk * len(G2) * 24 * 8 <= N.NOALLOC_SCRATCH_BYTES
+    dk2 = torch.zeros((nk, 3), dtype=torch.float64, device="cuda")
+    rc = gpu.uepm_assemble_device_noalloc(small.h, C.c_void_p(dk2.data_ptr()), nk, C.c_void_p(dH.data_ptr()), None)
+    assert rc == N.UEPM_ERR_INVALID
+    assert "32768" in N.last_error()
+    small.close()
     ctx.close()

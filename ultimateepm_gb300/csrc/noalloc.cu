@@ -11,9 +11,12 @@
 // The array (UEPM_NOALLOC_SCRATCH_BYTES = 16 MiB) exists on every GPU that loads this library, for as
 // long as the library stays loaded. Its device address is looked up once per device, with that device
 // current, by the first call on that device (cudaGetSymbolAddress); make that first call before any
-// stream capture. Every call shares the array and it keeps the last call's contents: each call
+// stream capture. The address is kept for the life of the process: after cudaDeviceReset (or any
+// other teardown of the device's primary context) it is stale, so the entry point must not be used
+// on that device again. Every call shares the array and it keeps the last call's contents: each call
 // rewrites every entry it reads, so nothing has to start at zero, but two calls whose work overlaps on
-// the GPU (different streams, or different host threads) race on it.
+// the GPU (different streams, or different host threads) race on it. One call takes at most
+// kMaxNoallocK = 32768 k-points (the assembly grid's extent) and at most the scratch's worth.
 #include <cuda_runtime.h>
 
 #include <mutex>
@@ -33,6 +36,7 @@ using namespace uepm;
 namespace {
 
 constexpr size_t kScratchDoubles = UEPM_NOALLOC_SCRATCH_BYTES / sizeof(double);
+constexpr size_t kMaxNoallocK    = 32768;  // k-points per launch: the assembly grid's z extent is <= 65535
 
 // The scratch row table. In host code this name is only a host-side stand-in for the device
 // object: its device address comes from cudaGetSymbolAddress (scratch_on_current_device).
@@ -73,6 +77,11 @@ extern "C" int uepm_assemble_device_noalloc(uepm_ctx* ctx, const double* d_k, si
         return UEPM_ERR_INVALID;
     }
     if (nk == 0) return UEPM_OK;
+    if (nk > kMaxNoallocK) {
+        set_error("uepm_assemble_device_noalloc: " + std::to_string(nk) + " k-points in one call; the limit is " +
+                  std::to_string(kMaxNoallocK) + " per call");
+        return UEPM_ERR_INVALID;
+    }
     const size_t need = nk * (size_t)t.N * ROW_STRIDE;
     if (need > kScratchDoubles) {
         set_error("uepm_assemble_device_noalloc: " + std::to_string(nk) + " k-points with basis " + std::to_string(t.N) +
