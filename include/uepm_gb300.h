@@ -144,11 +144,12 @@ int uepm_assemble_device(uepm_ctx* ctx, const double* d_k, size_t nk, double* d_
  * (a serving loop with memory reserved at start-up, a host program whose device memory belongs to its
  * own allocator): the per-plane-wave row table lives in a fixed 16 MiB device array of the library,
  * present on every GPU that loads it until exit, instead of a workspace grown on demand. Limit:
- * nk * N * 24 * 8 bytes <= UEPM_NOALLOC_SCRATCH_BYTES (e.g. 637 k-points per call for basis 137);
- * larger requests fail with UEPM_ERR_INVALID. The first call on a device looks up the array's
- * device address (with that device current) and should come before any stream capture. All calls
- * share the array: calls that overlap on the GPU race. The context must have been created (which
- * allocates) beforehand, with the same device current. */
+ * nk * N * 24 * 8 bytes <= UEPM_NOALLOC_SCRATCH_BYTES (e.g. 637 k-points per call for basis 137)
+ * and nk <= 32768; larger requests fail with UEPM_ERR_INVALID. The first call on a device looks up
+ * the array's device address (with that device current) and should come before any stream capture;
+ * the address is kept for the life of the process, so after cudaDeviceReset on a device this entry
+ * point must not be used there again. All calls share the array: calls that overlap on the GPU race.
+ * The context must have been created (which allocates) beforehand, with the same device current. */
 #define UEPM_NOALLOC_SCRATCH_BYTES (16u << 20)
 int uepm_assemble_device_noalloc(uepm_ctx* ctx, const double* d_k, size_t nk, double* d_H, void* stream);
 
@@ -189,6 +190,13 @@ int uepm_measure_peak(int precision, double* tflops);
  *   chunk         k-points per pipeline pass (smaller keeps H(k) resident in L2 between the
  *                 kernels of a pass), 64..32768
  *   cluster       CTAs per cluster of reduction 3: 2, 4, 8 or 16
+ *   max_iter      iteration cap (0..1000) of the iterative kernels: bisection steps per phase
+ *                 (automatic 64 / 200), inverse-iteration solves per vector (automatic 4 FP32, 5 FP64)
+ *                 and projected-Jacobi sweeps (automatic 12). A k-point whose iteration the cap ends
+ *                 before it converged gets UEPM_K_NOCONVERGE, and uepm_solve returns
+ *                 UEPM_ERR_NOT_CONVERGED (the reference throws "Eigenvalue decomposition failed"
+ *                 when Eigen reports NoConvergence, Hamiltonian.cpp:129-133). Not a shape: the
+ *                 autotuner keeps the context's value.
  * Every choice gives results within the parity tolerances; a given choice is deterministic.
  * uepm_ctx_autotune times candidate shapes on sample_k seeded random first-zone k-points (coordinate
  * descent over the fields, CUDA events on `stream`) and keeps the fastest; results are cached
@@ -200,6 +208,7 @@ typedef struct uepm_tuning {
     int32_t vector_lanes;
     int32_t chunk;
     int32_t cluster;
+    int32_t max_iter;
 } uepm_tuning;
 int uepm_ctx_get_tuning(const uepm_ctx* ctx, uepm_tuning* out);
 int uepm_ctx_set_tuning(uepm_ctx* ctx, const uepm_tuning* t);

@@ -19,6 +19,9 @@ UEPM_ERR_OUT_OF_RANGE = -3
 UEPM_ERR_CUDA = -4
 UEPM_ERR_NOMEM = -5
 UEPM_ERR_NOT_CONVERGED = -6
+UEPM_K_OK = 0
+UEPM_K_NOCONVERGE = 1  # an iteration cap ended an iterative kernel before it converged
+UEPM_K_NONFINITE = 2  # NaN / Inf reached H(k) or the reduction
 
 UEPM_NONLOCAL = 1
 UEPM_SOC = 2
@@ -67,7 +70,7 @@ class UepmTuning(C.Structure):
     """struct uepm_tuning (include/uepm_gb300.h); 0 in a field means automatic."""
 
     _fields_ = [("reduction", C.c_int32), ("ctas_per_sm", C.c_int32), ("vector_lanes", C.c_int32),
-                ("chunk", C.c_int32), ("cluster", C.c_int32)]
+                ("chunk", C.c_int32), ("cluster", C.c_int32), ("max_iter", C.c_int32)]
 
     def as_dict(self) -> dict:
         return {f: getattr(self, f) for f, _ in self._fields_}

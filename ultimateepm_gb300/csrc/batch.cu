@@ -56,6 +56,7 @@ bool valid_tuning(const uepm_ctx* ctx, const uepm_tuning& t) {
     if (t.cluster != 0 && t.cluster != 2 && t.cluster != 4 && t.cluster != 8 && t.cluster != 16) return false;
     if (t.vector_lanes != 0 && t.vector_lanes != 8 && t.vector_lanes != 16 && t.vector_lanes != 32) return false;
     if (t.chunk != 0 && (t.chunk < 64 || t.chunk > 32768)) return false;
+    if (t.max_iter < 0 || t.max_iter > 1000) return false;
     (void)ctx;
     return true;
 }
@@ -122,7 +123,9 @@ int uepm_ctx_autotune(uepm_ctx* ctx, int nb, uint32_t want, size_t sample_k, voi
         std::lock_guard<std::mutex> g(g_tune_mu);
         auto                        it = g_tune_cache.find(key);
         if (it != g_tune_cache.end()) {
-            ctx->tune = it->second;
+            const int32_t cap = ctx->tune.max_iter;
+            ctx->tune          = it->second;
+            ctx->tune.max_iter = cap;
             return UEPM_OK;
         }
     }
@@ -172,7 +175,8 @@ int uepm_ctx_autotune(uepm_ctx* ctx, int nb, uint32_t want, size_t sample_k, voi
         return UEPM_OK;
     };
 
-    uepm_tuning best = uepm_tuning{0, 0, 0, 0, 0};
+    uepm_tuning best = uepm_tuning{};
+    best.max_iter    = saved.max_iter;  // not a shape: kept as the caller set it
     ctx->tune        = best;
     double best_ms   = 0;
     rc               = timed(&best_ms);

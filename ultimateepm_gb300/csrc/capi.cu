@@ -240,14 +240,14 @@ void run_chunk(uepm_ctx* ctx, const Layout& L, char* ws, const double* kk, int c
         }
         {
             ProfScope p(ctx, s, KK_BISECT);
-            launch_bisect<double>(d, e, n, nb, E, nb, c, s);
+            launch_bisect<double>(d, e, n, nb, E, nb, c, s, ctx->tune.max_iter, st);
         }
         if (vec) {
             auto* work = reinterpret_cast<double*>(ws + L.work);
             auto* z    = reinterpret_cast<double*>(ws + L.z);
             {
                 ProfScope p(ctx, s, KK_INVIT);
-                launch_invit<double>(d, e, E, nb, n, nb, work, z, st, c, s);
+                launch_invit<double>(d, e, E, nb, n, nb, work, z, st, c, s, ctx->tune.max_iter);
             }
             ProfScope p(ctx, s, KK_BACKTRANSFORM);
             launch_backtransform<S>(H, n, n, mstride, tq, z, nb, Xo, ctx->P, kk, ctx->d_G, gr, c, s, ctx->tune.vector_lanes);
@@ -295,11 +295,11 @@ void run_chunk(uepm_ctx* ctx, const Layout& L, char* ws, const double* kk, int c
     }
     {
         ProfScope p(ctx, s, KK_BISECT);
-        launch_bisect<float>(d, e, n, m, ev, m, c, s);
+        launch_bisect<float>(d, e, n, m, ev, m, c, s, ctx->tune.max_iter, st);
     }
     {
         ProfScope p(ctx, s, KK_INVIT);
-        launch_invit<float>(d, e, ev, m, n, m, work, z, st, c, s);
+        launch_invit<float>(d, e, ev, m, n, m, work, z, st, c, s, ctx->tune.max_iter);
     }
     {
         ProfScope p(ctx, s, KK_BACKTRANSFORM);
@@ -315,7 +315,7 @@ void run_chunk(uepm_ctx* ctx, const Layout& L, char* ws, const double* kk, int c
     S* W = small + (size_t)2 * m * m;  // W block of the first matrix; matrices are refine_small_elems apart
     {
         ProfScope p(ctx, s, KK_SMALL_EIGH);
-        launch_small_eigh<S>(small, m, nb, E, vec ? W : nullptr, st, c, s);
+        launch_small_eigh<S>(small, m, nb, E, vec ? W : nullptr, st, c, s, ctx->tune.max_iter);
     }
     if (vec) {
         ProfScope p(ctx, s, KK_REFINE_VECTORS);

@@ -214,9 +214,11 @@ __device__ __forceinline__ cx<float> to_lower(cx<double> v) { return mk((float)v
 __device__ __forceinline__ double from_lower(float v) { return (double)v; }
 __device__ __forceinline__ cx<double> from_lower(cx<float> v) { return mk((double)v.x, (double)v.y); }
 
+// cap > 0 (UEPM tuning max_iter) bounds the Jacobi sweeps (automatic: 12); sweeps that end by the
+// cap with couplings still above the stopping threshold set UEPM_K_NOCONVERGE.
 template <typename S>
 __global__ void __launch_bounds__(32 * kSmallWarps) k_small_eigh(S* __restrict__ small, int m, int nb, double* __restrict__ Eout,
-                                                                 int want_w, int* __restrict__ status, int batch) {
+                                                                 int want_w, int* __restrict__ status, int batch, int cap) {
     using R         = double;
     const int warp  = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int b     = blockIdx.x * kSmallWarps + warp;
@@ -375,8 +377,10 @@ __global__ void __launch_bounds__(32 * kSmallWarps) k_small_eigh(S* __restrict__
     dia = warp_max(dia);
     // remaining off-diagonals move the Ritz values by at most ~off (degenerate pairs) or
     // off^2 / gap: 1e-10 of the largest diagonal is ~2e-9 eV here
-    R thr2 = (1e-10 * dia) * (1e-10 * dia);
-    for (int sweep = 0; sweep < 12; ++sweep) {
+    R          thr2      = (1e-10 * dia) * (1e-10 * dia);
+    const int  sweeps    = cap > 0 ? cap : 12;
+    bool       converged = false;
+    for (int sweep = 0; sweep < sweeps; ++sweep) {
         if (want_w) {
             R off2 = 0;
             dia    = 0;
@@ -388,7 +392,10 @@ __global__ void __launch_bounds__(32 * kSmallWarps) k_small_eigh(S* __restrict__
             off2 = warp_max(off2);
             dia  = warp_max(dia);
             thr2 = (1e-10 * dia) * (1e-10 * dia);
-            if (off2 <= thr2 || off2 == 0.0) break;
+            if (off2 <= thr2 || off2 == 0.0) {
+                converged = true;
+                break;
+            }
         }
         bool rotated = false;
         for (int round = 0; round < me - 1; ++round) {
@@ -489,7 +496,19 @@ __global__ void __launch_bounds__(32 * kSmallWarps) k_small_eigh(S* __restrict__
             }
             __syncwarp();
         }
-        if (!want_w && !rotated) break;
+        if (!want_w && !rotated) {
+            converged = true;
+            break;
+        }
+    }
+    if (!converged && want_w) {  // the cap ended the sweeps: one last check of the couplings
+        R off2 = 0;
+        for (int q = lane; q < m * m; q += 32) {
+            const int i = q / m, c = q - i * m;
+            if (i < c) off2 = fmax(off2, ST<S>::norm(CC(i, c)));
+        }
+        off2      = warp_max(off2);
+        converged = off2 <= thr2 || off2 == 0.0;
     }
     if (!want_w) {
         // lambda_p = C_pp + sum_q |C_pq|^2 / (C_pp - C_qq) over the couplings left above the
@@ -576,7 +595,9 @@ __global__ void __launch_bounds__(32 * kSmallWarps) k_small_eigh(S* __restrict__
         }
     }
     bad = __any_sync(0xffffffffu, bad);
-    if (bad && lane == 0 && status) atomicOr(status + b, 2);
+    // converged is warp-uniform (warp reductions and warp-uniform branches); a NaN coupling never
+    // compares below the threshold, so a non-finite matrix reports NONFINITE only
+    if (lane == 0 && status && (bad || !converged)) atomicOr(status + b, bad ? 2 : 1);
 #undef LL
 #undef CC
 #undef VV
@@ -646,12 +667,12 @@ void launch_refine_project(const typename Split<S>::type* H, int n, int ld, size
 }
 
 template <typename S>
-void launch_small_eigh(S* small, int m, int nb, double* Eout, S* W, int* status, int batch, cudaStream_t s) {
+void launch_small_eigh(S* small, int m, int nb, double* Eout, S* W, int* status, int batch, cudaStream_t s, int cap) {
     const size_t smem = small_eigh_warp_bytes<S>(m) * kSmallWarps;
     auto         kern = k_small_eigh<S>;
     if (smem > 48 * 1024) cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     kern<<<(batch + kSmallWarps - 1) / kSmallWarps, 32 * kSmallWarps, smem, s>>>(small, m, nb, Eout, W != nullptr, status,
-                                                                              batch);
+                                                                              batch, cap);
     count_launch();
 }
 
@@ -665,7 +686,7 @@ void launch_refine_vectors(int n, int m, int nb, const cx<float>* X32, const S* 
 #define UEPM_RF_INST(S)                                                                                             \
     template void launch_refine_project<S>(const typename Split<S>::type*, int, int, size_t, const cx<float>*, int, S*, S*, \
                                            int, cudaStream_t, const SparseV&);                                    \
-    template void launch_small_eigh<S>(S*, int, int, double*, S*, int*, int, cudaStream_t);                        \
+    template void launch_small_eigh<S>(S*, int, int, double*, S*, int*, int, cudaStream_t, int);                   \
     template void launch_refine_vectors<S>(int, int, int, const cx<float>*, const S*, cx<double>*, double*, const DevParams&, \
                                            const double*, const int*, int, cudaStream_t);
 UEPM_RF_INST(double)

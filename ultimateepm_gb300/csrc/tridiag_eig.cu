@@ -118,9 +118,13 @@ __device__ __forceinline__ dsf ds_of(double v) {
     return dsf{h, __double2float_rn(v - (double)h)};
 }
 
+// Iterations per bisection phase: `cap` when positive (UEPM tuning max_iter), else 64 for the FP32
+// and double-single pre-bracketing and 200 for the final phase (which needs ~60: the range over
+// eps ||T||). An eigenvalue whose final bracket is still open when the cap ends it sets
+// UEPM_K_NOCONVERGE in status; a non-finite bracket (NaN / Inf in T) sets UEPM_K_NONFINITE.
 template <typename T>
 __global__ void k_bisect(const T* __restrict__ dIn, const T* __restrict__ eIn, int n, int nb, int lpm, T* __restrict__ evOut,
-                         int ev_ld, int batch) {
+                         int ev_ld, int batch, int cap, int* __restrict__ status) {
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int mpw  = 32 / lpm;
     const int g    = lane / lpm, gl = lane - g * lpm;
@@ -173,7 +177,10 @@ __global__ void k_bisect(const T* __restrict__ dIn, const T* __restrict__ eIn, i
     const T widen  = T(2) * eps * tnorm * T(n) + T(2) * pivmin;
     lo -= widen;
     hi += widen;
-    const T atol = eps * tnorm;
+    const T   atol    = eps * tnorm;
+    const int it_pre  = cap > 0 ? min(cap, 64) : 64;
+    const int it_last = cap > 0 ? cap : 200;
+    int       flags   = 0;
     for (int j = gl; j < nb; j += lpm) {
         T a = lo, c = hi;
         if (sizeof(T) == 8) {
@@ -183,7 +190,7 @@ __global__ void k_bisect(const T* __restrict__ dIn, const T* __restrict__ eIn, i
             const float pivf = FLT_MIN * fmaxf(1.f, (float)emax2);
             const float tolf = 4.f * FLT_EPSILON * (float)tnorm;
             float       af = (float)a, cf = (float)c;
-            for (int it = 0; it < 64; ++it) {
+            for (int it = 0; it < it_pre; ++it) {
                 const float mf = 0.5f * (af + cf);
                 if (cf - af <= tolf || mf <= af || mf >= cf) break;
                 if (sturm_count(df, e2f, n, mf, pivf) > j) cf = mf;
@@ -198,7 +205,7 @@ __global__ void k_bisect(const T* __restrict__ dIn, const T* __restrict__ eIn, i
                 // that error and keep the bracket only if two FP64 counts confirm it
                 const T ulp_ds = T(3.552713678800501e-15) * tnorm;  // 2^-48 ||T||
                 T       ad = a, cd = c;
-                for (int it = 0; it < 64; ++it) {
+                for (int it = 0; it < it_pre; ++it) {
                     const T mid = T(0.5) * (ad + cd);
                     if (cd - ad <= T(64) * ulp_ds || mid <= ad || mid >= cd) break;
                     if (sturm_count_ds(df, dlo, e2f, e2lo, n, ds_of((double)mid), pivf) > j) cd = mid;
@@ -212,19 +219,28 @@ __global__ void k_bisect(const T* __restrict__ dIn, const T* __restrict__ eIn, i
             }
         }
         // count(a) <= j < count(c) holds throughout; at most ~log2(range / atol) < 200 steps.
-        for (int it = 0; it < 200; ++it) {
+        bool done = false;
+        for (int it = 0; it < it_last && !done; ++it) {
             const T mid = T(0.5) * (a + c);
             const T tol = max(atol, T(2) * eps * max(fabs(a), fabs(c)));
-            if (c - a <= tol || mid <= a || mid >= c) break;
+            done        = c - a <= tol || mid <= a || mid >= c;
+            if (done) break;
             if (sturm_count(d, e2, n, mid, pivmin) > j) c = mid;
             else a = mid;
         }
+        if (!done) {
+            const T mid = T(0.5) * (a + c);
+            done        = c - a <= max(atol, T(2) * eps * max(fabs(a), fabs(c))) || mid <= a || mid >= c;
+        }
+        if (!isfinite(a) || !isfinite(c)) flags |= 2;       // UEPM_K_NONFINITE
+        else if (!done) flags |= 1;                         // UEPM_K_NOCONVERGE
         evOut[(size_t)b * ev_ld + j] = T(0.5) * (a + c);
     }
+    if (flags && status) atomicOr(status + b, flags);
 }
 
 template <typename T>
-void launch_bisect(const T* d, const T* e, int n, int nb, T* ev, int ev_ld, int batch, cudaStream_t s) {
+void launch_bisect(const T* d, const T* e, int n, int nb, T* ev, int ev_ld, int batch, cudaStream_t s, int cap, int* status) {
     // lanes per matrix: >= nb (one lane per eigenvalue) and large enough that the d / e^2 copies
     // of the warp's matrices fit in 96 KB of shared memory per block
     const int max_mpw = (int)std::max<size_t>(1, (96 * 1024) / (bisect_matrix_bytes<T>(n) * kBisectWarpsPerBlock));
@@ -236,7 +252,7 @@ void launch_bisect(const T* d, const T* e, int n, int nb, T* ev, int ev_ld, int 
     const size_t smem   = bisect_matrix_bytes<T>(n) * mpw * kBisectWarpsPerBlock;
     auto         kern   = k_bisect<T>;
     if (smem > 48 * 1024) cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    kern<<<blocks, 32 * kBisectWarpsPerBlock, smem, s>>>(d, e, n, nb, lpm, ev, ev_ld, batch);
+    kern<<<blocks, 32 * kBisectWarpsPerBlock, smem, s>>>(d, e, n, nb, lpm, ev, ev_ld, batch, cap, status);
     count_launch();
 }
 
@@ -287,9 +303,11 @@ __host__ __device__ inline size_t invit_smem_bytes(int n, int ls) {
     return sizeof(T) * (4 * (size_t)n * ls + 2 * (size_t)n) + sizeof(unsigned) * (size_t)((n + 31) / 32) * ls;
 }
 
+// cap > 0 (UEPM tuning max_iter) bounds the solves per vector; a vector that would need more than
+// the cap (NIT, or the extra solves after a lossy Gram-Schmidt step) sets UEPM_K_NOCONVERGE.
 template <typename T, bool SMEM>
 __global__ void k_invit(const T* __restrict__ dIn, const T* __restrict__ eIn, const T* __restrict__ ev, int ev_ld, int n,
-                        int nb, T* __restrict__ work, T* __restrict__ zOut, int* __restrict__ status, int batch) {
+                        int nb, T* __restrict__ work, T* __restrict__ zOut, int* __restrict__ status, int batch, int cap) {
     constexpr int WPB  = SMEM ? 1 : kInvitWarpsPerBlock;
     constexpr int NIT  = InvitIters<T>::value;
     const int     warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -345,8 +363,10 @@ __global__ void k_invit(const T* __restrict__ dIn, const T* __restrict__ eIn, co
     const T ptight = T(8) * eps * onenrm;  // consecutive gaps below this form a group
     const T poff   = ptight;               // smallest offset of a group's shared shift
     // largest |z| for which sum z^2 stays finite
-    const T zsafe = sizeof(T) == 4 ? T(1e17) : T(1e150);
-    bool    bad   = false;
+    const T   zsafe  = sizeof(T) == 4 ? T(1e17) : T(1e150);
+    bool      bad    = false;
+    bool      capped = false;  // warp-uniform: a vector wanted more solves than the cap allows
+    const int maxit  = cap > 0 ? cap : NIT + 2;
 
     // carried across groups of 32: the previous shift, eigenvalue and cluster start
     T   prev_lam = T(0), prev_ev = T(0);
@@ -406,8 +426,9 @@ __global__ void k_invit(const T* __restrict__ dIn, const T* __restrict__ eIn, co
             }
         __syncwarp();
 
-        T   sc   = T(1);  // pending scale of Z
-        int need = NIT;   // solves to run (raised after a Gram-Schmidt step that kept little)
+        T   sc   = T(1);              // pending scale of Z
+        int need = min(NIT, maxit);   // solves to run (raised after a Gram-Schmidt step that kept little)
+        capped |= NIT > maxit;
         for (int it = 0; it < need; ++it) {
             if (active) {
                 T rp = AT(Z, 0) * sc;
@@ -525,8 +546,11 @@ __global__ void k_invit(const T* __restrict__ dIn, const T* __restrict__ eIn, co
                 // removes most of a vector (close groups still turning into each other) gets one
                 // more. At most NIT + 2 solves in all; kept2 is warp-uniform (warp sums), so the
                 // trip count stays uniform.
-                if (kept2 < T(kGsKeep * kGsKeep)) need = min(NIT + 2, max(need, it + 3));
-                else if (it == need - 1 && kept2 < T(kGsSettle * kGsSettle)) need = min(NIT + 2, it + 2);
+                int want_n = need;
+                if (kept2 < T(kGsKeep * kGsKeep)) want_n = min(NIT + 2, max(need, it + 3));
+                else if (it == need - 1 && kept2 < T(kGsSettle * kGsSettle)) want_n = min(NIT + 2, it + 2);
+                capped |= want_n > maxit;
+                need = min(want_n, maxit);
             }
         }
         // write this group's vectors ([j][i], coalesced over i), with the pending scale
@@ -540,29 +564,29 @@ __global__ void k_invit(const T* __restrict__ dIn, const T* __restrict__ eIn, co
     }
 #undef AT
     bad = __any_sync(0xffffffffu, bad);
-    if (bad && lane == 0 && status) status[b] |= 2;  // UEPM_K_NONFINITE
+    if (lane == 0 && status && (bad || capped)) status[b] |= (bad ? 2 : 0) | (capped ? 1 : 0);  // NONFINITE, NOCONVERGE
 }
 
 template <typename T>
 void launch_invit(const T* d, const T* e, const T* ev, int ev_ld, int n, int nb, T* work, T* z, int* status, int batch,
-                  cudaStream_t s) {
+                  cudaStream_t s, int cap) {
     const size_t smem = invit_smem_bytes<T>(n, std::min(nb, 32));
     if (smem <= 200 * 1024) {
         auto kern = k_invit<T, true>;
         if (smem > 48 * 1024) cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        kern<<<batch, 32, smem, s>>>(d, e, ev, ev_ld, n, nb, work, z, status, batch);
+        kern<<<batch, 32, smem, s>>>(d, e, ev, ev_ld, n, nb, work, z, status, batch, cap);
     } else {
         const int blocks = (batch + kInvitWarpsPerBlock - 1) / kInvitWarpsPerBlock;
-        k_invit<T, false><<<blocks, 32 * kInvitWarpsPerBlock, 0, s>>>(d, e, ev, ev_ld, n, nb, work, z, status, batch);
+        k_invit<T, false><<<blocks, 32 * kInvitWarpsPerBlock, 0, s>>>(d, e, ev, ev_ld, n, nb, work, z, status, batch, cap);
     }
     count_launch();
 }
 
-template void launch_bisect<double>(const double*, const double*, int, int, double*, int, int, cudaStream_t);
-template void launch_bisect<float>(const float*, const float*, int, int, float*, int, int, cudaStream_t);
+template void launch_bisect<double>(const double*, const double*, int, int, double*, int, int, cudaStream_t, int, int*);
+template void launch_bisect<float>(const float*, const float*, int, int, float*, int, int, cudaStream_t, int, int*);
 template void launch_invit<double>(const double*, const double*, const double*, int, int, int, double*, double*, int*, int,
-                                   cudaStream_t);
+                                   cudaStream_t, int);
 template void launch_invit<float>(const float*, const float*, const float*, int, int, int, float*, float*, int*, int,
-                                  cudaStream_t);
+                                  cudaStream_t, int);
 
 }  // namespace uepm

@@ -52,10 +52,11 @@ void launch_tridiag_reg_local(const float* V32, const cx<double>* Vloc, const do
 
 // tridiag_eig.cu
 template <typename T>
-void launch_bisect(const T* d, const T* e, int n, int nb, T* ev, int ev_ld, int batch, cudaStream_t s);
+void launch_bisect(const T* d, const T* e, int n, int nb, T* ev, int ev_ld, int batch, cudaStream_t s, int cap = 0,
+                   int* status = nullptr);
 template <typename T>
 void launch_invit(const T* d, const T* e, const T* ev, int ev_ld, int n, int nb, T* work, T* z, int* status, int batch,
-                  cudaStream_t s);
+                  cudaStream_t s, int cap = 0);
 // Inverse-iteration workspace per matrix (used where the arrays exceed shared memory): U0, U1, the
 // multipliers and Z, each n x 32 interleaved by lane, and the row-interchange bits.
 template <typename T>
@@ -97,7 +98,7 @@ template <typename S>
 void launch_refine_project(const typename Split<S>::type* H, int n, int ld, size_t mstride, const cx<float>* X32, int m,
                            S* work, S* small, int batch, cudaStream_t s, const SparseV& sv);
 template <typename S>
-void launch_small_eigh(S* small, int m, int nb, double* Eout, S* W, int* status, int batch, cudaStream_t s);
+void launch_small_eigh(S* small, int m, int nb, double* Eout, S* W, int* status, int batch, cudaStream_t s, int cap = 0);
 template <typename S>
 void launch_refine_vectors(int n, int m, int nb, const cx<float>* X32, const S* W, cx<double>* Xout, double* grad,
                            const DevParams& P, const double* d_k, const int* d_G, int batch, cudaStream_t s);
