@@ -183,8 +183,11 @@ int uepm_measure_peak(int precision, double* tflops);
  *                 the cluster's shared memory (orders beyond one SM), 4 one CTA per matrix in global
  *                 memory with each step's update fused into the next step's product (FP32 matrices
  *                 beyond the on-chip sizes, n <= 512), 5 the same with every other update deferred
- *                 to the next pass (a read-only pass, then a rank-4 pass: 3 passes per two steps);
- *                 automatic: 1 where it applies, 5 for the other FP32 matrices up to n = 512, else 2
+ *                 to the next pass (a read-only pass, then a rank-4 pass: 3 passes per two steps), 6 blocked:
+ *                 panels of 16 columns whose updates are applied once per panel, only the lower
+ *                 triangle read and written, one matrix per SM (FP32, n <= 512);
+ *                 automatic: 1 where it applies, 6 for the FP32 orders 300..512, 5 for the other FP32
+ *                 matrices, else 2
  *   ctas_per_sm   CTAs per SM of the global-memory reduction (its L2 working set), 1..8
  *   vector_lanes  lanes per eigenvector in the back-transformation: 8, 16 or 32
  *   chunk         k-points per pipeline pass (smaller keeps H(k) resident in L2 between the

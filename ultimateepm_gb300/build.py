@@ -29,7 +29,7 @@ NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompil
 PER_FILE = {"assemble.cu": ["--fmad=false"]}
 CXX_FLAGS = ["-O3", "-std=c++17", "-fPIC", "-Wall", "-I" + INCLUDE, "-I" + CSRC]
 
-CU_SOURCES = ["assemble.cu", "tridiag.cu", "tridiag_reg.cu", "tridiag_cluster.cu", "tridiag_eig.cu", "backtransform.cu", "refine.cu", "capi.cu", "batch.cu", "server.cu", "star.cu", "peak.cu",
+CU_SOURCES = ["assemble.cu", "tridiag.cu", "tridiag_reg.cu", "tridiag_cluster.cu", "tridiag_blocked.cu", "tridiag_eig.cu", "backtransform.cu", "refine.cu", "capi.cu", "batch.cu", "server.cu", "star.cu", "peak.cu",
               "noalloc.cu", "dielectric.cu"]
 CXX_SOURCES = ["host.cpp"]
 

@@ -51,7 +51,7 @@ TuneKey tune_key(const uepm_ctx* ctx, int nb, uint32_t want) {
 }
 
 bool valid_tuning(const uepm_ctx* ctx, const uepm_tuning& t) {
-    if (t.reduction < 0 || t.reduction > 5) return false;
+    if (t.reduction < 0 || t.reduction > 6) return false;
     if (t.ctas_per_sm < 0 || t.ctas_per_sm > 8) return false;
     if (t.cluster != 0 && t.cluster != 2 && t.cluster != 4 && t.cluster != 8 && t.cluster != 16) return false;
     if (t.vector_lanes != 0 && t.vector_lanes != 8 && t.vector_lanes != 16 && t.vector_lanes != 32) return false;
@@ -188,7 +188,7 @@ int uepm_ctx_autotune(uepm_ctx* ctx, int nb, uint32_t want, size_t sample_k, voi
     std::vector<int> chunks, reds, ctas, lanes, clusters;
     for (int c : {256, 512, 1024, 2048, 4096, 8192})
         if ((size_t)c < sample_k) chunks.push_back(c);
-    reds = mixed ? std::vector<int>{2, 3, 4, 5} : std::vector<int>{2, 3};  // 4, 5: FP32 only
+    reds = mixed ? std::vector<int>{2, 3, 4, 5, 6} : std::vector<int>{2, 3};  // 4, 5, 6: FP32 only
     ctas = {1, 2, 4, 6, 8};
     for (int c : {2, 4, 8, 16})
         if ((size_t)es * ctx->n * ((ctx->n + c - 1) / c) <= (200u << 10)) clusters.push_back(c);

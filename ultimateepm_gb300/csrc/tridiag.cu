@@ -785,6 +785,12 @@ void launch_tridiag(S* H, int n, int ld, size_t mstride, typename ST<S>::R* d, t
     // update deferred, 3 passes per two steps, 5 and automatic). Reduction time per 2000 k: Ge SOC
     // n = 362 222 ms unfused, 102.7 fused, 81.3 deferred; GaP SOC n = 458 230.6 -> 198.3 ms.
     if constexpr (F32) {
+        // the blocked kernel (6) is automatic from order 300 (2000 k, mixed: Ge SOC n = 362 81.3 ->
+        // 47.5 ms, Si SOC n = 338 67.1 -> 41.7, GaP SOC n = 458 198.3 -> 81.8); below, the deferred
+        // kernel stays ahead (GaAs SOC n = 178 9.5 against 12.6 ms, InAs n = 229 equal)
+        if ((variant == 6 || (variant == 0 && n >= 300)) &&
+            launch_tridiag_blocked<S>(H, n, ld, mstride, d, e, tq, status, batch, s))
+            return;
         // automatic: the deferred kernel for every FP32 order beyond the register kernel, also where
         // the matrix would fit shared memory (2000 k: Ge nonlocal n = 181 real 5.85 ms against 14.3
         // for the shared-memory kernel; InP n = 113 complex 2.37 against 3.27; GaAs n = 89 complex

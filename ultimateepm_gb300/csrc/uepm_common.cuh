@@ -72,6 +72,8 @@ __device__ __forceinline__ void stc(cx<float>* p, cx<float> a) { *reinterpret_ca
 // matrices (H(k) is exactly real for diamond-structure local / symmetric-nonlocal EPM without SOC).
 __device__ __forceinline__ double cadd(double a, double b) { return a + b; }
 __device__ __forceinline__ float cadd(float a, float b) { return a + b; }
+__device__ __forceinline__ double csub(double a, double b) { return a - b; }
+__device__ __forceinline__ float csub(float a, float b) { return a - b; }
 __device__ __forceinline__ double cmul(double a, double b) { return a * b; }
 __device__ __forceinline__ float cmul(float a, float b) { return a * b; }
 __device__ __forceinline__ double cfma(double a, double b, double c) { return fma(a, b, c); }

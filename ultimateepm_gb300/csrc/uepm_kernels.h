@@ -25,8 +25,9 @@ void launch_assemble(const DevParams& P, const cx<double>* Vloc, const double2* 
 // matrix (shared memory where the matrix fits, else global memory with a persistent grid), 3 one
 // thread-block cluster per matrix (tridiag_cluster.cu), 4 one CTA per matrix in global memory with
 // each step's update fused into the next step's product (FP32, n <= 512), 5 the same with every
-// other update deferred to the next pass. Automatic: 1 where it applies, 5 for the other FP32
-// matrices up to n = 512, else 2. ctas_per_sm (0: automatic) caps the
+// other update deferred to the next pass, 6 blocked (panels of 16 columns, lower triangle only, one
+// matrix per SM, tridiag_blocked.cu; FP32, n <= 512). Automatic: 1 where it applies, 6 for FP32 orders
+// 300..512, 5 for the other FP32 matrices, else 2. ctas_per_sm (0: automatic) caps the
 // persistent grid of the global-memory kernels; cluster (0: automatic) is the cluster size of
 // variant 3.
 template <typename S>
@@ -39,6 +40,11 @@ int tridiag_cluster_size(int n, int want);
 template <typename S>
 bool launch_tridiag_cluster(S* H, int n, int ld, size_t mstride, typename ST<S>::R* d, typename ST<S>::R* e, S* tq,
                             int* status, int batch, cudaStream_t s, int want_c);
+// tridiag_blocked.cu: the blocked reduction (false when it cannot run this order).
+int tridiag_blocked_max_n();
+template <typename S>
+bool launch_tridiag_blocked(S* H, int n, int ld, size_t mstride, typename ST<S>::R* d, typename ST<S>::R* e, S* tq,
+                            int* status, int batch, cudaStream_t s);
 // tridiag_reg.cu: the same reduction for real FP32 matrices with n <= tridiag_reg_max_n(), held in
 // registers (launch_tridiag<float> dispatches to it).
 int  tridiag_reg_max_n();
