@@ -157,6 +157,12 @@ int uepm_assemble_device_noalloc(uepm_ctx* ctx, const double* d_k, size_t nk, do
  * and whether FindBandGap succeeded via *found. soc selects 8 instead of 4 valence bands. */
 int uepm_adjust_values(double* E, size_t nk, int nb, int soc, int min_cond_zero, double* gap, int* found);
 
+/* Diagnostics (no reference counterpart): the FP64 Sturm count's pivot step, r = 1 / guard(q), for
+ * n device values q (guard: a pivot within pivmin becomes -pivmin, as in the bisection), written to
+ * device r, enqueued on `stream`. Exposes the refined hardware reciprocal the bisection uses so that
+ * tests can bound it against the correctly rounded 1.0 / q. pivmin must be positive. */
+int uepm_pivot_reciprocal_device(const double* d_q, double pivmin, size_t n, double* d_r, void* stream);
+
 /* Launch counters (kernels enqueued by this library since load), for launch accounting. */
 uint64_t uepm_kernel_launches(void);
 

@@ -23,11 +23,14 @@ LIB = os.path.join(OUT, "libuepm_gb300.so")
 EPP_LIB = os.path.join(OUT, "libuepm_epp.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-Wall",
+NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-Wall", "-Xcompiler",
+              "-ffp-contract=off",
               "--extended-lambda", "-I" + INCLUDE, "-I" + CSRC]
 # assemble.cu mirrors the reference's operand order and rounding: no FMA contraction there.
 PER_FILE = {"assemble.cu": ["--fmad=false"]}
-CXX_FLAGS = ["-O3", "-std=c++17", "-fPIC", "-Wall", "-I" + INCLUDE, "-I" + CSRC]
+# Host code: no FMA contraction, so the k-paths and the other host results are the same bits on
+# x86 and Arm (gcc contracts a * b + c into one fma by default where the target has one).
+CXX_FLAGS = ["-O3", "-std=c++17", "-fPIC", "-Wall", "-ffp-contract=off", "-I" + INCLUDE, "-I" + CSRC]
 
 CU_SOURCES = ["assemble.cu", "tridiag.cu", "tridiag_reg.cu", "tridiag_cluster.cu", "tridiag_blocked.cu", "tridiag_eig.cu", "backtransform.cu", "refine.cu", "capi.cu", "batch.cu", "server.cu", "star.cu", "peak.cu",
               "noalloc.cu", "dielectric.cu"]
@@ -93,7 +96,7 @@ def build(verbose: bool = False, jobs: int | None = None) -> str:
         ahdrs = [os.path.join(INCLUDE, "uepm", f) for f in os.listdir(os.path.join(INCLUDE, "uepm"))] \
             if os.path.isdir(os.path.join(INCLUDE, "uepm")) else []
         if asrcs and _stale(EPP_LIB, asrcs + ahdrs + [LIB]):
-            cmd = ["g++", "-O2", "-std=c++20", "-fPIC", "-shared", "-Wall", "-I" + INCLUDE,
+            cmd = ["g++", "-O2", "-std=c++20", "-fPIC", "-shared", "-Wall", "-ffp-contract=off", "-I" + INCLUDE,
                    "-I" + os.path.join(INCLUDE, "uepm"), *asrcs, "-o", EPP_LIB,
                    "-L" + OUT, "-luepm_gb300", "-Wl,-rpath,$ORIGIN"]
             if verbose:

@@ -25,27 +25,41 @@ namespace uepm {
 constexpr int kBisectWarpsPerBlock = 4;
 constexpr int kInvitWarpsPerBlock  = 2;
 
+// Reciprocal of a Sturm-count pivot: PTX's rcp.approx.ftz.f64 as the start value, refined by two
+// Newton-Raphson steps for 1/q written with fused multiply-adds, e = 1 - q r, r <- r + r e (the
+// relative error squares at every step; the fma form of P. Markstein, "Computation of elementary
+// functions on the IBM RISC System/6000 processor", IBM J. Res. Dev. 34 (1990) 111-119). The pivots
+// that reach it are normal numbers, |q| > pivmin >= DBL_MIN (the guard below replaces smaller ones);
+// where 1/q itself would be subnormal (|q| > 2^1022) the approximation flushes it to zero, a
+// perturbation of e^2 / q below 2^-1022. The GPU test of uepm_pivot_reciprocal_device bounds the
+// result against the correctly rounded 1.0 / q over the whole pivot range.
+__device__ __forceinline__ double sturm_rcp(double q) {
+    double r;
+    asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(r) : "d"(q));
+    double er = fma(-q, r, 1.0);
+    r         = fma(r, er, r);
+    er        = fma(-q, r, 1.0);
+    return fma(r, er, r);
+}
+// The pivot guard of the Sturm count (dstebz): a pivot within pivmin becomes -pivmin. It compares
+// the high words (sign cleared), so it also catches pivots slightly above pivmin.
+__device__ __forceinline__ double sturm_guard(double q, int piv_hi, double pivmin) {
+    return ((__double2hiint(q) & 0x7fffffff) <= piv_hi) ? -pivmin : q;
+}
+
 // Sturm count: the number of eigenvalues of T below x, from the LDL^T pivots
 // q_0 = d_0 - x, q_i = (d_i - x) - e_{i-1}^2 / q_{i-1} (pivots within pivmin replaced by -pivmin).
-// FP64: 1 / q comes from the hardware reciprocal approximation refined by two Newton steps (relative
-// error far below 1e-20, i.e. a backward perturbation of e^2 well under the tolerance), and the
+// FP64: 1 / q from sturm_rcp (a backward perturbation of e^2 far below the tolerance), and the
 // pivot guard and sign test use integer compares on the high word, so a step issues 6 FP64
 // instructions instead of a full IEEE division sequence.
 __device__ __forceinline__ int sturm_count(const double* __restrict__ d, const double* __restrict__ e2, int n, double x,
                                            double pivmin) {
     const int piv_hi = __double2hiint(pivmin);
-    double    q      = d[0] - x;
-    if ((__double2hiint(q) & 0x7fffffff) <= piv_hi) q = -pivmin;
-    int cnt = (int)((unsigned)__double2hiint(q) >> 31);
+    double    q      = sturm_guard(d[0] - x, piv_hi, pivmin);
+    int       cnt    = (int)((unsigned)__double2hiint(q) >> 31);
     for (int i = 1; i < n; ++i) {
-        double r;
-        asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(r) : "d"(q));
-        double er = fma(-q, r, 1.0);
-        r         = fma(r, er, r);
-        er        = fma(-q, r, 1.0);
-        r         = fma(r, er, r);
-        q         = fma(-e2[i - 1], r, d[i] - x);
-        if ((__double2hiint(q) & 0x7fffffff) <= piv_hi) q = -pivmin;
+        const double r = sturm_rcp(q);
+        q              = sturm_guard(fma(-e2[i - 1], r, d[i] - x), piv_hi, pivmin);
         cnt += (int)((unsigned)__double2hiint(q) >> 31);
     }
     return cnt;
@@ -590,3 +604,20 @@ template void launch_invit<float>(const float*, const float*, const float*, int,
                                   cudaStream_t, int);
 
 }  // namespace uepm
+
+// ------------------------------------------------------------------------------------------------
+namespace {
+__global__ void k_pivot_reciprocal(const double* __restrict__ q, double pivmin, size_t n, double* __restrict__ r) {
+    const size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < n) r[t] = uepm::sturm_rcp(uepm::sturm_guard(q[t], __double2hiint(pivmin), pivmin));
+}
+}  // namespace
+
+extern "C" int uepm_pivot_reciprocal_device(const double* d_q, double pivmin, size_t n, double* d_r, void* stream) {
+    if (n == 0) return 0;
+    if (!d_q || !d_r || !(pivmin > 0.0)) return -1;  // UEPM_ERR_INVALID
+    const unsigned blocks = (unsigned)((n + 255) / 256);
+    k_pivot_reciprocal<<<blocks, 256, 0, (cudaStream_t)stream>>>(d_q, pivmin, n, d_r);
+    uepm::count_launch();
+    return cudaGetLastError() == cudaSuccess ? 0 : -4;  // UEPM_ERR_CUDA
+}
