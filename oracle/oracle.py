@@ -168,12 +168,31 @@ def build():
         subprocess.run(["make", "-s", "-C", HERE, "ref"], check=True, env=env)
 
 
+_fast = None
+
+
+def fast_lib():
+    """The same restatement built with the reference's Release numerics flags (-O3 -ffast-math,
+    OpenMP): the timed CPU baseline only, never a parity checker."""
+    global _fast
+    if _fast is None:
+        if not os.path.exists(FAST_LIB_PATH):
+            build()
+        _fast = _bind(C.CDLL(FAST_LIB_PATH))
+    return _fast
+
+
 def lib():
     global _lib
     if _lib is None:
         if not os.path.exists(LIB_PATH):
             build()
-        L = C.CDLL(LIB_PATH)
+        _lib = _bind(C.CDLL(LIB_PATH))
+    return _lib
+
+
+def _bind(L):
+    if True:
         dp = C.POINTER(C.c_double)
         ip = C.POINTER(C.c_int32)
         mp = C.POINTER(OrMaterial)
@@ -210,8 +229,7 @@ def lib():
         L.or_generate_path.argtypes = [C.c_char_p, C.c_uint, dp, C.c_int, C.POINTER(C.c_uint32)]
         L.or_generate_path.restype = C.c_int
         assert L.or_material_size() == C.sizeof(OrMaterial)
-        _lib = L
-    return _lib
+    return L
 
 
 def ref_lib():
@@ -301,9 +319,10 @@ def eigh(H: np.ndarray, vectors=False):
 
 
 def band_structure(mat: OrMaterial, G: np.ndarray, kpts: np.ndarray, nb: int, nl=False, soc=False,
-                   grad=False, vectors=False, nthreads=None):
-    """BandStructure::Compute_parallel over kpts -> dict(E [nk,nb], grad, vecs, status)."""
-    L = lib()
+                   grad=False, vectors=False, nthreads=None, fast=False):
+    """BandStructure::Compute_parallel over kpts -> dict(E [nk,nb], grad, vecs, status). fast: the
+    Release-flags build (timing only)."""
+    L = fast_lib() if fast else lib()
     G = np.ascontiguousarray(G, dtype=np.int32)
     k = np.ascontiguousarray(kpts, dtype=np.float64).reshape(-1, 3)
     nk = k.shape[0]
