@@ -285,23 +285,6 @@ __device__ __forceinline__ cx<float> copy32(ds4 v) { return mk(v.rhi, v.ihi); }
 __device__ __forceinline__ float copy32(double v) { return (float)v; }
 __device__ __forceinline__ cx<float> copy32(cx<double> v) { return mk((float)v.x, (float)v.y); }
 
-// Writes element (r, c) of the full matrix and, when r != c, its Hermitian mirror (c, r). The
-// element is converted to its stored form once; the mirror and the FP32 copy are taken from that
-// form (a sign flip, the hi parts), the same values as converting each separately, since rounding
-// commutes with negation (conversions run at the FP64 rate).
-template <typename SO, typename SF>
-__device__ __forceinline__ void put_pair(SO* Hb, SF* Fb, int ld, int r, int c, cx<double> h) {
-    const SO v = stored(Hb, h);
-    Hb[(size_t)c * ld + r] = v;
-    if (Fb) Fb[(size_t)c * ld + r] = copy32(v);
-    if (r != c) {
-        const SO w = conj_stored(v);
-        Hb[(size_t)r * ld + c] = w;
-        if (Fb) Fb[(size_t)r * ld + c] = copy32(w);
-    }
-}
-
-
 // Without spin-orbit coupling: one CTA per 32 x 32 tile of the lower triangle, 32 x 8 threads, four
 // elements per thread. The tile is written directly (coalesced down its columns) and, through a
 // shared-memory transpose, as its Hermitian mirror (coalesced down the mirror's columns), so no
@@ -350,33 +333,78 @@ __global__ void __launch_bounds__(256) k_assemble_tiles(const DevParams P, const
     }
 }
 
-template <bool NL, bool SOC, typename SO>
-__global__ void k_assemble(const DevParams P, const cx<double>* __restrict__ Vloc, const double2* __restrict__ phNL,
-                           const double2* __restrict__ phSO, const double* __restrict__ rows, SO* __restrict__ H, int ld,
-                           size_t mstride, typename Lower<SO>::type* __restrict__ H32, size_t mstride32, int batch) {
-    using SF    = typename Lower<SO>::type;
-    const int i = blockIdx.x * 32 + threadIdx.x;
-    const int j = blockIdx.y * 8 + threadIdx.y;
-    const int b = blockIdx.z;
-    const int N = P.N;
-    if (i >= N || j >= N || i < j || b >= batch) return;
-    const double* Ri = rows + ((size_t)b * N + i) * ROW_STRIDE;
-    const double* Rj = rows + ((size_t)b * N + j) * ROW_STRIDE;
-    const cx<double> h = scalar_element<NL>(P, Vloc, phNL, rows, b, i, j);
-    SO* Hb = H + (size_t)b * mstride;
-    SF* Fb = H32 ? H32 + (size_t)b * mstride32 : nullptr;
-    if (!SOC) {
-        put_pair(Hb, Fb, ld, i, j, h);
-        return;
+// With spin-orbit coupling: the same tiling over the scalar problem's lower triangle. Each scalar
+// element (i, j), i >= j, yields four blocks' elements, UU(i, j) = h + s00, DD(i, j) = h + s11,
+// DU(i, j) = s10 and UD(i, j) = s01 (i > j), written directly at (i, j), (i + N, j + N), (i + N, j)
+// and (i, j + N), coalesced down their columns; their Hermitian mirrors (j, i), (j + N, i + N),
+// (j, i + N) and (j + N, i) go through a shared-memory transpose. On the diagonal (i = j) the
+// mirror of DU(i, i) fills (i, i + N), as in the element-per-thread form.
+template <bool NL, typename SO>
+__global__ void __launch_bounds__(256) k_assemble_soc_tiles(const DevParams P, const cx<double>* __restrict__ Vloc,
+                                                            const double2* __restrict__ phNL,
+                                                            const double2* __restrict__ phSO, const double* __restrict__ rows,
+                                                            SO* __restrict__ H, int ld, size_t mstride,
+                                                            typename Lower<SO>::type* __restrict__ H32,
+                                                            size_t mstride32, int batch) {
+    using SF = typename Lower<SO>::type;
+    extern __shared__ __align__(16) unsigned char smraw[];
+    SO(*tile)[32][33] = reinterpret_cast<SO(*)[32][33]>(smraw);  // [4][jl][il]: UU, DD, DU, UD of h(i, j)
+    const int b = blockIdx.y;
+    if (b >= batch) return;
+    int t = blockIdx.x, ti = 0;
+    while (t > ti) {
+        t -= ti + 1;
+        ++ti;
     }
-    // 2N x 2N: [[UU, UD], [DU, DD]] with UU = H + s00, DD = H + s11, DU = s10, UD = DU^H
-    const double2 ph = phSO[(size_t)j * N + i];
-    cx<double>    s[4];
-    soc_element(P, Ri, Rj, ph.x, ph.y, s);
-    put_pair(Hb, Fb, ld, i, j, mk(h.x + s[0].x, h.y + s[0].y));          // UU(i, j), UU(j, i)
-    put_pair(Hb, Fb, ld, i + N, j + N, mk(h.x + s[3].x, h.y + s[3].y));  // DD(i, j), DD(j, i)
-    put_pair(Hb, Fb, ld, i + N, j, s[2]);                                // DU(i, j), UD(j, i)
-    if (i > j) put_pair(Hb, Fb, ld, j + N, i, conjd(s[1]));             // DU(j, i) = conj(UD(i, j))
+    const int tj = t;
+    const int N  = P.N;
+    const int tx = threadIdx.x, ty = threadIdx.y;
+    SO*       Hb = H + (size_t)b * mstride;
+    SF*       Fb = H32 ? H32 + (size_t)b * mstride32 : nullptr;
+    auto put = [&](int r, int c, SO v) {
+        Hb[(size_t)c * ld + r] = v;
+        if (Fb) Fb[(size_t)c * ld + r] = copy32(v);
+    };
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        const int jl = ty + 8 * q, i = ti * 32 + tx, j = tj * 32 + jl;
+        if (i < N && j < N && i >= j) {
+            const cx<double> h  = scalar_element<NL>(P, Vloc, phNL, rows, b, i, j);
+            const double*    Ri = rows + ((size_t)b * N + i) * ROW_STRIDE;
+            const double*    Rj = rows + ((size_t)b * N + j) * ROW_STRIDE;
+            const double2    ph = phSO[(size_t)j * N + i];
+            cx<double>       sv[4];
+            soc_element(P, Ri, Rj, ph.x, ph.y, sv);
+            const SO uu = stored(Hb, mk(h.x + sv[0].x, h.y + sv[0].y));
+            const SO dd = stored(Hb, mk(h.x + sv[3].x, h.y + sv[3].y));
+            const SO du = stored(Hb, sv[2]);
+            put(i, j, uu);
+            put(i + N, j + N, dd);
+            put(i + N, j, du);
+            tile[0][jl][tx] = uu;
+            tile[1][jl][tx] = dd;
+            tile[2][jl][tx] = du;
+            if (i > j) {
+                const SO ud = stored(Hb, sv[1]);
+                put(i, j + N, ud);
+                tile[3][jl][tx] = ud;
+            }
+        }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        // mirrors: threads run down the rows j (coalesced down column i, i + N)
+        const int il = ty + 8 * q, j = tj * 32 + tx, i = ti * 32 + il;
+        if (i < N && j < N && i >= j) {
+            put(j, i + N, conj_stored(tile[2][tx][il]));  // UD(j, i) = conj DU(i, j)
+            if (i > j) {
+                put(j, i, conj_stored(tile[0][tx][il]));          // UU(j, i)
+                put(j + N, i + N, conj_stored(tile[1][tx][il]));  // DD(j, i)
+                put(j + N, i, conj_stored(tile[3][tx][il]));      // DU(j, i) = conj UD(i, j)
+            }
+        }
+    }
 }
 
 // ------------------------------------------------------------------------------------------------
@@ -399,11 +427,12 @@ void launch_assemble(const DevParams& P, const cx<double>* Vloc, const double2* 
         count_launch();
         return;
     }
-    dim3 grd((P.N + 31) / 32, (P.N + 7) / 8, batch);
-#define UEPM_ASM(NL_, SO_) k_assemble<NL_, SO_, SO><<<grd, blk, 0, s>>>(P, Vloc, phNL, phSO, rows, H, ld, mstride, H32, mstride32, batch)
-    if (P.nl) UEPM_ASM(true, true);
-    else UEPM_ASM(false, true);
-#undef UEPM_ASM
+    const int    T    = (P.N + 31) / 32;
+    dim3         grd(T * (T + 1) / 2, batch);
+    const size_t smem = sizeof(SO) * 4 * 32 * 33;
+    auto         kern = P.nl ? k_assemble_soc_tiles<true, SO> : k_assemble_soc_tiles<false, SO>;
+    if (smem > 48 * 1024) cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    kern<<<grd, blk, smem, s>>>(P, Vloc, phNL, phSO, rows, H, ld, mstride, H32, mstride32, batch);
     count_launch();
 }
 
