@@ -94,9 +94,22 @@ __device__ void sph_triple(int l, double x, double* j) {
 }
 
 // Modified spherical i_2 by the reference's closed form (bessel_func.hpp:47-52).
+// bessel_2nd_order_first_kind (bessel_func.hpp:47-52): i2(x) = ((x^2 + 3) sinh x - 3 x cosh x) / x^3,
+// the reference's closed form. Above x = 2 sinh and cosh come from one exponential,
+// (e^x -+ e^-x) / 2 (relative error ~ eps there, the numerator cancels by < 10x); below, the
+// library's sinh and cosh (the closed form cancels to ~3 eps / x^2 near 0).
 __device__ __forceinline__ double bessel_i2(double x) {
     if (x == 0.0) return 0.0;
-    return ((x * x + 3) * sinh(x) - 3 * x * cosh(x)) / (x * x * x);
+    double sh, ch;
+    if (x > 2.0) {
+        const double E = exp(x), Ei = 1.0 / E;
+        sh             = 0.5 * (E - Ei);
+        ch             = 0.5 * (E + Ei);
+    } else {
+        sh = sinh(x);
+        ch = cosh(x);
+    }
+    return ((x * x + 3) * sh - 3 * x * ch) / (x * x * x);
 }
 
 __device__ __forceinline__ double soc_B(unsigned period, double nK, double bohr, double r) {
@@ -127,6 +140,7 @@ __global__ void k_rows(const DevParams P, const double* __restrict__ kpts, const
     R[RF_KZ] = K[2];
     R[RF_NK] = nK;
     if (P.nl) {  // the cation's values only where its parameters differ (nl_element reads them then)
+        R[P.square ? RF_INVK_SQUARE : RF_INVK_GAUSS] = (nK > 0.0) ? 1.0 / nK : 0.0;
         if (P.has_R0a) sph_triple(0, nK * P.R0a, R + RF_J0A);
         if (P.has_R0c && !P.same_nl) sph_triple(0, nK * P.R0c, R + RF_J0C);
         if (P.square) {
@@ -167,15 +181,20 @@ __device__ __forceinline__ double F_l(int l, double n1, double n2, bool far, dou
 // structure phase 2 pi (tau/a).(G_i - G_j). Where anion and cation carry the same parameters their
 // two terms are equal bit for bit (the same operations on the same values), so the cation's is not
 // recomputed: Vs = (Va + Va) / 2 = Va and Vas = 0 exactly.
+// The angle's cosine takes the per-row reciprocals of |K| (one product instead of an FP64 division per
+// element, within 2 ulp of dp / (n1 n2)), and the F_l reciprocal is formed only where an F_l term
+// exists (an l = 0 well, or square l = 2 wells).
 __device__ cx<double> nl_element(const DevParams& P, const double* Ri, const double* Rj, double pc, double ps) {
-    const double n1  = Ri[RF_NK], n2 = Rj[RF_NK];
-    const double dp  = Ri[RF_KX] * Rj[RF_KX] + Ri[RF_KY] * Rj[RF_KY] + Ri[RF_KZ] * Rj[RF_KZ];
-    const double np  = n1 * n2;
-    const double ca  = (np < 1.0e-13) ? 1.0 : dp / (n1 * n2);
-    const double lg2 = 0.5 * (3 * ca * ca - 1);
-    const double t   = n1 * n2 - P.kF2;
-    const bool   far = F_l_far(n1, n2);
-    const double inv = far ? 1.0 / (n1 * n1 - n2 * n2) : 0.0;
+    const double n1   = Ri[RF_NK], n2 = Rj[RF_NK];
+    const double dp   = Ri[RF_KX] * Rj[RF_KX] + Ri[RF_KY] * Rj[RF_KY] + Ri[RF_KZ] * Rj[RF_KZ];
+    const double np   = n1 * n2;
+    const int    fi   = P.square ? RF_INVK_SQUARE : RF_INVK_GAUSS;
+    const double ca   = (np < 1.0e-13) ? 1.0 : dp * (Ri[fi] * Rj[fi]);
+    const double lg2  = 0.5 * (3 * ca * ca - 1);
+    const double t    = n1 * n2 - P.kF2;
+    const bool   far  = F_l_far(n1, n2);
+    const bool   F_on = P.has_R0a || P.has_R0c || (P.square && (P.has_A2a || P.has_A2c));
+    const double inv  = (far && F_on) ? 1.0 / (n1 * n1 - n2 * n2) : 0.0;
 
     double       Va  = 0.0;
     const double A0a = P.alpha0a + P.nl_df * P.beta0a * t;

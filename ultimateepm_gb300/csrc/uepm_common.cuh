@@ -301,7 +301,11 @@ enum RowField {
     RF_GEC,                       // exp(-0.25 |K|^2 R2c^2)
     RF_BC,                        // SOC radial factor B_period(|K|), cation
     RF_BA,                        // anion
-    ROW_STRIDE = 24
+    ROW_STRIDE = 24,
+    // 1 / |K_i| (0 where K = 0), in a slot the well type leaves free: the gaussian exponentials'
+    // slot for square wells, the l = 2 Bessel slot for gaussian wells
+    RF_INVK_SQUARE = RF_GEA,
+    RF_INVK_GAUSS  = RF_J2A
 };
 
 }  // namespace uepm
