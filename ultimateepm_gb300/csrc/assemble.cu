@@ -24,6 +24,8 @@
 //   (hi, lo) pairs (the mixed path's Rayleigh-Ritz operand). When H(k) is exactly real (no SOC, no
 //   antisymmetric form factors, identical anion/cation nonlocal parameters) only real parts are
 //   stored.
+#include <type_traits>
+
 #include "uepm_common.cuh"
 #include "uepm_kernels.h"
 
@@ -121,7 +123,7 @@ __device__ __forceinline__ double soc_B(unsigned period, double nK, double bohr,
 }
 
 __global__ void k_rows(const DevParams P, const double* __restrict__ kpts, const int* __restrict__ G,
-                       double* __restrict__ rows, int batch) {
+                       double* __restrict__ rows, int batch, float2* __restrict__ rows32) {
     const int idx = blockIdx.x * blockDim.x + threadIdx.x;
     if (idx >= batch * P.N) return;
     const int     b = idx / P.N, i = idx - b * P.N;
@@ -154,6 +156,27 @@ __global__ void k_rows(const DevParams P, const double* __restrict__ kpts, const
     if (P.soc) {
         R[RF_BC] = soc_B(P.pc, nK, P.bohr, P.rc);
         R[RF_BA] = soc_B(P.pa, nK, P.bohr, P.ra);
+    }
+    if (rows32 && P.nl && P.square) {  // double-single copy for the mixed path's FP32-pipe element
+        float2* R32 = rows32 + (size_t)idx * ROW_STRIDE;
+        auto    put = [&](int f) {
+            const ds v = ds_of_double(R[f]);
+            R32[f]     = make_float2(v.h, v.l);
+        };
+        put(RF_KIN);
+        put(RF_KX);
+        put(RF_KY);
+        put(RF_KZ);
+        put(RF_NK);
+        put(RF_INVK_SQUARE);
+        const ds ns  = ds_of_double(nK / P.ff);
+        R32[RF_NKS32] = make_float2(ns.h, ns.l);
+        for (int q = 0; q < 3; ++q) {
+            if (P.has_R0a) put(RF_J0A + q);
+            if (P.has_R0c && !P.same_nl) put(RF_J0C + q);
+            if (P.has_A2a) put(RF_J2A + q);
+            if (P.has_A2c && !P.same_nl) put(RF_J2C + q);
+        }
     }
 }
 
@@ -232,6 +255,60 @@ __device__ cx<double> nl_element(const DevParams& P, const double* Ri, const dou
     const double Vs  = 1.0 * (Va + Vc) / 2.0;
     const double Vas = 1.0 * (Va - Vc) / 2.0;
     return mk(pc * Vs, ps * Vas);
+}
+
+// The square-well element of nl_element in double-single arithmetic on the FP32 pipe (the mixed
+// path's matrix for the Rayleigh-Ritz products, which it stores as FP32 pairs anyway): the same
+// formula and branches (taken on the double-single values), from the rows' double-single copies
+// (rows32) and the structure phase's (pc, ps). The F_l terms are carried times 4 pi / volume (VF_l
+// below) and the far branch in norms of units 2 pi / a, so every intermediate stays inside FP32's
+// exponent range; the regrouped products differ from the FP64 element by a few units of 2^-46.
+__device__ __forceinline__ ds rd(const float2* R, int f) { return ds{R[f].x, R[f].y}; }
+// Vpre F_l; n1s, n2s: the norms in units of 2 pi / a; inv = 1 / (n1s^2 - n2s^2).
+__device__ __forceinline__ ds VF_l_ds(int l, ds n1s, bool far, bool big, ds inv, const float2* Ri, const float2* Rj,
+                                      int f, ds n2s, ds VR2s, ds VR3h, ds VR3t) {
+    if (far) {
+        const ds F = ds_sub(ds_mul(ds_mul(n1s, rd(Ri, f + 2)), rd(Rj, f + 1)), ds_mul(ds_mul(n2s, rd(Rj, f + 2)), rd(Ri, f + 1)));
+        return ds_mul(ds_mul(VR2s, inv), F);
+    } else if (big) {
+        const ds F = ds_sub(ds_mul(rd(Ri, f + 1), rd(Ri, f + 1)), ds_mul(rd(Ri, f), rd(Ri, f + 2)));
+        return ds_mul(VR3h, F);
+    }
+    return (l == 0) ? VR3t : ds{0.f, 0.f};
+}
+// far: the reference's branch |n1 - n2| > 1e-4, decided on the FP64 norms by the caller (the
+// double-single difference is not resolved finely enough for it).
+__device__ void nl_element_ds(const DevParamsDS& Q, const float2* Ri, const float2* Rj, ds pc, ds ps, bool far, ds& re,
+                              ds& im) {
+    const ds   n1  = rd(Ri, RF_NK), n2 = rd(Rj, RF_NK);
+    const ds   dp  = ds_add(ds_add(ds_mul(rd(Ri, RF_KX), rd(Rj, RF_KX)), ds_mul(rd(Ri, RF_KY), rd(Rj, RF_KY))),
+                            ds_mul(rd(Ri, RF_KZ), rd(Rj, RF_KZ)));
+    const ds   np  = ds_mul(n1, n2);
+    const ds   ca  = (np.h < 1.0e-13f) ? ds{1.f, 0.f} : ds_mul(dp, ds_mul(rd(Ri, RF_INVK_SQUARE), rd(Rj, RF_INVK_SQUARE)));
+    const ds   lg2 = ds_mulf(ds_sub(ds_mulf(ds_mul(ca, ca), 3.f), ds{1.f, 0.f}), 0.5f);
+    const ds   t   = ds_sub(np, Q.kF2);
+    const ds   n1s = rd(Ri, RF_NKS32), n2s = rd(Rj, RF_NKS32);
+    const bool big = n1.h > 1.0e-4f;
+    const ds   inv = far ? ds_div(ds{1.f, 0.f}, ds_sub(ds_mul(n1s, n1s), ds_mul(n2s, n2s))) : ds{0.f, 0.f};
+    ds         Va  = ds{0.f, 0.f};
+    const ds   A0a = ds_add(Q.alpha0a, ds_mul(Q.nl_df_beta0a, t));
+    if (Q.has_R0a) Va = ds_mul(A0a, VF_l_ds(0, n1s, far, big, inv, Ri, Rj, RF_J0A, n2s, Q.VR0a2s, Q.VR0a3h, Q.VR0a3t));
+    if (Q.has_A2a)
+        Va = ds_add(Va, ds_mul(ds_mul(Q.A2a_5, lg2),
+                               VF_l_ds(2, n1s, far, big, inv, Ri, Rj, RF_J2A, n2s, Q.VR2a2s, Q.VR2a3h, ds{0.f, 0.f})));
+    if (Q.same_nl) {
+        re = ds_mul(pc, Va);
+        im = ds{0.f, 0.f};
+        return;
+    }
+    ds       Vc  = ds{0.f, 0.f};
+    const ds A0c = ds_add(Q.alpha0c, ds_mul(Q.beta0c_nl_df, t));
+    if (Q.has_R0c) Vc = ds_mul(A0c, VF_l_ds(0, n1s, far, big, inv, Ri, Rj, RF_J0C, n2s, Q.VR0c2s, Q.VR0c3h, Q.VR0c3t));
+    if (Q.has_A2c)
+        Vc = ds_add(Vc, ds_mul(ds_mul(Q.A2c_5, lg2),
+                               VF_l_ds(2, n1s, far, big, inv, Ri, Rj, RF_J2C, n2s, Q.VR2c2s, Q.VR2c3h, ds{0.f, 0.f})));
+    re = ds_mul(pc, ds_mulf(ds_add(Va, Vc), 0.5f));
+    im = ds_mul(ps, ds_mulf(ds_sub(Va, Vc), 0.5f));
 }
 
 // compute_soc_contribution (SpinOrbitFunctional.cpp:111-138). s[0..3] = s00, s01, s10, s11.
@@ -352,6 +429,96 @@ __global__ void __launch_bounds__(256) k_assemble_tiles(const DevParams P, const
     }
 }
 
+// The mixed path without spin-orbit coupling and with square nonlocal wells: the same tiles, each
+// element formed in double-single arithmetic (nl_element_ds) from the k-independent V and structure
+// phase in FP32 pairs (Vloc32, phNL32: re hi, re lo, im hi, im lo) and the rows' double-single copy,
+// stored directly as its FP32 pair, with the pair's hi part as the FP32 copy. No FP64 instruction.
+// An element whose two norms are far apart by the reference's test but within 1e-5 of each other
+// (high-symmetry k, where |k + G_i| = |k + G_j| in exact arithmetic and the rounding of the FP64
+// norms takes the reference's far branch, dividing one rounding-level difference by another) is
+// formed by the FP64 element instead: double-single cannot follow that cancellation.
+template <typename SO>
+__global__ void __launch_bounds__(256) k_assemble_tiles_ds(const DevParams P, const DevParamsDS Q, const float4* __restrict__ Vloc32,
+                                                           const float4* __restrict__ phNL32, const float2* __restrict__ rows32,
+                                                           const cx<double>* __restrict__ Vloc, const double2* __restrict__ phNL,
+                                                           const double* __restrict__ rows,
+                                                           SO* __restrict__ H, int ld, size_t mstride,
+                                                           typename Lower<SO>::type* __restrict__ H32, size_t mstride32,
+                                                           int batch) {
+    using SF = typename Lower<SO>::type;
+    __shared__ SO tile[32][33];
+    const int b = blockIdx.y;
+    if (b >= batch) return;
+    int t = blockIdx.x, ti = 0;
+    while (t > ti) {
+        t -= ti + 1;
+        ++ti;
+    }
+    const int tj = t;
+    const int N  = P.N;
+    const int tx = threadIdx.x, ty = threadIdx.y;
+    SO*       Hb = H + (size_t)b * mstride;
+    SF*       Fb = H32 ? H32 + (size_t)b * mstride32 : nullptr;
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        const int jl = ty + 8 * q, i = ti * 32 + tx, j = tj * 32 + jl;
+        if (i < N && j < N && i >= j) {
+            const double  n1 = rows[((size_t)b * N + i) * ROW_STRIDE + RF_NK];
+            const double  n2 = rows[((size_t)b * N + j) * ROW_STRIDE + RF_NK];
+            const double  dn = fabs(n1 - n2);
+            const bool    far = F_l_far(n1, n2);
+            SO            v;
+            if (far && dn < 1.0e-5 * fmax(n1, n2)) {
+                v = stored(Hb, scalar_element<true>(P, Vloc, phNL, rows, b, i, j));
+            } else {
+                const float2* Ri = rows32 + ((size_t)b * N + i) * ROW_STRIDE;
+                const float2* Rj = rows32 + ((size_t)b * N + j) * ROW_STRIDE;
+                const float4  vl = Vloc32[(size_t)j * N + i];
+                const float4  ph = phNL32[(size_t)j * N + i];
+                ds            vr, vi;
+                nl_element_ds(Q, Ri, Rj, ds{ph.x, ph.y}, ds{ph.z, ph.w}, far, vr, vi);
+                ds hr = ds{vl.x, vl.y}, hi = ds{vl.z, vl.w};
+                if (i == j) hr = ds_add(hr, rd(Ri, RF_KIN));
+                hr = ds_add(hr, vr);
+                hi = ds_add(hi, vi);
+                if constexpr (std::is_same<SO, ds2>::value) v = ds2{hr.h, hr.l};
+                else v = ds4{hr.h, hr.l, hi.h, hi.l};
+            }
+            tile[jl][tx]           = v;
+            Hb[(size_t)j * ld + i] = v;
+            if (Fb) Fb[(size_t)j * ld + i] = copy32(v);
+        }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        const int il = ty + 8 * q, j = tj * 32 + tx, i = ti * 32 + il;
+        if (i < N && j < N && i > j) {
+            const SO v             = conj_stored(tile[tx][il]);
+            Hb[(size_t)i * ld + j] = v;
+            if (Fb) Fb[(size_t)i * ld + j] = copy32(v);
+        }
+    }
+}
+
+template <typename SO>
+void launch_assemble_ds(const DevParams& P, const DevParamsDS& Q, const float4* Vloc32, const float4* phNL32,
+                        const float2* rows32, const cx<double>* Vloc, const double2* phNL, const double* rows, SO* H,
+                        int ld, size_t mstride, typename Lower<SO>::type* H32, size_t mstride32, int batch,
+                        cudaStream_t s) {
+    const int T = (P.N + 31) / 32;
+    dim3      grd(T * (T + 1) / 2, batch), blk(32, 8);
+    k_assemble_tiles_ds<SO><<<grd, blk, 0, s>>>(P, Q, Vloc32, phNL32, rows32, Vloc, phNL, rows, H, ld, mstride, H32,
+                                                mstride32, batch);
+    count_launch();
+}
+template void launch_assemble_ds<ds2>(const DevParams&, const DevParamsDS&, const float4*, const float4*, const float2*,
+                                      const cx<double>*, const double2*, const double*, ds2*, int, size_t, float*, size_t,
+                                      int, cudaStream_t);
+template void launch_assemble_ds<ds4>(const DevParams&, const DevParamsDS&, const float4*, const float4*, const float2*,
+                                      const cx<double>*, const double2*, const double*, ds4*, int, size_t, cx<float>*,
+                                      size_t, int, cudaStream_t);
+
 // With spin-orbit coupling: the same tiling over the scalar problem's lower triangle. Each scalar
 // element (i, j), i >= j, yields four blocks' elements, UU(i, j) = h + s00, DD(i, j) = h + s11,
 // DU(i, j) = s10 and UD(i, j) = s01 (i > j), written directly at (i, j), (i + N, j + N), (i + N, j)
@@ -427,9 +594,10 @@ __global__ void __launch_bounds__(256) k_assemble_soc_tiles(const DevParams P, c
 }
 
 // ------------------------------------------------------------------------------------------------
-void launch_rows(const DevParams& P, const double* d_k, const int* d_G, double* d_rows, int batch, cudaStream_t s) {
+void launch_rows(const DevParams& P, const double* d_k, const int* d_G, double* d_rows, int batch, cudaStream_t s,
+                 float2* d_rows32) {
     const int total = batch * P.N;
-    k_rows<<<(total + 127) / 128, 128, 0, s>>>(P, d_k, d_G, d_rows, batch);
+    k_rows<<<(total + 127) / 128, 128, 0, s>>>(P, d_k, d_G, d_rows, batch, d_rows32);
     count_launch();
 }
 

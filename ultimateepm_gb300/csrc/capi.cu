@@ -148,7 +148,7 @@ void pp_value(const uepm_material& m, int gx, int gy, int gz, double tau, double
 size_t align_up(size_t x) { return (x + 255) & ~(size_t)255; }
 
 struct Layout {
-    size_t rows, H, H32, d, e, tq, ev, work, z, X32, refine, small, total;
+    size_t rows, rows32, H, H32, d, e, tq, ev, work, z, X32, refine, small, total;
 };
 
 // Bytes of workspace one chunk of `c` matrices needs, with the offset of every region.
@@ -167,7 +167,8 @@ Layout plan(const uepm_ctx* ctx, int nb, uint32_t want, size_t c) {
         off            = align_up(off + bytes);
         return o;
     };
-    L.rows = take(c * N * ROW_STRIDE * sizeof(double));
+    L.rows   = take(c * N * ROW_STRIDE * sizeof(double));
+    L.rows32 = (mixed && ctx->ds_nl) ? take(c * N * ROW_STRIDE * sizeof(float2)) : 0;
     L.H    = take(mixed && ctx->sparse_local ? 0 : c * n * n * es);  // the sparse path never forms it
     L.H32  = mixed ? take(c * n * n * es32) : 0;
     L.d    = take(c * n * rs);
@@ -221,9 +222,11 @@ void run_chunk(uepm_ctx* ctx, const Layout& L, char* ws, const double* kk, int c
     const size_t mstride = (size_t)n * n;
     auto*        rows    = reinterpret_cast<double*>(ws + L.rows);
     auto*        H       = reinterpret_cast<S*>(ws + L.H);
+    const bool   ds_asm  = ctx->precision == UEPM_PREC_MIXED && ctx->ds_nl;
+    auto*        rows32  = ds_asm ? reinterpret_cast<float2*>(ws + L.rows32) : nullptr;
     {
         ProfScope p(ctx, s, KK_ROWS);
-        launch_rows(ctx->P, kk, ctx->d_G, rows, c, s);
+        launch_rows(ctx->P, kk, ctx->d_G, rows, c, s, rows32);
     }
     if (ctx->precision != UEPM_PREC_MIXED) {
         {
@@ -268,6 +271,9 @@ void run_chunk(uepm_ctx* ctx, const Layout& L, char* ws, const double* kk, int c
         // with a local potential only, those products use the resident sparse V instead
         if (ctx->sparse_local)
             launch_assemble<S32>(ctx->P, ctx->d_Vloc, ctx->d_phNL, ctx->d_phSO, rows, H32, n, mstride, nullptr, 0, c, s);
+        else if (ds_asm)
+            launch_assemble_ds<SP>(ctx->P, ctx->Q, ctx->d_Vloc32, ctx->d_phNL32, rows32, ctx->d_Vloc, ctx->d_phNL, rows, Hs, n,
+                                   mstride, H32, mstride, c, s);
         else
             launch_assemble<SP>(ctx->P, ctx->d_Vloc, ctx->d_phNL, ctx->d_phSO, rows, Hs, n, mstride, H32, mstride, c, s);
     }
@@ -519,6 +525,47 @@ int uepm_ctx_create(const uepm_material* mat, const int32_t* G, int N, uint32_t 
         if ((e = cudaMemcpy(ctx->d_phNL, phNL.data(), sizeof(double2) * phNL.size(), cudaMemcpyHostToDevice)) != cudaSuccess)
             return fail(e, "copy phNL");
     }
+    ctx->ds_nl = nl && !soc && P.square && (P.has_R0a || P.has_R0c || P.has_A2a || P.has_A2c);
+    if (ctx->ds_nl) {
+        // the nonlocal constants and the k-independent tables as FP32 pairs; products the FP64
+        // element forms first are formed here in FP64, in the same order
+        DevParamsDS& Q = ctx->Q;
+        Q.has_R0a      = P.has_R0a;
+        Q.has_R0c      = P.has_R0c;
+        Q.has_A2a      = P.has_A2a;
+        Q.has_A2c      = P.has_A2c;
+        Q.same_nl      = P.same_nl;
+        Q.kF2          = ds_of_double(P.kF2);
+        Q.alpha0a      = ds_of_double(P.alpha0a);
+        Q.nl_df_beta0a = ds_of_double(P.nl_df * P.beta0a);
+        Q.alpha0c      = ds_of_double(P.alpha0c);
+        Q.beta0c_nl_df = ds_of_double(P.beta0c * P.nl_df);
+        Q.A2a_5        = ds_of_double(P.A2a * 5);
+        Q.A2c_5        = ds_of_double(P.A2c * 5);
+        Q.VR0a2s       = ds_of_double(P.Vpre * P.R0a2 / P.ff);
+        Q.VR0c2s       = ds_of_double(P.Vpre * P.R0c2 / P.ff);
+        Q.VR2a2s       = ds_of_double(P.Vpre * P.R2a2 / P.ff);
+        Q.VR2c2s       = ds_of_double(P.Vpre * P.R2c2 / P.ff);
+        Q.VR0a3h       = ds_of_double(P.Vpre * P.R0a3h);
+        Q.VR0c3h       = ds_of_double(P.Vpre * P.R0c3h);
+        Q.VR2a3h       = ds_of_double(P.Vpre * P.R2a3h);
+        Q.VR2c3h       = ds_of_double(P.Vpre * P.R2c3h);
+        Q.VR0a3t       = ds_of_double(P.Vpre * P.R0a3t);
+        Q.VR0c3t       = ds_of_double(P.Vpre * P.R0c3t);
+        std::vector<float4> v32(V.size()), p32(V.size());
+        for (size_t q = 0; q < V.size(); ++q) {
+            const ds a = ds_of_double(V[q].x), b = ds_of_double(V[q].y);
+            const ds c = ds_of_double(phNL[q].x), d = ds_of_double(phNL[q].y);
+            v32[q]     = make_float4(a.h, a.l, b.h, b.l);
+            p32[q]     = make_float4(c.h, c.l, d.h, d.l);
+        }
+        if ((e = cudaMalloc(&ctx->d_Vloc32, sizeof(float4) * v32.size())) != cudaSuccess) return fail(e, "cudaMalloc(V32)");
+        if ((e = cudaMemcpy(ctx->d_Vloc32, v32.data(), sizeof(float4) * v32.size(), cudaMemcpyHostToDevice)) != cudaSuccess)
+            return fail(e, "copy V32");
+        if ((e = cudaMalloc(&ctx->d_phNL32, sizeof(float4) * p32.size())) != cudaSuccess) return fail(e, "cudaMalloc(phNL32)");
+        if ((e = cudaMemcpy(ctx->d_phNL32, p32.data(), sizeof(float4) * p32.size(), cudaMemcpyHostToDevice)) != cudaSuccess)
+            return fail(e, "copy phNL32");
+    }
     if (soc) {
         if ((e = cudaMalloc(&ctx->d_phSO, sizeof(double2) * phSO.size())) != cudaSuccess) return fail(e, "cudaMalloc(phSO)");
         if ((e = cudaMemcpy(ctx->d_phSO, phSO.data(), sizeof(double2) * phSO.size(), cudaMemcpyHostToDevice)) != cudaSuccess)
@@ -586,6 +633,8 @@ int uepm_ctx_destroy(uepm_ctx* ctx) {
     if (ctx->d_Vloc) cudaFree(ctx->d_Vloc);
     if (ctx->d_phNL) cudaFree(ctx->d_phNL);
     if (ctx->d_phSO) cudaFree(ctx->d_phSO);
+    if (ctx->d_Vloc32) cudaFree(ctx->d_Vloc32);
+    if (ctx->d_phNL32) cudaFree(ctx->d_phNL32);
     if (ctx->d_ell_col) cudaFree(ctx->d_ell_col);
     if (ctx->d_ell_re) cudaFree(ctx->d_ell_re);
     if (ctx->d_ell_im) cudaFree(ctx->d_ell_im);

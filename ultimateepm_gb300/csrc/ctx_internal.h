@@ -26,6 +26,12 @@ struct uepm_ctx {
     uepm::cx<double>* d_Vloc    = nullptr;
     double2*      d_phNL    = nullptr;
     double2*      d_phSO    = nullptr;
+    // square nonlocal wells without spin-orbit: the mixed path forms H(k) in double-single
+    // arithmetic from V and the nonlocal phase in FP32 pairs (re hi, re lo, im hi, im lo)
+    bool              ds_nl     = false;
+    uepm::DevParamsDS Q{};
+    float4*           d_Vloc32  = nullptr;
+    float4*           d_phNL32  = nullptr;
     // local potential only (no nonlocal, no spin-orbit): H(k) = V + diag(kinetic(k)) with V the
     // k-independent local form-factor matrix, sparse (|G_i - G_j|^2 in {3, 4, 8, 11}); its rows as
     // CSR (every row also lists its diagonal) with values as FP32 pairs, for the mixed path's H X

@@ -206,6 +206,46 @@ __device__ __forceinline__ void ds_add_prod(dsacc& a, float x, float y) {
 }
 __device__ __forceinline__ double ds_value(dsacc a) { return (double)a.h + (double)a.l; }
 
+// Double-single numbers (an FP32 pair h + l, |l| <= ulp(h) / 2, about 48 significant bits) with the
+// classical error-free transformations (Dekker, Knuth) on non-contracted FP32 operations: the mixed
+// path evaluates the nonlocal matrix elements on the FP32 pipe with them instead of the FP64 pipe.
+struct ds {
+    float h, l;
+};
+__host__ __device__ inline ds ds_of_double(double v) {
+    const float h = (float)v;
+    return ds{h, (float)(v - (double)h)};
+}
+__device__ __forceinline__ ds ds_quick(float s, float e) {  // |s| >= |e|
+    const float t = __fadd_rn(s, e);
+    return ds{t, __fsub_rn(e, __fsub_rn(t, s))};
+}
+__device__ __forceinline__ ds ds_add(ds a, ds b) {
+    const float s  = __fadd_rn(a.h, b.h);
+    const float bb = __fsub_rn(s, a.h);
+    const float e  = __fadd_rn(__fsub_rn(a.h, __fsub_rn(s, bb)), __fsub_rn(b.h, bb));
+    return ds_quick(s, __fadd_rn(e, __fadd_rn(a.l, b.l)));
+}
+__device__ __forceinline__ ds ds_neg(ds a) { return ds{-a.h, -a.l}; }
+__device__ __forceinline__ ds ds_sub(ds a, ds b) { return ds_add(a, ds_neg(b)); }
+__device__ __forceinline__ ds ds_mul(ds a, ds b) {
+    const float p = __fmul_rn(a.h, b.h);
+    const float e = fmaf(a.h, b.h, -p);
+    return ds_quick(p, fmaf(a.h, b.l, fmaf(a.l, b.h, e)));
+}
+__device__ __forceinline__ ds ds_mulf(ds a, float b) {  // times an exact FP32 value
+    const float p = __fmul_rn(a.h, b);
+    const float e = fmaf(a.h, b, -p);
+    return ds_quick(p, fmaf(a.l, b, e));
+}
+__device__ __forceinline__ ds ds_div(ds a, ds b) {  // long division, two quotient digits
+    const float q1 = __fdiv_rn(a.h, b.h);
+    const ds    r  = ds_sub(a, ds_mulf(b, q1));
+    const float q2 = __fdiv_rn(r.h, b.h);
+    return ds_quick(q1, q2);
+}
+__device__ __forceinline__ float ds_abs_hi(ds a) { return fabsf(a.h); }
+
 // cp.async of one naturally aligned element of B = 4 or 8 bytes, global -> shared
 template <int B>
 __device__ __forceinline__ void cp_async_elem(void* dst, const void* src) {
@@ -286,6 +326,22 @@ struct DevParams {
     double ra, rc, alpha_soc, mu_soc, kfac, bohr;
 };
 
+// The nonlocal constants of DevParams as double-single numbers, for the mixed path's square-well
+// element on the FP32 pipe; products the FP64 element forms first are formed on the host in FP64
+// (the same order of operations) and then split.
+struct DevParamsDS {
+    int  has_R0a, has_R0c, has_A2a, has_A2c, same_nl;
+    ds   kF2;
+    ds   alpha0a, nl_df_beta0a, alpha0c, beta0c_nl_df;  // A0 = alpha0 + (nl_df beta0) t
+    ds   A2a_5, A2c_5;                                  // A2 5 (eV)
+    // The F_l terms times Vpre = 4 pi / volume, so that every intermediate stays well inside FP32's
+    // exponent range (R^2 / (n1^2 - n2^2) ~ 1e-41 in SI units is not): VR2s = Vpre R^2 / (2 pi / a)
+    // for the far branch, whose norms are taken in units of 2 pi / a, VR3h = Vpre R^3 / 2 and
+    // VR3t = Vpre R^3 / 3 for the near branch and its K = 0 limit.
+    ds   VR0a2s, VR0c2s, VR2a2s, VR2c2s;
+    ds   VR0a3h, VR0c3h, VR2a3h, VR2c3h, VR0a3t, VR0c3t;
+};
+
 // Per-(k, basis vector) quantities computed once per k in the row kernel and read by the
 // element kernel. Layout: rows[(b * N + i) * ROW_STRIDE + field].
 enum RowField {
@@ -305,7 +361,9 @@ enum RowField {
     // 1 / |K_i| (0 where K = 0), in a slot the well type leaves free: the gaussian exponentials'
     // slot for square wells, the l = 2 Bessel slot for gaussian wells
     RF_INVK_SQUARE = RF_GEA,
-    RF_INVK_GAUSS  = RF_J2A
+    RF_INVK_GAUSS  = RF_J2A,
+    // in the mixed path's double-single copy of the rows only: |K_i| in units of 2 pi / a
+    RF_NKS32 = RF_GEC
 };
 
 }  // namespace uepm

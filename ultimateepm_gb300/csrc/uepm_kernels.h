@@ -13,7 +13,16 @@ void count_launch(int n = 1);
 
 // assemble.cu: H(k) in FULL column-major storage (both triangles). SO = double (real H) or
 // cx<double>; H32 (optional) receives the FP32 copy for the mixed path (float or cx<float>).
-void launch_rows(const DevParams& P, const double* d_k, const int* d_G, double* d_rows, int batch, cudaStream_t s);
+void launch_rows(const DevParams& P, const double* d_k, const int* d_G, double* d_rows, int batch, cudaStream_t s,
+                 float2* d_rows32 = nullptr);
+// Mixed path, no spin-orbit, square nonlocal wells: the assembly in double-single arithmetic on the
+// FP32 pipe (SO = ds2 or ds4), from the k-independent tables in FP32 pairs and d_rows32 (written by
+// launch_rows when given).
+template <typename SO>
+void launch_assemble_ds(const DevParams& P, const DevParamsDS& Q, const float4* Vloc32, const float4* phNL32,
+                        const float2* rows32, const cx<double>* Vloc, const double2* phNL, const double* rows, SO* H,
+                        int ld, size_t mstride, typename Lower<SO>::type* H32, size_t mstride32, int batch,
+                        cudaStream_t s);
 template <typename SO>
 void launch_assemble(const DevParams& P, const cx<double>* Vloc, const double2* phNL, const double2* phSO, const double* rows,
                      SO* H, int ld, size_t mstride, typename Lower<SO>::type* H32, size_t mstride32, int batch,

@@ -4,8 +4,8 @@ to time (or profile) the path on a given case.
     python -m ultimateepm_gb300.solve_sample materials.yaml Ge --shells 12 --nl --soc --bands 16 \\
         --k 2000 [--precision fp64|mixed] [--reduction R] [--repeat N]
 
-Prints the first k-point's lowest energies and the mean wall time per solve (the solve runs through
-uepm_solve with host buffers, so the time includes the copies). Parameter files are looked up in
+Prints the first k-point's lowest energies and the mean wall time per solve after a small warm-up
+solve (the solve runs through uepm_solve with host buffers, so the time includes the copies). Parameter files are looked up in
 the package's params/ folder unless a path is given.
 """
 from __future__ import annotations
@@ -43,6 +43,7 @@ def main(argv=None) -> int:
     ctx = _Context(mats.materials[a.material], generate_basis_vectors(a.shells), a.nl, a.soc, prec)
     N.check(N.load().uepm_ctx_set_tuning(ctx.h, C.byref(N.UepmTuning(reduction=a.reduction))))
     k = sample_bz(a.k, np.random.default_rng(a.seed))
+    ctx.solve(k[: min(len(k), 64)], a.bands)  # warm-up: workspace and module loading
     t0 = time.perf_counter()
     for _ in range(a.repeat):
         E, _, _, st = ctx.solve(k, a.bands)
