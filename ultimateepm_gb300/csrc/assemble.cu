@@ -157,7 +157,7 @@ __global__ void k_rows(const DevParams P, const double* __restrict__ kpts, const
         R[RF_BC] = soc_B(P.pc, nK, P.bohr, P.rc);
         R[RF_BA] = soc_B(P.pa, nK, P.bohr, P.ra);
     }
-    if (rows32 && P.nl && P.square) {  // double-single copy for the mixed path's FP32-pipe element
+    if (rows32 && P.nl) {  // double-single copy for the mixed path's FP32-pipe element
         float2* R32 = rows32 + (size_t)idx * ROW_STRIDE;
         auto    put = [&](int f) {
             const ds v = ds_of_double(R[f]);
@@ -168,14 +168,18 @@ __global__ void k_rows(const DevParams P, const double* __restrict__ kpts, const
         put(RF_KY);
         put(RF_KZ);
         put(RF_NK);
-        put(RF_INVK_SQUARE);
-        const ds ns  = ds_of_double(nK / P.ff);
-        R32[RF_NKS32] = make_float2(ns.h, ns.l);
+        put(P.square ? RF_INVK_SQUARE : RF_INVK_GAUSS);
+        const ds ns = ds_of_double(nK / P.ff);
+        R32[P.square ? RF_NKS32_SQUARE : RF_NKS32_GAUSS] = make_float2(ns.h, ns.l);
         for (int q = 0; q < 3; ++q) {
             if (P.has_R0a) put(RF_J0A + q);
             if (P.has_R0c && !P.same_nl) put(RF_J0C + q);
-            if (P.has_A2a) put(RF_J2A + q);
-            if (P.has_A2c && !P.same_nl) put(RF_J2C + q);
+            if (P.square && P.has_A2a) put(RF_J2A + q);
+            if (P.square && P.has_A2c && !P.same_nl) put(RF_J2C + q);
+        }
+        if (!P.square) {
+            put(RF_GEA);
+            if (!P.same_nl) put(RF_GEC);
         }
     }
 }
@@ -276,6 +280,17 @@ __device__ __forceinline__ ds VF_l_ds(int l, ds n1s, bool far, bool big, ds inv,
     }
     return (l == 0) ? VR3t : ds{0.f, 0.f};
 }
+// The gaussian well's i2(x) = ((x^2 + 3) sinh x - 3 x cosh x) / x^3 for x > 2 (callers route smaller x
+// to the FP64 element): e^x from the FP64 exponential (one FP64 call), the rest in double-single.
+__device__ __forceinline__ ds i2_ds(ds x) {
+    const ds E  = ds_of_double(exp((double)x.h + (double)x.l));
+    const ds Ei = ds_div(ds{1.f, 0.f}, E);
+    const ds sh = ds_mulf(ds_sub(E, Ei), 0.5f), ch = ds_mulf(ds_add(E, Ei), 0.5f);
+    const ds x2 = ds_mul(x, x);
+    const ds num = ds_sub(ds_mul(ds_add(x2, ds{3.f, 0.f}), sh), ds_mulf(ds_mul(x, ch), 3.f));
+    return ds_div(num, ds_mul(x2, x));
+}
+
 // far: the reference's branch |n1 - n2| > 1e-4, decided on the FP64 norms by the caller (the
 // double-single difference is not resolved finely enough for it).
 __device__ void nl_element_ds(const DevParamsDS& Q, const float2* Ri, const float2* Rj, ds pc, ds ps, bool far, ds& re,
@@ -284,18 +299,24 @@ __device__ void nl_element_ds(const DevParamsDS& Q, const float2* Ri, const floa
     const ds   dp  = ds_add(ds_add(ds_mul(rd(Ri, RF_KX), rd(Rj, RF_KX)), ds_mul(rd(Ri, RF_KY), rd(Rj, RF_KY))),
                             ds_mul(rd(Ri, RF_KZ), rd(Rj, RF_KZ)));
     const ds   np  = ds_mul(n1, n2);
-    const ds   ca  = (np.h < 1.0e-13f) ? ds{1.f, 0.f} : ds_mul(dp, ds_mul(rd(Ri, RF_INVK_SQUARE), rd(Rj, RF_INVK_SQUARE)));
+    const int  fi  = Q.square ? RF_INVK_SQUARE : RF_INVK_GAUSS;
+    const int  fs  = Q.square ? RF_NKS32_SQUARE : RF_NKS32_GAUSS;
+    const ds   ca  = (np.h < 1.0e-13f) ? ds{1.f, 0.f} : ds_mul(dp, ds_mul(rd(Ri, fi), rd(Rj, fi)));
     const ds   lg2 = ds_mulf(ds_sub(ds_mulf(ds_mul(ca, ca), 3.f), ds{1.f, 0.f}), 0.5f);
     const ds   t   = ds_sub(np, Q.kF2);
-    const ds   n1s = rd(Ri, RF_NKS32), n2s = rd(Rj, RF_NKS32);
+    const ds   n1s = rd(Ri, fs), n2s = rd(Rj, fs);
     const bool big = n1.h > 1.0e-4f;
     const ds   inv = far ? ds_div(ds{1.f, 0.f}, ds_sub(ds_mul(n1s, n1s), ds_mul(n2s, n2s))) : ds{0.f, 0.f};
     ds         Va  = ds{0.f, 0.f};
     const ds   A0a = ds_add(Q.alpha0a, ds_mul(Q.nl_df_beta0a, t));
     if (Q.has_R0a) Va = ds_mul(A0a, VF_l_ds(0, n1s, far, big, inv, Ri, Rj, RF_J0A, n2s, Q.VR0a2s, Q.VR0a3h, Q.VR0a3t));
-    if (Q.has_A2a)
-        Va = ds_add(Va, ds_mul(ds_mul(Q.A2a_5, lg2),
-                               VF_l_ds(2, n1s, far, big, inv, Ri, Rj, RF_J2A, n2s, Q.VR2a2s, Q.VR2a3h, ds{0.f, 0.f})));
+    if (Q.has_A2a) {
+        if (Q.square)
+            Va = ds_add(Va, ds_mul(ds_mul(Q.A2a_5, lg2),
+                                   VF_l_ds(2, n1s, far, big, inv, Ri, Rj, RF_J2A, n2s, Q.VR2a2s, Q.VR2a3h, ds{0.f, 0.f})));
+        else
+            Va = ds_add(Va, ds_mul(ds_mul(Q.gA2a, lg2), ds_mul(i2_ds(ds_mul(Q.R2a2h, np)), ds_mul(rd(Ri, RF_GEA), rd(Rj, RF_GEA)))));
+    }
     if (Q.same_nl) {
         re = ds_mul(pc, Va);
         im = ds{0.f, 0.f};
@@ -304,9 +325,13 @@ __device__ void nl_element_ds(const DevParamsDS& Q, const float2* Ri, const floa
     ds       Vc  = ds{0.f, 0.f};
     const ds A0c = ds_add(Q.alpha0c, ds_mul(Q.beta0c_nl_df, t));
     if (Q.has_R0c) Vc = ds_mul(A0c, VF_l_ds(0, n1s, far, big, inv, Ri, Rj, RF_J0C, n2s, Q.VR0c2s, Q.VR0c3h, Q.VR0c3t));
-    if (Q.has_A2c)
-        Vc = ds_add(Vc, ds_mul(ds_mul(Q.A2c_5, lg2),
-                               VF_l_ds(2, n1s, far, big, inv, Ri, Rj, RF_J2C, n2s, Q.VR2c2s, Q.VR2c3h, ds{0.f, 0.f})));
+    if (Q.has_A2c) {
+        if (Q.square)
+            Vc = ds_add(Vc, ds_mul(ds_mul(Q.A2c_5, lg2),
+                                   VF_l_ds(2, n1s, far, big, inv, Ri, Rj, RF_J2C, n2s, Q.VR2c2s, Q.VR2c3h, ds{0.f, 0.f})));
+        else
+            Vc = ds_add(Vc, ds_mul(ds_mul(Q.gA2c, lg2), ds_mul(i2_ds(ds_mul(Q.R2c2h, np)), ds_mul(rd(Ri, RF_GEC), rd(Rj, RF_GEC)))));
+    }
     re = ds_mul(pc, ds_mulf(ds_add(Va, Vc), 0.5f));
     im = ds_mul(ps, ds_mulf(ds_sub(Va, Vc), 0.5f));
 }
@@ -467,8 +492,12 @@ __global__ void __launch_bounds__(256) k_assemble_tiles_ds(const DevParams P, co
             const double  n2 = rows[((size_t)b * N + j) * ROW_STRIDE + RF_NK];
             const double  dn = fabs(n1 - n2);
             const bool    far = F_l_far(n1, n2);
+            // gaussian wells: i2's closed form cancels below x = 2 (the FP64 element handles it)
+            const bool    small_x = !P.square && 0.5 * (P.R2a * P.R2a) * (n1 * n2) <= 2.0 &&
+                                 (P.has_A2a || (P.has_A2c && !P.same_nl));
             SO            v;
-            if (far && dn < 1.0e-5 * fmax(n1, n2)) {
+            if ((far && dn < 1.0e-5 * fmax(n1, n2)) || small_x ||
+                (!P.square && !P.same_nl && P.has_A2c && 0.5 * (P.R2c * P.R2c) * (n1 * n2) <= 2.0)) {
                 v = stored(Hb, scalar_element<true>(P, Vloc, phNL, rows, b, i, j));
             } else {
                 const float2* Ri = rows32 + ((size_t)b * N + i) * ROW_STRIDE;

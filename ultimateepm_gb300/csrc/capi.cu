@@ -525,7 +525,7 @@ int uepm_ctx_create(const uepm_material* mat, const int32_t* G, int N, uint32_t 
         if ((e = cudaMemcpy(ctx->d_phNL, phNL.data(), sizeof(double2) * phNL.size(), cudaMemcpyHostToDevice)) != cudaSuccess)
             return fail(e, "copy phNL");
     }
-    ctx->ds_nl = nl && !soc && P.square && (P.has_R0a || P.has_R0c || P.has_A2a || P.has_A2c);
+    ctx->ds_nl = nl && !soc && (P.has_R0a || P.has_R0c || P.has_A2a || P.has_A2c);
     if (ctx->ds_nl) {
         // the nonlocal constants and the k-independent tables as FP32 pairs; products the FP64
         // element forms first are formed here in FP64, in the same order
@@ -552,6 +552,11 @@ int uepm_ctx_create(const uepm_material* mat, const int32_t* G, int N, uint32_t 
         Q.VR2c3h       = ds_of_double(P.Vpre * P.R2c3h);
         Q.VR0a3t       = ds_of_double(P.Vpre * P.R0a3t);
         Q.VR0c3t       = ds_of_double(P.Vpre * P.R0c3t);
+        Q.square       = P.square;
+        Q.gA2a         = ds_of_double(P.gpre_a * P.A2a);
+        Q.gA2c         = ds_of_double(P.gpre_c * P.A2c);
+        Q.R2a2h        = ds_of_double(0.5 * (P.R2a * P.R2a));
+        Q.R2c2h        = ds_of_double(0.5 * (P.R2c * P.R2c));
         std::vector<float4> v32(V.size()), p32(V.size());
         for (size_t q = 0; q < V.size(); ++q) {
             const ds a = ds_of_double(V[q].x), b = ds_of_double(V[q].y);

@@ -340,6 +340,9 @@ struct DevParamsDS {
     // VR3t = Vpre R^3 / 3 for the near branch and its K = 0 limit.
     ds   VR0a2s, VR0c2s, VR2a2s, VR2c2s;
     ds   VR0a3h, VR0c3h, VR2a3h, VR2c3h, VR0a3t, VR0c3t;
+    // gaussian d-wells: V2 = (gpre A2) P2 i2(x) e_i e_j with x = (R2^2 / 2) n1 n2
+    int  square;
+    ds   gA2a, gA2c, R2a2h, R2c2h;  // gpre A2, R2^2 / 2
 };
 
 // Per-(k, basis vector) quantities computed once per k in the row kernel and read by the
@@ -362,8 +365,10 @@ enum RowField {
     // slot for square wells, the l = 2 Bessel slot for gaussian wells
     RF_INVK_SQUARE = RF_GEA,
     RF_INVK_GAUSS  = RF_J2A,
-    // in the mixed path's double-single copy of the rows only: |K_i| in units of 2 pi / a
-    RF_NKS32 = RF_GEC
+    // in the mixed path's double-single copy of the rows only: |K_i| in units of 2 pi / a, in the
+    // slot the well type leaves free
+    RF_NKS32_SQUARE = RF_GEC,
+    RF_NKS32_GAUSS  = RF_J2C
 };
 
 }  // namespace uepm
