@@ -157,13 +157,27 @@ __global__ void k_rows(const DevParams P, const double* __restrict__ kpts, const
         R[RF_BC] = soc_B(P.pc, nK, P.bohr, P.rc);
         R[RF_BA] = soc_B(P.pa, nK, P.bohr, P.ra);
     }
-    if (rows32 && P.nl) {  // double-single copy for the mixed path's FP32-pipe element
+    if (rows32 && (P.nl || P.soc)) {  // double-single copy for the mixed path's FP32-pipe element
         float2* R32 = rows32 + (size_t)idx * ROW_STRIDE;
         auto    put = [&](int f) {
             const ds v = ds_of_double(R[f]);
             R32[f]     = make_float2(v.h, v.l);
         };
         put(RF_KIN);
+        if (P.soc) {
+            put(RF_KGX);
+            put(RF_KGY);
+            put(RF_KGZ);
+            put(RF_BC);
+            put(RF_BA);
+        }
+    }
+    if (rows32 && P.nl) {
+        float2* R32 = rows32 + (size_t)idx * ROW_STRIDE;
+        auto    put = [&](int f) {
+            const ds v = ds_of_double(R[f]);
+            R32[f]     = make_float2(v.h, v.l);
+        };
         put(RF_KX);
         put(RF_KY);
         put(RF_KZ);
@@ -454,6 +468,56 @@ __global__ void __launch_bounds__(256) k_assemble_tiles(const DevParams P, const
     }
 }
 
+// Whether the double-single nonlocal element must give way to the FP64 one for the pair of norms
+// (n1, n2): where the reference's far branch divides rounding-level differences (|n1 - n2| within
+// 1e-5 of the norms), and for gaussian wells where i2's closed form cancels (x <= 2). far returns
+// the reference's branch.
+__device__ __forceinline__ bool nl_needs_fp64(const DevParams& P, double n1, double n2, bool& far) {
+    const double dn = fabs(n1 - n2);
+    far             = F_l_far(n1, n2);
+    if (far && dn < 1.0e-5 * fmax(n1, n2)) return true;
+    if (!P.square) {
+        if (P.has_A2a && 0.5 * (P.R2a * P.R2a) * (n1 * n2) <= 2.0) return true;
+        if (!P.same_nl && P.has_A2c && 0.5 * (P.R2c * P.R2c) * (n1 * n2) <= 2.0) return true;
+    }
+    return false;
+}
+
+// compute_soc_contribution (SpinOrbitFunctional.cpp:111-138) in double-single: sv = (re, im) of
+// s00, s01, s10, s11, as soc_element.
+__device__ __forceinline__ void soc_element_ds(const DevParamsDS& Q, const float2* Ri, const float2* Rj, ds pc, ds ps,
+                                               ds* sv) {
+    const ds l1  = ds_mul(ds_mul(Q.mu_soc, rd(Ri, RF_BC)), rd(Rj, RF_BC));
+    const ds l2  = ds_mul(ds_mul(Q.alpha_mu_soc, rd(Ri, RF_BA)), rd(Rj, RF_BA));
+    const ds ls  = ds_mulf(ds_add(l1, l2), 0.5f);
+    const ds la  = ds_mulf(ds_sub(l1, l2), 0.5f);
+    const ds Kx = rd(Ri, RF_KGX), Ky = rd(Ri, RF_KGY), Kz = rd(Ri, RF_KGZ);
+    const ds Qx = rd(Rj, RF_KGX), Qy = rd(Rj, RF_KGY), Qz = rd(Rj, RF_KGZ);
+    const ds cz  = ds_sub(ds_mul(Kx, Qy), ds_mul(Ky, Qx));
+    const ds cxv = ds_sub(ds_mul(Ky, Qz), ds_mul(Kz, Qy));
+    const ds cyv = ds_sub(ds_mul(Kx, Qz), ds_mul(Kz, Qx));
+    const ds phr = ds_mul(la, ps), phi = ds_neg(ds_mul(ls, pc));
+    sv[0] = ds_mul(cz, phr);
+    sv[1] = ds_mul(cz, phi);
+    sv[2] = ds_sub(ds_mul(cxv, phr), ds_mul(cyv, phi));
+    sv[3] = ds_add(ds_mul(cxv, phi), ds_mul(cyv, phr));
+    sv[4] = ds_add(ds_mul(cxv, phr), ds_mul(cyv, phi));
+    sv[5] = ds_sub(ds_mul(cxv, phi), ds_mul(cyv, phr));
+    sv[6] = ds_neg(sv[0]);
+    sv[7] = ds_neg(sv[1]);
+}
+
+template <typename SO>
+__device__ __forceinline__ SO make_stored(ds re, ds im);
+template <>
+__device__ __forceinline__ ds2 make_stored<ds2>(ds re, ds) {
+    return ds2{re.h, re.l};
+}
+template <>
+__device__ __forceinline__ ds4 make_stored<ds4>(ds re, ds im) {
+    return ds4{re.h, re.l, im.h, im.l};
+}
+
 // The mixed path without spin-orbit coupling and with square nonlocal wells: the same tiles, each
 // element formed in double-single arithmetic (nl_element_ds) from the k-independent V and structure
 // phase in FP32 pairs (Vloc32, phNL32: re hi, re lo, im hi, im lo) and the rows' double-single copy,
@@ -490,14 +554,9 @@ __global__ void __launch_bounds__(256) k_assemble_tiles_ds(const DevParams P, co
         if (i < N && j < N && i >= j) {
             const double  n1 = rows[((size_t)b * N + i) * ROW_STRIDE + RF_NK];
             const double  n2 = rows[((size_t)b * N + j) * ROW_STRIDE + RF_NK];
-            const double  dn = fabs(n1 - n2);
-            const bool    far = F_l_far(n1, n2);
-            // gaussian wells: i2's closed form cancels below x = 2 (the FP64 element handles it)
-            const bool    small_x = !P.square && 0.5 * (P.R2a * P.R2a) * (n1 * n2) <= 2.0 &&
-                                 (P.has_A2a || (P.has_A2c && !P.same_nl));
+            bool          far;
             SO            v;
-            if ((far && dn < 1.0e-5 * fmax(n1, n2)) || small_x ||
-                (!P.square && !P.same_nl && P.has_A2c && 0.5 * (P.R2c * P.R2c) * (n1 * n2) <= 2.0)) {
+            if (nl_needs_fp64(P, n1, n2, far)) {
                 v = stored(Hb, scalar_element<true>(P, Vloc, phNL, rows, b, i, j));
             } else {
                 const float2* Ri = rows32 + ((size_t)b * N + i) * ROW_STRIDE;
@@ -554,13 +613,18 @@ template void launch_assemble_ds<ds4>(const DevParams&, const DevParamsDS&, cons
 // and (i, j + N), coalesced down their columns; their Hermitian mirrors (j, i), (j + N, i + N),
 // (j, i + N) and (j + N, i) go through a shared-memory transpose. On the diagonal (i = j) the
 // mirror of DU(i, i) fills (i, i + N), as in the element-per-thread form.
-template <bool NL, typename SO>
+// DSM (the mixed path, SO = ds2 / ds4): the four values in double-single arithmetic on the FP32
+// pipe from the FP32-pair tables (Vloc32, phNL32, phSO32) and rows32, the nonlocal part by
+// nl_element_ds, and the FP64 element where that one routes an element to FP64.
+template <bool NL, bool DSM, typename SO>
 __global__ void __launch_bounds__(256) k_assemble_soc_tiles(const DevParams P, const cx<double>* __restrict__ Vloc,
                                                             const double2* __restrict__ phNL,
                                                             const double2* __restrict__ phSO, const double* __restrict__ rows,
                                                             SO* __restrict__ H, int ld, size_t mstride,
                                                             typename Lower<SO>::type* __restrict__ H32,
-                                                            size_t mstride32, int batch) {
+                                                            size_t mstride32, int batch, const DevParamsDS Q,
+                                                            const float4* __restrict__ Vloc32, const float4* __restrict__ phNL32,
+                                                            const float4* __restrict__ phSO32, const float2* __restrict__ rows32) {
     using SF = typename Lower<SO>::type;
     extern __shared__ __align__(16) unsigned char smraw[];
     SO(*tile)[32][33] = reinterpret_cast<SO(*)[32][33]>(smraw);  // [4][jl][il]: UU, DD, DU, UD of h(i, j)
@@ -584,15 +648,50 @@ __global__ void __launch_bounds__(256) k_assemble_soc_tiles(const DevParams P, c
     for (int q = 0; q < 4; ++q) {
         const int jl = ty + 8 * q, i = ti * 32 + tx, j = tj * 32 + jl;
         if (i < N && j < N && i >= j) {
-            const cx<double> h  = scalar_element<NL>(P, Vloc, phNL, rows, b, i, j);
-            const double*    Ri = rows + ((size_t)b * N + i) * ROW_STRIDE;
-            const double*    Rj = rows + ((size_t)b * N + j) * ROW_STRIDE;
-            const double2    ph = phSO[(size_t)j * N + i];
-            cx<double>       sv[4];
-            soc_element(P, Ri, Rj, ph.x, ph.y, sv);
-            const SO uu = stored(Hb, mk(h.x + sv[0].x, h.y + sv[0].y));
-            const SO dd = stored(Hb, mk(h.x + sv[3].x, h.y + sv[3].y));
-            const SO du = stored(Hb, sv[2]);
+            SO   uu, dd, du, ud;
+            bool fp64 = true;
+            if constexpr (DSM) {
+                const float2* Ri32 = rows32 + ((size_t)b * N + i) * ROW_STRIDE;
+                const float2* Rj32 = rows32 + ((size_t)b * N + j) * ROW_STRIDE;
+                const float4  vl   = Vloc32[(size_t)j * N + i];
+                ds            hr = ds{vl.x, vl.y}, hm = ds{vl.z, vl.w};
+                if (i == j) hr = ds_add(hr, rd(Ri32, RF_KIN));
+                fp64 = false;
+                if (NL) {
+                    const double n1 = rows[((size_t)b * N + i) * ROW_STRIDE + RF_NK];
+                    const double n2 = rows[((size_t)b * N + j) * ROW_STRIDE + RF_NK];
+                    bool         far;
+                    fp64 = nl_needs_fp64(P, n1, n2, far);
+                    if (!fp64) {
+                        const float4 pn = phNL32[(size_t)j * N + i];
+                        ds           vr, vi;
+                        nl_element_ds(Q, Ri32, Rj32, ds{pn.x, pn.y}, ds{pn.z, pn.w}, far, vr, vi);
+                        hr = ds_add(hr, vr);
+                        hm = ds_add(hm, vi);
+                    }
+                }
+                if (!fp64) {
+                    const float4 ps = phSO32[(size_t)j * N + i];
+                    ds           sv[8];
+                    soc_element_ds(Q, Ri32, Rj32, ds{ps.x, ps.y}, ds{ps.z, ps.w}, sv);
+                    uu = make_stored<SO>(ds_add(hr, sv[0]), ds_add(hm, sv[1]));
+                    dd = make_stored<SO>(ds_add(hr, sv[6]), ds_add(hm, sv[7]));
+                    du = make_stored<SO>(sv[4], sv[5]);
+                    ud = make_stored<SO>(sv[2], sv[3]);
+                }
+            }
+            if (fp64) {
+                const cx<double> h  = scalar_element<NL>(P, Vloc, phNL, rows, b, i, j);
+                const double*    Ri = rows + ((size_t)b * N + i) * ROW_STRIDE;
+                const double*    Rj = rows + ((size_t)b * N + j) * ROW_STRIDE;
+                const double2    ph = phSO[(size_t)j * N + i];
+                cx<double>       sv[4];
+                soc_element(P, Ri, Rj, ph.x, ph.y, sv);
+                uu = stored(Hb, mk(h.x + sv[0].x, h.y + sv[0].y));
+                dd = stored(Hb, mk(h.x + sv[3].x, h.y + sv[3].y));
+                du = stored(Hb, sv[2]);
+                ud = stored(Hb, sv[1]);
+            }
             put(i, j, uu);
             put(i + N, j + N, dd);
             put(i + N, j, du);
@@ -600,7 +699,6 @@ __global__ void __launch_bounds__(256) k_assemble_soc_tiles(const DevParams P, c
             tile[1][jl][tx] = dd;
             tile[2][jl][tx] = du;
             if (i > j) {
-                const SO ud = stored(Hb, sv[1]);
                 put(i, j + N, ud);
                 tile[3][jl][tx] = ud;
             }
@@ -646,9 +744,10 @@ void launch_assemble(const DevParams& P, const cx<double>* Vloc, const double2* 
     const int    T    = (P.N + 31) / 32;
     dim3         grd(T * (T + 1) / 2, batch);
     const size_t smem = sizeof(SO) * 4 * 32 * 33;
-    auto         kern = P.nl ? k_assemble_soc_tiles<true, SO> : k_assemble_soc_tiles<false, SO>;
+    auto         kern = P.nl ? k_assemble_soc_tiles<true, false, SO> : k_assemble_soc_tiles<false, false, SO>;
     if (smem > 48 * 1024) cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    kern<<<grd, blk, smem, s>>>(P, Vloc, phNL, phSO, rows, H, ld, mstride, H32, mstride32, batch);
+    kern<<<grd, blk, smem, s>>>(P, Vloc, phNL, phSO, rows, H, ld, mstride, H32, mstride32, batch, DevParamsDS{}, nullptr,
+                                nullptr, nullptr, nullptr);
     count_launch();
 }
 
@@ -664,5 +763,23 @@ template void launch_assemble<ds2>(const DevParams&, const cx<double>*, const do
                                    int, size_t, float*, size_t, int, cudaStream_t);
 template void launch_assemble<ds4>(const DevParams&, const cx<double>*, const double2*, const double2*, const double*, ds4*,
                                    int, size_t, cx<float>*, size_t, int, cudaStream_t);
+
+template <typename SO>
+void launch_assemble_soc_ds(const DevParams& P, const DevParamsDS& Q, const float4* Vloc32, const float4* phNL32,
+                            const float4* phSO32, const float2* rows32, const cx<double>* Vloc, const double2* phNL,
+                            const double2* phSO, const double* rows, SO* H, int ld, size_t mstride,
+                            typename Lower<SO>::type* H32, size_t mstride32, int batch, cudaStream_t s) {
+    const int    T    = (P.N + 31) / 32;
+    dim3         grd(T * (T + 1) / 2, batch), blk(32, 8);
+    const size_t smem = sizeof(SO) * 4 * 32 * 33;
+    auto         kern = P.nl ? k_assemble_soc_tiles<true, true, SO> : k_assemble_soc_tiles<false, true, SO>;
+    if (smem > 48 * 1024) cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    kern<<<grd, blk, smem, s>>>(P, Vloc, phNL, phSO, rows, H, ld, mstride, H32, mstride32, batch, Q, Vloc32, phNL32, phSO32,
+                                rows32);
+    count_launch();
+}
+template void launch_assemble_soc_ds<ds4>(const DevParams&, const DevParamsDS&, const float4*, const float4*, const float4*,
+                                          const float2*, const cx<double>*, const double2*, const double2*, const double*,
+                                          ds4*, int, size_t, cx<float>*, size_t, int, cudaStream_t);
 
 }  // namespace uepm

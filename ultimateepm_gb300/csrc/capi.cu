@@ -168,7 +168,7 @@ Layout plan(const uepm_ctx* ctx, int nb, uint32_t want, size_t c) {
         return o;
     };
     L.rows   = take(c * N * ROW_STRIDE * sizeof(double));
-    L.rows32 = (mixed && ctx->ds_nl) ? take(c * N * ROW_STRIDE * sizeof(float2)) : 0;
+    L.rows32 = (mixed && (ctx->ds_nl || ctx->ds_soc)) ? take(c * N * ROW_STRIDE * sizeof(float2)) : 0;
     L.H    = take(mixed && ctx->sparse_local ? 0 : c * n * n * es);  // the sparse path never forms it
     L.H32  = mixed ? take(c * n * n * es32) : 0;
     L.d    = take(c * n * rs);
@@ -222,7 +222,7 @@ void run_chunk(uepm_ctx* ctx, const Layout& L, char* ws, const double* kk, int c
     const size_t mstride = (size_t)n * n;
     auto*        rows    = reinterpret_cast<double*>(ws + L.rows);
     auto*        H       = reinterpret_cast<S*>(ws + L.H);
-    const bool   ds_asm  = ctx->precision == UEPM_PREC_MIXED && ctx->ds_nl;
+    const bool   ds_asm  = ctx->precision == UEPM_PREC_MIXED && (ctx->ds_nl || ctx->ds_soc);
     auto*        rows32  = ds_asm ? reinterpret_cast<float2*>(ws + L.rows32) : nullptr;
     {
         ProfScope p(ctx, s, KK_ROWS);
@@ -271,7 +271,11 @@ void run_chunk(uepm_ctx* ctx, const Layout& L, char* ws, const double* kk, int c
         // with a local potential only, those products use the resident sparse V instead
         if (ctx->sparse_local)
             launch_assemble<S32>(ctx->P, ctx->d_Vloc, ctx->d_phNL, ctx->d_phSO, rows, H32, n, mstride, nullptr, 0, c, s);
-        else if (ds_asm)
+        else if (ds_asm && ctx->ds_soc) {
+            if constexpr (std::is_same<SP, ds4>::value)
+                launch_assemble_soc_ds<SP>(ctx->P, ctx->Q, ctx->d_Vloc32, ctx->d_phNL32, ctx->d_phSO32, rows32, ctx->d_Vloc,
+                                           ctx->d_phNL, ctx->d_phSO, rows, Hs, n, mstride, H32, mstride, c, s);
+        } else if (ds_asm)
             launch_assemble_ds<SP>(ctx->P, ctx->Q, ctx->d_Vloc32, ctx->d_phNL32, rows32, ctx->d_Vloc, ctx->d_phNL, rows, Hs, n,
                                    mstride, H32, mstride, c, s);
         else
@@ -525,8 +529,9 @@ int uepm_ctx_create(const uepm_material* mat, const int32_t* G, int N, uint32_t 
         if ((e = cudaMemcpy(ctx->d_phNL, phNL.data(), sizeof(double2) * phNL.size(), cudaMemcpyHostToDevice)) != cudaSuccess)
             return fail(e, "copy phNL");
     }
-    ctx->ds_nl = nl && !soc && (P.has_R0a || P.has_R0c || P.has_A2a || P.has_A2c);
-    if (ctx->ds_nl) {
+    ctx->ds_nl  = nl && !soc && (P.has_R0a || P.has_R0c || P.has_A2a || P.has_A2c);
+    ctx->ds_soc = soc;
+    if (ctx->ds_nl || ctx->ds_soc) {
         // the nonlocal constants and the k-independent tables as FP32 pairs; products the FP64
         // element forms first are formed here in FP64, in the same order
         DevParamsDS& Q = ctx->Q;
@@ -557,19 +562,25 @@ int uepm_ctx_create(const uepm_material* mat, const int32_t* G, int N, uint32_t 
         Q.gA2c         = ds_of_double(P.gpre_c * P.A2c);
         Q.R2a2h        = ds_of_double(0.5 * (P.R2a * P.R2a));
         Q.R2c2h        = ds_of_double(0.5 * (P.R2c * P.R2c));
-        std::vector<float4> v32(V.size()), p32(V.size());
-        for (size_t q = 0; q < V.size(); ++q) {
-            const ds a = ds_of_double(V[q].x), b = ds_of_double(V[q].y);
-            const ds c = ds_of_double(phNL[q].x), d = ds_of_double(phNL[q].y);
-            v32[q]     = make_float4(a.h, a.l, b.h, b.l);
-            p32[q]     = make_float4(c.h, c.l, d.h, d.l);
-        }
-        if ((e = cudaMalloc(&ctx->d_Vloc32, sizeof(float4) * v32.size())) != cudaSuccess) return fail(e, "cudaMalloc(V32)");
-        if ((e = cudaMemcpy(ctx->d_Vloc32, v32.data(), sizeof(float4) * v32.size(), cudaMemcpyHostToDevice)) != cudaSuccess)
-            return fail(e, "copy V32");
-        if ((e = cudaMalloc(&ctx->d_phNL32, sizeof(float4) * p32.size())) != cudaSuccess) return fail(e, "cudaMalloc(phNL32)");
-        if ((e = cudaMemcpy(ctx->d_phNL32, p32.data(), sizeof(float4) * p32.size(), cudaMemcpyHostToDevice)) != cudaSuccess)
-            return fail(e, "copy phNL32");
+        Q.mu_soc       = ds_of_double(P.mu_soc);
+        Q.alpha_mu_soc = ds_of_double(P.alpha_soc * P.mu_soc);
+        auto pairs4 = [](const std::vector<double2>& src) {
+            std::vector<float4> out(src.size());
+            for (size_t q = 0; q < src.size(); ++q) {
+                const ds a = ds_of_double(src[q].x), b = ds_of_double(src[q].y);
+                out[q]     = make_float4(a.h, a.l, b.h, b.l);
+            }
+            return out;
+        };
+        auto upload = [&](float4** dst, const std::vector<float4>& v, const char* what) -> cudaError_t {
+            cudaError_t r = cudaMalloc(dst, sizeof(float4) * v.size());
+            if (r == cudaSuccess) r = cudaMemcpy(*dst, v.data(), sizeof(float4) * v.size(), cudaMemcpyHostToDevice);
+            if (r != cudaSuccess) set_error(std::string(what) + ": " + cudaGetErrorString(r));
+            return r;
+        };
+        if ((e = upload(&ctx->d_Vloc32, pairs4(V), "V32")) != cudaSuccess) return fail(e, "upload(V32)");
+        if (nl && (e = upload(&ctx->d_phNL32, pairs4(phNL), "phNL32")) != cudaSuccess) return fail(e, "upload(phNL32)");
+        if (soc && (e = upload(&ctx->d_phSO32, pairs4(phSO), "phSO32")) != cudaSuccess) return fail(e, "upload(phSO32)");
     }
     if (soc) {
         if ((e = cudaMalloc(&ctx->d_phSO, sizeof(double2) * phSO.size())) != cudaSuccess) return fail(e, "cudaMalloc(phSO)");
@@ -640,6 +651,7 @@ int uepm_ctx_destroy(uepm_ctx* ctx) {
     if (ctx->d_phSO) cudaFree(ctx->d_phSO);
     if (ctx->d_Vloc32) cudaFree(ctx->d_Vloc32);
     if (ctx->d_phNL32) cudaFree(ctx->d_phNL32);
+    if (ctx->d_phSO32) cudaFree(ctx->d_phSO32);
     if (ctx->d_ell_col) cudaFree(ctx->d_ell_col);
     if (ctx->d_ell_re) cudaFree(ctx->d_ell_re);
     if (ctx->d_ell_im) cudaFree(ctx->d_ell_im);

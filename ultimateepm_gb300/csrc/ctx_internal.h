@@ -32,6 +32,8 @@ struct uepm_ctx {
     uepm::DevParamsDS Q{};
     float4*           d_Vloc32  = nullptr;
     float4*           d_phNL32  = nullptr;
+    bool              ds_soc    = false;  // spin-orbit: the same, with the spin-orbit phase in pairs
+    float4*           d_phSO32  = nullptr;
     // local potential only (no nonlocal, no spin-orbit): H(k) = V + diag(kinetic(k)) with V the
     // k-independent local form-factor matrix, sparse (|G_i - G_j|^2 in {3, 4, 8, 11}); its rows as
     // CSR (every row also lists its diagonal) with values as FP32 pairs, for the mixed path's H X

@@ -343,6 +343,8 @@ struct DevParamsDS {
     // gaussian d-wells: V2 = (gpre A2) P2 i2(x) e_i e_j with x = (R2^2 / 2) n1 n2
     int  square;
     ds   gA2a, gA2c, R2a2h, R2c2h;  // gpre A2, R2^2 / 2
+    // spin-orbit: lambda_1 = mu B_c B_c', lambda_2 = (alpha mu) B_a B_a'
+    ds   mu_soc, alpha_mu_soc;
 };
 
 // Per-(k, basis vector) quantities computed once per k in the row kernel and read by the

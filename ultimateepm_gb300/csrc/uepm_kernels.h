@@ -18,6 +18,13 @@ void launch_rows(const DevParams& P, const double* d_k, const int* d_G, double* 
 // Mixed path, no spin-orbit, square nonlocal wells: the assembly in double-single arithmetic on the
 // FP32 pipe (SO = ds2 or ds4), from the k-independent tables in FP32 pairs and d_rows32 (written by
 // launch_rows when given).
+// The same with spin-orbit coupling (SO = ds4): the scalar part and the spin-orbit blocks in
+// double-single, the FP64 element where the nonlocal part needs it.
+template <typename SO>
+void launch_assemble_soc_ds(const DevParams& P, const DevParamsDS& Q, const float4* Vloc32, const float4* phNL32,
+                            const float4* phSO32, const float2* rows32, const cx<double>* Vloc, const double2* phNL,
+                            const double2* phSO, const double* rows, SO* H, int ld, size_t mstride,
+                            typename Lower<SO>::type* H32, size_t mstride32, int batch, cudaStream_t s);
 template <typename SO>
 void launch_assemble_ds(const DevParams& P, const DevParamsDS& Q, const float4* Vloc32, const float4* phNL32,
                         const float2* rows32, const cx<double>* Vloc, const double2* phNL, const double* rows, SO* H,
