@@ -124,12 +124,14 @@ __global__ void __launch_bounds__(kProjNT) k_refine_project(const typename Split
         cp_async_wait_all();
         __syncthreads();
     }
-    // ---- Y = H X: item (block of kProjVB vectors, row r); H(r, c) coalesced over r ----------------
+    // ---- Y = H X: item (row r, block of kProjVB vectors), the vector block fastest, so that the
+    // lanes sharing a row take H(r, c) in one request and each element of H leaves memory once;
+    // H(r, c + 1) is fetched while the products of column c run --------------------------------------
     YT*       Y    = reinterpret_cast<YT*>(work) + (size_t)b * refine_work_elems(n, m) * sizeof(S) / sizeof(YT);  // [r][mp]
     const SE* A    = H + (size_t)b * mstride;
     const int nblk = mp / kProjVB;
     for (int item = tid; item < nblk * n; item += kProjNT) {
-        const int jb = item / n, r = item - jb * n, j0 = jb * kProjVB;
+        const int r = item / nblk, jb = item - r * nblk, j0 = jb * kProjVB;
         dsacc     yr[kProjVB], yi[kProjVB];
 #pragma unroll
         for (int q = 0; q < kProjVB; ++q) yr[q] = yi[q] = dsacc{0.f, 0.f};
@@ -142,7 +144,12 @@ __global__ void __launch_bounds__(kProjNT) k_refine_project(const typename Split
                 proj_accumulate<S, STAGED>(yr, yi, sparse_slot<S>(sv, o), Xs, Xg, n, m, mp, sv.col[o], j0);
             }
         } else {
-            for (int c = 0; c < n; ++c) proj_accumulate<S, STAGED>(yr, yi, A[(size_t)c * ld + r], Xs, Xg, n, m, mp, c, j0);
+            SE h = A[r];
+            for (int c = 0; c < n; ++c) {
+                const SE hc = h;
+                if (c + 1 < n) h = A[(size_t)(c + 1) * ld + r];
+                proj_accumulate<S, STAGED>(yr, yi, hc, Xs, Xg, n, m, mp, c, j0);
+            }
         }
 #pragma unroll
         for (int q = 0; q < kProjVB; ++q) {
