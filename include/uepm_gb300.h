@@ -191,7 +191,9 @@ int uepm_measure_peak(int precision, double* tflops);
  *                 beyond the on-chip sizes, n <= 512), 5 the same with every other update deferred
  *                 to the next pass (a read-only pass, then a rank-4 pass: 3 passes per two steps), 6 blocked:
  *                 panels of 16 columns whose updates are applied once per panel, only the lower
- *                 triangle read and written, one matrix per SM (FP32, n <= 512);
+ *                 triangle read and written, one matrix per SM (FP32, n <= 512), the complex panel
+ *                 updates on the tensor cores (tcgen05, TF32 with hi/lo operand splits: FP32-level
+ *                 products), 7 the same blocked reduction with every update on the FP32 pipe;
  *                 automatic: 1 where it applies, 6 for the FP32 orders 300..512, 5 for the other FP32
  *                 matrices, else 2
  *   ctas_per_sm   CTAs per SM of the global-memory reduction (its L2 working set), 1..8

@@ -233,10 +233,11 @@ def test_vectors_at_size_are_orthonormal_eigenvectors(gpu, oracle, mats, precisi
     ctx.close()
 
 
-@pytest.mark.parametrize("reduction", [2, 3, 4, 5, 6])
+@pytest.mark.parametrize("reduction", [2, 3, 4, 5, 6, 7])
 def test_mixed_precision_complex_reductions(gpu, oracle, mats, reduction):
     """Every FP32 reduction kernel on a complex matrix (InP with nonlocal wells, n = 113, which fits
-    shared memory): 2 shared memory, 3 cluster, 4 fused, 5 deferred, 6 blocked."""
+    shared memory): 2 shared memory, 3 cluster, 4 fused, 5 deferred, 6 blocked with the first
+    panel's trailing update on the tensor cores, 7 blocked with SIMT updates only."""
     key, shells, nl, soc, _ = _case("inp_nl_113")
     G = oracle.generate_basis(shells)
     ks = _kset(oracle, 37, 10)
@@ -406,17 +407,19 @@ def test_real_and_complex_kernels_agree(gpu, oracle, mats):
         assert np.abs(Er - Ec).max() <= tol
 
 
+@pytest.mark.parametrize("reduction", [6, 7])
 @pytest.mark.parametrize("case,nb", [("ge_nl_soc_181", 16), ("gaas_nl_soc_89", 16), ("si_d_nonlocal_137", 12),
                                      ("alas_local_169", 16)])
-def test_blocked_reduction_against_the_oracle(gpu, oracle, mats, case, nb):
-    """The blocked reduction (tuning 6: panels of 16 columns, lower triangle only) on complex orders
-    362, 178 and 169 (odd: unaligned row pairs) and the real order 137, mixed precision: eigenvalues
-    against the oracle within 1e-6 eV, Ritz vectors orthonormal."""
+def test_blocked_reduction_against_the_oracle(gpu, oracle, mats, case, nb, reduction):
+    """The blocked reduction (panels of 16 columns, lower triangle only; tuning 6 with the complex
+    trailing updates on the tensor cores, tcgen05 TF32 with hi/lo splits, 7 with SIMT updates) on
+    complex orders 362, 178 and 169 (odd: unaligned row pairs) and the real order 137, mixed
+    precision: eigenvalues against the oracle within 1e-6 eV, Ritz vectors orthonormal."""
     key, shells, nl, soc, fcx = _case(case)
     G = oracle.generate_basis(shells)
     ks = _kset(oracle, 41, 6)
     ctx = _ctx(mats[key], G, nl, soc, N.UEPM_PREC_MIXED, force_complex=fcx)
-    N.check(gpu.uepm_ctx_set_tuning(ctx.h, C.byref(N.UepmTuning(reduction=6))))
+    N.check(gpu.uepm_ctx_set_tuning(ctx.h, C.byref(N.UepmTuning(reduction=reduction))))
     E, X, _, st = ctx.solve(ks, nb, vectors=True)
     Eo = oracle.band_structure(mats[key], G, ks, nb, nl=nl, soc=soc)["E"]
     assert not st.any()

@@ -51,7 +51,7 @@ TuneKey tune_key(const uepm_ctx* ctx, int nb, uint32_t want) {
 }
 
 bool valid_tuning(const uepm_ctx* ctx, const uepm_tuning& t) {
-    if (t.reduction < 0 || t.reduction > 6) return false;
+    if (t.reduction < 0 || t.reduction > 7) return false;
     if (t.ctas_per_sm < 0 || t.ctas_per_sm > 8) return false;
     if (t.cluster != 0 && t.cluster != 2 && t.cluster != 4 && t.cluster != 8 && t.cluster != 16) return false;
     if (t.vector_lanes != 0 && t.vector_lanes != 8 && t.vector_lanes != 16 && t.vector_lanes != 32) return false;

@@ -788,8 +788,8 @@ void launch_tridiag(S* H, int n, int ld, size_t mstride, typename ST<S>::R* d, t
         // the blocked kernel (6) is automatic from order 300 (2000 k, mixed: Ge SOC n = 362 81.3 ->
         // 47.5 ms, Si SOC n = 338 67.1 -> 41.7, GaP SOC n = 458 198.3 -> 81.8); below, the deferred
         // kernel stays ahead (GaAs SOC n = 178 9.5 against 12.6 ms, InAs n = 229 equal)
-        if ((variant == 6 || (variant == 0 && n >= 300)) &&
-            launch_tridiag_blocked<S>(H, n, ld, mstride, d, e, tq, status, batch, s))
+        if ((variant == 6 || variant == 7 || (variant == 0 && n >= 300)) &&
+            launch_tridiag_blocked<S>(H, n, ld, mstride, d, e, tq, status, batch, s, variant != 7))
             return;
         // automatic: the deferred kernel for every FP32 order beyond the register kernel, also where
         // the matrix would fit shared memory (2000 k: Ge nonlocal n = 181 real 5.85 ms against 14.3

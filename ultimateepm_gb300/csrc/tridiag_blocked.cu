@@ -29,6 +29,7 @@
 #include <algorithm>
 #include <type_traits>
 
+#include "tcgen05.cuh"
 #include "uepm_common.cuh"
 #include "uepm_kernels.h"
 
@@ -39,6 +40,21 @@ namespace {
 constexpr int kBlkNT = 512;  // threads per CTA (16 warps)
 constexpr int kBlkNW = kBlkNT / 32;
 constexpr int kBlkNB = 16;   // panel width
+
+// Tensor-core trailing update (complex matrices): tiles of 128 rows x NC columns (NC = 64, 48 or
+// 32, the widest whose operand staging fits shared memory) of the trailing matrix, D = P_rows
+// Q_cols^T in the real form with K = 64 (Re V, Im V, Re W, Im W of the panel's 16 reflectors), each
+// operand split into TF32 hi + lo parts (hi hi + hi lo + lo hi: FP32-level products), accumulated in
+// TMEM. The column operand and the accumulators are double-buffered, so that the MMAs of one tile run
+// while the previous tile is read back and the next one staged.
+constexpr int      kTcM       = 128;
+constexpr int      kTcK       = 4 * kBlkNB;
+constexpr int      kTcCols    = 512;  // TMEM columns: 2 buffers x (Re, Im+, Im-) x 64
+constexpr int      kTcMinRows = 96;   // smaller trailing matrices take the SIMT update
+__host__ __device__ constexpr size_t tc_stage_bytes(int nc) {  // A hi/lo, two B buffers hi/lo
+    return (size_t)2 * (kTcM + 2 * nc) * kTcK * sizeof(float);
+}
+constexpr long long kTcWaitCycles = 2000000000ll;  // ~1 s at the SM clock: a bounded wait
 
 template <typename S>
 __device__ __forceinline__ S sh_xor(S v, int o);
@@ -68,12 +84,185 @@ struct BlkSmem {
         return sizeof(S) * ((size_t)2 * kBlkNB * n + (size_t)kBlkNW * n + (n + 32) + 2 * kBlkNB) +
                sizeof(R) * 4 * kBlkNW + 64;
     }
+    // with the tensor-core update: its operand staging overlays the per-warp partial vectors and
+    // everything after them (dead during the trailing update; the zero padding of v is restored)
+    static __host__ __device__ size_t bytes_tc(int n, int nc) {
+        const size_t stage = sizeof(S) * (size_t)2 * kBlkNB * n + tc_stage_bytes(nc);
+        const size_t base  = bytes(n);
+        return stage > base ? stage : base;
+    }
 };
+
+// Rows [r0, r0 + ROWS) of the panel in the real K-major form of the tensor-core operands: K index
+// 0..15 Re V_k, 16..31 Im V_k, 32..47 Re W_k, 48..63 Im W_k; element (r, k) at float
+// (k / 4) * ROWS * 4 + (r - r0) * 4 + k % 4, split into TF32 hi (rounded to nearest) and the FP32
+// remainder lo. Rows past n are zero.
+template <int ROWS>
+__device__ __forceinline__ void tc_stage(const cx<float>* Vp, const cx<float>* Wp, int n, int r0, float* hi, float* lo) {
+    for (int it = threadIdx.x; it < ROWS * 8; it += kBlkNT) {
+        const int rl = it % ROWS, gq = it / ROWS;  // consecutive threads: consecutive rows
+        const int w = gq >> 2, g = gq & 3, r = r0 + rl;
+        const cx<float>* src = (w ? Wp : Vp) + (size_t)(4 * g) * n + r;
+        float re[4], im[4];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const cx<float> x = (r < n) ? src[(size_t)j * n] : cx<float>{0.f, 0.f};
+            re[j]             = x.x;
+            im[j]             = x.y;
+        }
+        const int gre = w * 8 + g, gim = gre + 4;  // 4-wide K groups of the Re and Im parts
+        float4    h, l;
+        h.x = tc::to_tf32(re[0]); h.y = tc::to_tf32(re[1]); h.z = tc::to_tf32(re[2]); h.w = tc::to_tf32(re[3]);
+        l   = make_float4(re[0] - h.x, re[1] - h.y, re[2] - h.z, re[3] - h.w);
+        *reinterpret_cast<float4*>(hi + ((size_t)gre * ROWS + rl) * 4) = h;
+        *reinterpret_cast<float4*>(lo + ((size_t)gre * ROWS + rl) * 4) = l;
+        h.x = tc::to_tf32(im[0]); h.y = tc::to_tf32(im[1]); h.z = tc::to_tf32(im[2]); h.w = tc::to_tf32(im[3]);
+        l   = make_float4(im[0] - h.x, im[1] - h.y, im[2] - h.z, im[3] - h.w);
+        *reinterpret_cast<float4*>(hi + ((size_t)gim * ROWS + rl) * 4) = h;
+        *reinterpret_cast<float4*>(lo + ((size_t)gim * ROWS + rl) * 4) = l;
+    }
+}
+
+// Waits (bounded) for the phase of the given parity; the same answer in every thread of the CTA.
+__device__ __forceinline__ bool tc_wait(uint64_t* bar, uint32_t parity) {
+    bool            ok = false;
+    const long long t0 = clock64();
+    while (!(ok = tc::mbar_try_wait(bar, parity)) && clock64() - t0 < kTcWaitCycles) {
+    }
+    return __syncthreads_and(ok) != 0;
+}
+
+// A tile of the tensor-core update: rows [rb, rb + 128) (stored: [rlo, rhi)), columns [cb, cb + NC)
+// (stored: [clo, chi)), its operand / accumulator buffer.
+struct TcTile {
+    int rb, rlo, rhi, cb, clo, chi, buf;
+};
+
+// One thread issues the tile's 48 MMAs (Re: 8 chunk pairs, Im+ and Im-: 4 each, 3 split products per
+// pair) into TMEM buffer t.buf and commits them to that buffer's mbarrier.
+template <int NC>
+__device__ __forceinline__ void tc_issue(const TcTile& t, const float* aH, const float* aL, const float* bH0,
+                                         uint32_t tbase, uint64_t* bar) {
+    tc::fence_after_sync();
+    constexpr uint32_t idesc = tc::idesc_tf32(kTcM, NC);
+    const float*       bH    = bH0 + (size_t)t.buf * 2 * NC * kTcK;
+    const float*       bL    = bH + (size_t)NC * kTcK;
+    const uint32_t     sa = tc::smem_addr(aH), sl = tc::smem_addr(aL), ta = tc::smem_addr(bH), tl = tc::smem_addr(bL);
+    // 8-wide K chunks: 0,1 Re V; 2,3 Im V; 4,5 Re W; 6,7 Im W
+    constexpr int pa[16] = {0, 1, 2, 3, 4, 5, 6, 7, 0, 1, 4, 5, 2, 3, 6, 7};
+    constexpr int pb[16] = {4, 5, 6, 7, 0, 1, 2, 3, 6, 7, 2, 3, 4, 5, 0, 1};
+#pragma unroll
+    for (int p = 0; p < 16; ++p) {
+        const int      acc   = p < 8 ? 0 : p < 12 ? 1 : 2;  // Re, Im+, Im-
+        const uint32_t d     = tbase + 192 * t.buf + 64 * acc;
+        const uint32_t oa    = 2 * pa[p] * kTcM * 16, ob = 2 * pb[p] * NC * 16;
+        const uint64_t ah    = tc::smem_desc(sa + oa, kTcM * 16, 128);
+        const uint64_t al    = tc::smem_desc(sl + oa, kTcM * 16, 128);
+        const uint64_t bh    = tc::smem_desc(ta + ob, NC * 16, 128);
+        const uint64_t bl    = tc::smem_desc(tl + ob, NC * 16, 128);
+        const uint32_t accum = (p == 0 || p == 8 || p == 12) ? 0u : 1u;  // the first MMA of D overwrites it
+        tc::mma_tf32(d, ah, bh, idesc, accum);
+        tc::mma_tf32(d, ah, bl, idesc, 1u);
+        tc::mma_tf32(d, al, bh, idesc, 1u);
+    }
+    tc::mma_commit(bar + t.buf);
+}
+
+// Every thread: its row and 16 columns of tile t from TMEM, A + (-Re, Im+ - Im-) stored (lower
+// triangle, the tile's own rows and columns). False if the wait gave up.
+template <int NC>
+__device__ __forceinline__ bool tc_readback(const TcTile& t, cx<float>* A, int ld, uint32_t tbase, uint64_t* bar,
+                                            uint32_t& phase) {
+    const int  lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int  qd = warp & 3, cg = warp >> 2;  // TMEM lane quarter, 16-column group
+    const int  r = t.rb + 32 * qd + lane, c0 = t.cb + 16 * cg;
+    const bool rok = r >= t.rlo && r < t.rhi && 16 * cg < NC;
+    cx<float>  x[16];
+#pragma unroll
+    for (int j = 0; j < 16; ++j) {
+        const int c = c0 + j;
+        x[j] = (rok && c >= t.clo && c < t.chi && c <= r) ? ldc(A + (size_t)c * ld + r) : cx<float>{0.f, 0.f};
+    }
+    const bool ok = tc_wait(bar + t.buf, (phase >> t.buf) & 1u);
+    phase ^= 1u << t.buf;
+    tc::fence_after_sync();
+    if (ok && 16 * cg < NC) {
+        const uint32_t tl = tbase + 192 * t.buf + ((uint32_t)(32 * qd) << 16) + 16 * cg;
+        float          dre[16], dip[16], dim[16];
+        tc::tmem_ld16(tl, dre);
+        tc::tmem_ld16(tl + 64, dip);
+        tc::tmem_ld16(tl + 128, dim);
+#pragma unroll
+        for (int j = 0; j < 16; ++j) {
+            const int c = c0 + j;
+            if (rok && c >= t.clo && c < t.chi && c <= r)
+                stc(A + (size_t)c * ld + r, cx<float>{x[j].x - dre[j], (r == c) ? 0.f : x[j].y + dip[j] - dim[j]});
+        }
+    }
+    tc::fence_before_sync();
+    return ok;
+}
+
+// A22 -= V W^H + W V^H on the tensor cores, lower triangle of rows / columns q0..n-1. Row blocks of
+// 128 and column blocks of NC are laid from the end (n rounded up to 8) towards q0; a block clamped
+// at q0 (rounded down to 8) overlaps its neighbour and stores only the rows / columns that are its
+// own. Tiles are pipelined: tile t's MMAs are issued, then tile t-1 is read back while they run, and
+// tile t+1 is staged into the other buffer. A new row block (its operand is restaged) first drains
+// the tile in flight. Returns false if a wait gave up (the update is then incomplete).
+template <int NC>
+__device__ bool tc_trailing_update(cx<float>* A, int n, int ld, int q0, const cx<float>* Vp, const cx<float>* Wp,
+                                   float* stage, uint32_t tbase, uint64_t* bar, uint32_t& phase) {
+    float*    aH = stage;
+    float*    aL = aH + (size_t)kTcM * kTcK;
+    float*    bH0 = aL + (size_t)kTcM * kTcK;  // buffer b: hi at bH0 + b * 2 NC K, lo NC K after it
+    const int base8 = q0 & ~7, n8 = (n + 7) & ~7;
+    bool      ok = true, pending = false;
+    TcTile    prev{};
+    int       buf = 0;
+    for (int rhi = n, rbe = n8; rhi > q0 && ok;) {
+        const int rb = max(rbe - kTcM, base8), rlo = max(rb, q0);
+        bool      first = true;
+        for (int chi = n, cbe = n8; chi > q0 && ok;) {
+            const int cb = max(cbe - NC, base8), clo = max(cb, q0);
+            if (clo < rhi) {  // the tile holds elements on or below the diagonal
+                if (first && pending) {  // the row operand is about to change: drain
+                    ok      = tc_readback<NC>(prev, A, ld, tbase, bar, phase);
+                    pending = false;
+                    if (!ok) break;
+                    __syncthreads();
+                }
+                const TcTile t{rb, rlo, rhi, cb, clo, chi, buf};
+                if (first) tc_stage<kTcM>(Vp, Wp, n, rb, aH, aL);
+                first = false;
+                tc_stage<NC>(Vp, Wp, n, cb, bH0 + (size_t)buf * 2 * NC * kTcK, bH0 + (size_t)buf * 2 * NC * kTcK + NC * kTcK);
+                tc::fence_async_smem();
+                tc::fence_before_sync();
+                __syncthreads();
+                if (threadIdx.x == 0) tc_issue<NC>(t, aH, aL, bH0, tbase, bar);
+                if (pending) ok = tc_readback<NC>(prev, A, ld, tbase, bar, phase);
+                prev    = t;
+                pending = true;
+                buf ^= 1;
+            }
+            chi = clo;
+            cbe = cb;
+        }
+        rhi = rlo;
+        rbe = rb;
+    }
+    if (pending) {
+        const bool ok2 = tc_readback<NC>(prev, A, ld, tbase, bar, phase);
+        ok             = ok && ok2;
+    }
+    __syncthreads();
+    return ok;
+}
 
 template <typename S>
 __global__ void __launch_bounds__(kBlkNT, 1)
     k_tridiag_blocked(S* __restrict__ H, int n, int ld, size_t mstride, typename ST<S>::R* __restrict__ dOut,
-                      typename ST<S>::R* __restrict__ eOut, S* __restrict__ tqOut, int* __restrict__ status, int batch) {
+                      typename ST<S>::R* __restrict__ eOut, S* __restrict__ tqOut, int* __restrict__ status, int batch,
+                      int use_tc) {
     using R = typename ST<S>::R;
     extern __shared__ __align__(16) unsigned char smraw[];
     S* Vp   = reinterpret_cast<S*>(smraw);              // [k][r], NB x n
@@ -83,10 +272,34 @@ __global__ void __launch_bounds__(kBlkNT, 1)
     S* tdot = v + (n + 32);                             // t1 (W^H v) then t2 (V^H v), NB each
     R* red  = reinterpret_cast<R*>(tdot + 2 * kBlkNB);  // 4 x NW
     __shared__ S s_c0;
+    __shared__ uint64_t s_bar[2];  // tensor-core completion, per operand / accumulator buffer
+    __shared__ uint32_t s_tmem;    // TMEM base address
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     // With an even order every column starts at an even element, so row pairs from an even row are
     // 16-byte (8-byte for real) aligned: the product's tiles then start at o rounded down to even.
     const bool vec = (n & 1) == 0 && (mstride & 1) == 0 && (ld & 1) == 0;
+    // the tensor-core update (complex only; use_tc = its column-block width, 0 off): TMEM for its
+    // accumulators, an mbarrier per buffer for its MMAs
+    constexpr bool TC = ST<S>::cplx;
+    bool           tc_on = TC && use_tc != 0;
+    uint32_t       tc_phase = 0, tbase = 0;  // bit b: parity of buffer b's next phase
+    if constexpr (TC) {
+        if (tc_on) {
+            if (tid == 0) {
+                tc::mbar_init(&s_bar[0], 1);
+                tc::mbar_init(&s_bar[1], 1);
+                asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+            }
+            if (warp == 0) {
+                tc::tmem_alloc(&s_tmem, kTcCols);
+                tc::tmem_relinquish();
+            }
+            tc::fence_before_sync();
+            __syncthreads();
+            tc::fence_after_sync();
+            tbase = s_tmem;
+        }
+    }
 
     for (int b = blockIdx.x; b < batch; b += gridDim.x) {
         S*   A   = H + (size_t)b * mstride;
@@ -329,7 +542,23 @@ __global__ void __launch_bounds__(kBlkNT, 1)
 
             // ---- trailing update A22 -= V W^H + W V^H (lower triangle, rows/cols q0..n-1) -----------
             const int q0 = j0 + jb, mt = n - q0;
-            if (mt > 0) {
+            bool      simt = mt > 0;
+            if constexpr (TC) {
+                if (tc_on && mt >= kTcMinRows) {
+                    simt = false;
+                    float* stage = reinterpret_cast<float*>(yp);
+                    const bool ok = use_tc == 64   ? tc_trailing_update<64>(A, n, ld, q0, Vp, Wp, stage, tbase, s_bar, tc_phase)
+                                    : use_tc == 48 ? tc_trailing_update<48>(A, n, ld, q0, Vp, Wp, stage, tbase, s_bar, tc_phase)
+                                                   : tc_trailing_update<32>(A, n, ld, q0, Vp, Wp, stage, tbase, s_bar, tc_phase);
+                    if (!ok) {
+                        // a wait gave up: this matrix is incomplete, and the CTA keeps to the SIMT update
+                        if (tid == 0 && status) atomicOr(status + b, 1);  // UEPM_K_NOCONVERGE
+                        tc_on = false;
+                    }
+                    for (int q = n + tid; q < n + 32; q += kBlkNT) v[q] = ST<S>::zero();  // staging overlaid it
+                }
+            }
+            if (simt) {
                 const int nt = (mt + 31) >> 5, T = nt * (nt + 1) / 2;
                 for (int t = warp; t < T; t += kBlkNW) {
                     int R_, C_;
@@ -380,6 +609,20 @@ __global__ void __launch_bounds__(kBlkNT, 1)
         bad = __syncthreads_or(bad);
         if (tid == 0 && bad && status) atomicOr(status + b, 2);  // UEPM_K_NONFINITE
     }
+    if constexpr (TC) {
+        if (use_tc) {
+            if (!tc_on) {  // a wait gave up: give the MMAs in flight once more a bounded wait
+                tc_wait(&s_bar[0], (tc_phase & 1u) ^ 1u);
+                tc_wait(&s_bar[1], ((tc_phase >> 1) & 1u) ^ 1u);
+            }
+            tc::fence_before_sync();
+            __syncthreads();
+            if (warp == 0) {
+                tc::fence_after_sync();
+                tc::tmem_dealloc(tbase, kTcCols);
+            }
+        }
+    }
 }
 
 }  // namespace
@@ -388,9 +631,14 @@ int tridiag_blocked_max_n() { return kBlkNT; }
 
 template <typename S>
 bool launch_tridiag_blocked(S* H, int n, int ld, size_t mstride, typename ST<S>::R* d, typename ST<S>::R* e, S* tq,
-                            int* status, int batch, cudaStream_t s) {
+                            int* status, int batch, cudaStream_t s, bool tensor_cores) {
     if (n < 2 || n > kBlkNT) return false;
-    const size_t smem = BlkSmem<S>::bytes(n);
+    // the tensor-core update with the widest column block whose staging fits
+    int nc = 0;
+    if (tensor_cores && ST<S>::cplx)
+        for (int w : {64, 48, 32})
+            if (!nc && BlkSmem<S>::bytes_tc(n, w) <= 227 * 1024) nc = w;
+    const size_t smem = nc ? BlkSmem<S>::bytes_tc(n, nc) : BlkSmem<S>::bytes(n);
     if (smem > 227 * 1024) return false;
     auto kern = k_tridiag_blocked<S>;
     if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) return false;
@@ -399,13 +647,14 @@ bool launch_tridiag_blocked(S* H, int n, int ld, size_t mstride, typename ST<S>:
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&fit, kern, kBlkNT, smem) != cudaSuccess || fit < 1) fit = 1;
     const int grid = std::min(batch, std::max(1, sms) * fit);
-    kern<<<grid, kBlkNT, smem, s>>>(H, n, ld, mstride, d, e, tq, status, batch);
+    kern<<<grid, kBlkNT, smem, s>>>(H, n, ld, mstride, d, e, tq, status, batch, nc);
     count_launch();
     return true;
 }
 
-template bool launch_tridiag_blocked<float>(float*, int, int, size_t, float*, float*, float*, int*, int, cudaStream_t);
+template bool launch_tridiag_blocked<float>(float*, int, int, size_t, float*, float*, float*, int*, int, cudaStream_t,
+                                           bool);
 template bool launch_tridiag_blocked<cx<float>>(cx<float>*, int, int, size_t, float*, float*, cx<float>*, int*, int,
-                                                cudaStream_t);
+                                                cudaStream_t, bool);
 
 }  // namespace uepm

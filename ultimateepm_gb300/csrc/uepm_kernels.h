@@ -56,11 +56,12 @@ int tridiag_cluster_size(int n, int want);
 template <typename S>
 bool launch_tridiag_cluster(S* H, int n, int ld, size_t mstride, typename ST<S>::R* d, typename ST<S>::R* e, S* tq,
                             int* status, int batch, cudaStream_t s, int want_c);
-// tridiag_blocked.cu: the blocked reduction (false when it cannot run this order).
+// tridiag_blocked.cu: the blocked reduction (false when it cannot run this order); tensor_cores puts
+// the complex trailing updates on tcgen05 (where the operand staging fits shared memory).
 int tridiag_blocked_max_n();
 template <typename S>
 bool launch_tridiag_blocked(S* H, int n, int ld, size_t mstride, typename ST<S>::R* d, typename ST<S>::R* e, S* tq,
-                            int* status, int batch, cudaStream_t s);
+                            int* status, int batch, cudaStream_t s, bool tensor_cores);
 // tridiag_reg.cu: the same reduction for real FP32 matrices with n <= tridiag_reg_max_n(), held in
 // registers (launch_tridiag<float> dispatches to it).
 int  tridiag_reg_max_n();
