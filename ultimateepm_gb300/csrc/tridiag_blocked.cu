@@ -96,10 +96,10 @@ struct BlkSmem {
 // Rows [r0, r0 + ROWS) of the panel in the real K-major form of the tensor-core operands: K index
 // 0..15 Re V_k, 16..31 Im V_k, 32..47 Re W_k, 48..63 Im W_k; element (r, k) at float
 // (k / 4) * ROWS * 4 + (r - r0) * 4 + k % 4, split into TF32 hi (rounded to nearest) and the FP32
-// remainder lo. Rows past n are zero.
+// remainder lo. Rows past n are zero. Written by the worker warps (1..15).
 template <int ROWS>
 __device__ __forceinline__ void tc_stage(const cx<float>* Vp, const cx<float>* Wp, int n, int r0, float* hi, float* lo) {
-    for (int it = threadIdx.x; it < ROWS * 8; it += kBlkNT) {
+    for (int it = threadIdx.x - 32; it < ROWS * 8; it += kBlkNT - 32) {
         const int rl = it % ROWS, gq = it / ROWS;  // consecutive threads: consecutive rows
         const int w = gq >> 2, g = gq & 3, r = r0 + rl;
         const cx<float>* src = (w ? Wp : Vp) + (size_t)(4 * g) * n + r;
@@ -123,80 +123,105 @@ __device__ __forceinline__ void tc_stage(const cx<float>* Vp, const cx<float>* W
     }
 }
 
-// Waits (bounded) for the phase of the given parity; the same answer in every thread of the CTA.
+// Waits (bounded, ~1 s) for the phase of the given parity of the mbarrier at bar.
 __device__ __forceinline__ bool tc_wait(uint64_t* bar, uint32_t parity) {
-    bool            ok = false;
     const long long t0 = clock64();
-    while (!(ok = tc::mbar_try_wait(bar, parity)) && clock64() - t0 < kTcWaitCycles) {
-    }
-    return __syncthreads_and(ok) != 0;
+    while (!tc::mbar_try_wait(bar, parity))
+        if (clock64() - t0 > kTcWaitCycles) return false;
+    return true;
 }
 
 // A tile of the tensor-core update: rows [rb, rb + 128) (stored: [rlo, rhi)), columns [cb, cb + NC)
-// (stored: [clo, chi)), its operand / accumulator buffer.
+// (stored: [clo, chi)); its sequence number (over the kernel) selects the buffer (seq & 1) and the
+// mbarrier phase (seq >> 1).
 struct TcTile {
-    int rb, rlo, rhi, cb, clo, chi, buf;
+    int      rb, rlo, rhi, cb, clo, chi;
+    uint32_t seq;
 };
 
-// One thread issues the tile's 48 MMAs (Re: 8 chunk pairs, Im+ and Im-: 4 each, 3 split products per
-// pair) into TMEM buffer t.buf and commits them to that buffer's mbarrier.
+// The issuer (one thread): waits for the workers' staging of tile t, issues its 48 MMAs (Re: 8 chunk
+// pairs, Im+ and Im-: 4 each, 3 split products per pair) into TMEM buffer seq & 1 and commits them to
+// that buffer's MMA mbarrier. False if the wait gave up (nothing issued).
 template <int NC>
-__device__ __forceinline__ void tc_issue(const TcTile& t, const float* aH, const float* aL, const float* bH0,
-                                         uint32_t tbase, uint64_t* bar) {
+__device__ __forceinline__ bool tc_issue(const TcTile& t, const float* aH, const float* aL, const float* bH0,
+                                         uint32_t tbase, uint64_t* staged, uint64_t* done) {
+    const uint32_t buf = t.seq & 1u;
+    if (!tc_wait(staged + buf, (t.seq >> 1) & 1u)) return false;
     tc::fence_after_sync();
     constexpr uint32_t idesc = tc::idesc_tf32(kTcM, NC);
-    const float*       bH    = bH0 + (size_t)t.buf * 2 * NC * kTcK;
+    const float*       bH    = bH0 + (size_t)buf * 2 * NC * kTcK;
     const float*       bL    = bH + (size_t)NC * kTcK;
-    const uint32_t     sa = tc::smem_addr(aH), sl = tc::smem_addr(aL), ta = tc::smem_addr(bH), tl = tc::smem_addr(bL);
-    // 8-wide K chunks: 0,1 Re V; 2,3 Im V; 4,5 Re W; 6,7 Im W
+    const uint64_t     ah0 = tc::smem_desc(tc::smem_addr(aH), kTcM * 16, 128);
+    const uint64_t     al0 = tc::smem_desc(tc::smem_addr(aL), kTcM * 16, 128);
+    const uint64_t     bh0 = tc::smem_desc(tc::smem_addr(bH), NC * 16, 128);
+    const uint64_t     bl0 = tc::smem_desc(tc::smem_addr(bL), NC * 16, 128);
+    // 8-wide K chunks: 0,1 Re V; 2,3 Im V; 4,5 Re W; 6,7 Im W. A chunk moves the start address
+    // (descriptor bits 0-13, in 16-byte units) by 2 * rows core-matrix rows.
     constexpr int pa[16] = {0, 1, 2, 3, 4, 5, 6, 7, 0, 1, 4, 5, 2, 3, 6, 7};
     constexpr int pb[16] = {4, 5, 6, 7, 0, 1, 2, 3, 6, 7, 2, 3, 4, 5, 0, 1};
 #pragma unroll
     for (int p = 0; p < 16; ++p) {
         const int      acc   = p < 8 ? 0 : p < 12 ? 1 : 2;  // Re, Im+, Im-
-        const uint32_t d     = tbase + 192 * t.buf + 64 * acc;
-        const uint32_t oa    = 2 * pa[p] * kTcM * 16, ob = 2 * pb[p] * NC * 16;
-        const uint64_t ah    = tc::smem_desc(sa + oa, kTcM * 16, 128);
-        const uint64_t al    = tc::smem_desc(sl + oa, kTcM * 16, 128);
-        const uint64_t bh    = tc::smem_desc(ta + ob, NC * 16, 128);
-        const uint64_t bl    = tc::smem_desc(tl + ob, NC * 16, 128);
+        const uint32_t d     = tbase + 192 * buf + 64 * acc;
+        const uint64_t oa    = (uint64_t)(2 * pa[p] * kTcM), ob = (uint64_t)(2 * pb[p] * NC);
         const uint32_t accum = (p == 0 || p == 8 || p == 12) ? 0u : 1u;  // the first MMA of D overwrites it
-        tc::mma_tf32(d, ah, bh, idesc, accum);
-        tc::mma_tf32(d, ah, bl, idesc, 1u);
-        tc::mma_tf32(d, al, bh, idesc, 1u);
+        tc::mma_tf32(d, ah0 + oa, bh0 + ob, idesc, accum);
+        tc::mma_tf32(d, ah0 + oa, bl0 + ob, idesc, 1u);
+        tc::mma_tf32(d, al0 + oa, bh0 + ob, idesc, 1u);
     }
-    tc::mma_commit(bar + t.buf);
+    tc::mma_commit(done + buf);
+    return true;
 }
 
-// Every thread: its row and 16 columns of tile t from TMEM, A + (-Re, Im+ - Im-) stored (lower
-// triangle, the tile's own rows and columns). False if the wait gave up.
-template <int NC>
-__device__ __forceinline__ bool tc_readback(const TcTile& t, cx<float>* A, int ld, uint32_t tbase, uint64_t* bar,
-                                            uint32_t& phase) {
-    const int  lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int  qd = warp & 3, cg = warp >> 2;  // TMEM lane quarter, 16-column group
-    const int  r = t.rb + 32 * qd + lane, c0 = t.cb + 16 * cg;
-    const bool rok = r >= t.rlo && r < t.rhi && 16 * cg < NC;
-    cx<float>  x[16];
-#pragma unroll
-    for (int j = 0; j < 16; ++j) {
-        const int c = c0 + j;
-        x[j] = (rok && c >= t.clo && c < t.chi && c <= r) ? ldc(A + (size_t)c * ld + r) : cx<float>{0.f, 0.f};
+// A worker warp's share of tile t: its rows (its TMEM lane quarter; warp w has quarter w & 3, and
+// quarter 0 has 3 worker warps, 4, 8 and 12, the others 4) and up to 3 of the tile's 8-column units
+// (u = wi, wi + nw, ...): its elements are loaded (lower triangle, the tile's own rows and columns;
+// zero elsewhere) before the wait for the tile's MMAs, then Re, Im+ and Im- are read from TMEM and
+// A + (-Re, Im+ - Im-) stored. False if the wait gave up.
+constexpr int kTcUnits = 3;  // at most ceil(64 / 8 / 3) units per worker warp
+struct TcShare {
+    int qd, nw, wi;
+    __device__ TcShare() {
+        const int warp = threadIdx.x >> 5;
+        qd = warp & 3;
+        nw = qd ? 4 : 3;
+        wi = (warp >> 2) - (qd ? 0 : 1);
     }
-    const bool ok = tc_wait(bar + t.buf, (phase >> t.buf) & 1u);
-    phase ^= 1u << t.buf;
-    tc::fence_after_sync();
-    if (ok && 16 * cg < NC) {
-        const uint32_t tl = tbase + 192 * t.buf + ((uint32_t)(32 * qd) << 16) + 16 * cg;
-        float          dre[16], dip[16], dim[16];
-        tc::tmem_ld16(tl, dre);
-        tc::tmem_ld16(tl + 64, dip);
-        tc::tmem_ld16(tl + 128, dim);
+};
+template <int NC>
+__device__ __forceinline__ bool tc_readback(const TcTile& t, cx<float>* A, int ld, uint32_t tbase, uint64_t* done) {
+    const TcShare  sh;
+    const int      r   = t.rb + 32 * sh.qd + (threadIdx.x & 31);
+    const bool     rok = r >= t.rlo && r < t.rhi;
+    const uint32_t buf = t.seq & 1u;
+    cx<float>      z[kTcUnits][8];  // the share's elements, in flight during the wait
 #pragma unroll
-        for (int j = 0; j < 16; ++j) {
-            const int c = c0 + j;
-            if (rok && c >= t.clo && c < t.chi && c <= r)
-                stc(A + (size_t)c * ld + r, cx<float>{x[j].x - dre[j], (r == c) ? 0.f : x[j].y + dip[j] - dim[j]});
+    for (int k = 0; k < kTcUnits; ++k) {
+        const int u = sh.wi + k * sh.nw;
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+            const int c = t.cb + 8 * u + j;
+            z[k][j] = (u < NC / 8 && rok && c >= t.clo && c < t.chi && c <= r) ? ldc(A + (size_t)c * ld + r)
+                                                                               : cx<float>{0.f, 0.f};
+        }
+    }
+    bool ok = tc_wait(done + buf, (t.seq >> 1) & 1u);
+    ok      = __all_sync(0xffffffffu, ok);
+    tc::fence_after_sync();
+    if (ok) {
+#pragma unroll
+        for (int k = 0; k < kTcUnits; ++k) {
+            const int u = sh.wi + k * sh.nw;
+            if (u >= NC / 8) break;
+            const uint32_t tl = tbase + 192 * buf + ((uint32_t)(32 * sh.qd) << 16) + 8 * u;
+            float          dre[8], dip[8], dim[8];
+            tc::tmem_ld8x3(tl, tl + 64, tl + 128, dre, dip, dim);
+#pragma unroll
+            for (int j = 0; j < 8; ++j) {
+                const int c = t.cb + 8 * u + j;
+                if (rok && c >= t.clo && c < t.chi && c <= r)
+                    stc(A + (size_t)c * ld + r, cx<float>{z[k][j].x - dre[j], (r == c) ? 0.f : z[k][j].y + dip[j] - dim[j]});
+            }
         }
     }
     tc::fence_before_sync();
@@ -206,43 +231,48 @@ __device__ __forceinline__ bool tc_readback(const TcTile& t, cx<float>* A, int l
 // A22 -= V W^H + W V^H on the tensor cores, lower triangle of rows / columns q0..n-1. Row blocks of
 // 128 and column blocks of NC are laid from the end (n rounded up to 8) towards q0; a block clamped
 // at q0 (rounded down to 8) overlaps its neighbour and stores only the rows / columns that are its
-// own. Tiles are pipelined: tile t's MMAs are issued, then tile t-1 is read back while they run, and
-// tile t+1 is staged into the other buffer. A new row block (its operand is restaged) first drains
-// the tile in flight. Returns false if a wait gave up (the update is then incomplete).
+// own. Warp-specialised: thread 0 issues each tile's MMAs as soon as the tile is staged; warps 1..15
+// stage tile t into buffer t & 1 (the row operand when the row block changes, after draining the tile
+// in flight), signal it on the staged mbarrier, then read back tile t - 1 while tile t's MMAs run.
+// Every wait is bounded. seq: the kernel's running tile count (buffer and phase parity). Returns
+// false if a wait gave up (the update is then incomplete).
 template <int NC>
 __device__ bool tc_trailing_update(cx<float>* A, int n, int ld, int q0, const cx<float>* Vp, const cx<float>* Wp,
-                                   float* stage, uint32_t tbase, uint64_t* bar, uint32_t& phase) {
-    float*    aH = stage;
-    float*    aL = aH + (size_t)kTcM * kTcK;
-    float*    bH0 = aL + (size_t)kTcM * kTcK;  // buffer b: hi at bH0 + b * 2 NC K, lo NC K after it
-    const int base8 = q0 & ~7, n8 = (n + 7) & ~7;
-    bool      ok = true, pending = false;
-    TcTile    prev{};
-    int       buf = 0;
-    for (int rhi = n, rbe = n8; rhi > q0 && ok;) {
+                                   float* stage, uint32_t tbase, uint64_t* staged, uint64_t* done, uint32_t& seq) {
+    float*         aH = stage;
+    float*         aL = aH + (size_t)kTcM * kTcK;
+    float*         bH0 = aL + (size_t)kTcM * kTcK;  // buffer b: hi at bH0 + b * 2 NC K, lo NC K after it
+    const int      base8 = q0 & ~7, n8 = (n + 7) & ~7;
+    const bool     issuer = threadIdx.x == 0, worker = threadIdx.x >= 32;
+    bool           ok = true, pending = false;
+    TcTile         prev{};
+    for (int rhi = n, rbe = n8; rhi > q0;) {
         const int rb = max(rbe - kTcM, base8), rlo = max(rb, q0);
         bool      first = true;
-        for (int chi = n, cbe = n8; chi > q0 && ok;) {
+        for (int chi = n, cbe = n8; chi > q0;) {
             const int cb = max(cbe - NC, base8), clo = max(cb, q0);
             if (clo < rhi) {  // the tile holds elements on or below the diagonal
-                if (first && pending) {  // the row operand is about to change: drain
-                    ok      = tc_readback<NC>(prev, A, ld, tbase, bar, phase);
-                    pending = false;
-                    if (!ok) break;
-                    __syncthreads();
+                const TcTile t{rb, rlo, rhi, cb, clo, chi, seq++};
+                if (worker) {
+                    if (first) {
+                        if (pending) {  // the row operand is about to change: drain the tile in flight
+                            ok      = tc_readback<NC>(prev, A, ld, tbase, done) && ok;
+                            pending = false;
+                        }
+                        tc_stage<kTcM>(Vp, Wp, n, rb, aH, aL);
+                    }
+                    float* bh = bH0 + (size_t)(t.seq & 1u) * 2 * NC * kTcK;
+                    tc_stage<NC>(Vp, Wp, n, cb, bh, bh + (size_t)NC * kTcK);
+                    tc::fence_async_smem();
+                    tc::fence_before_sync();
+                    tc::mbar_arrive(staged + (t.seq & 1u));
+                    if (pending) ok = tc_readback<NC>(prev, A, ld, tbase, done) && ok;
+                    prev    = t;
+                    pending = true;
+                } else if (issuer) {
+                    ok = tc_issue<NC>(t, aH, aL, bH0, tbase, staged, done) && ok;
                 }
-                const TcTile t{rb, rlo, rhi, cb, clo, chi, buf};
-                if (first) tc_stage<kTcM>(Vp, Wp, n, rb, aH, aL);
                 first = false;
-                tc_stage<NC>(Vp, Wp, n, cb, bH0 + (size_t)buf * 2 * NC * kTcK, bH0 + (size_t)buf * 2 * NC * kTcK + NC * kTcK);
-                tc::fence_async_smem();
-                tc::fence_before_sync();
-                __syncthreads();
-                if (threadIdx.x == 0) tc_issue<NC>(t, aH, aL, bH0, tbase, bar);
-                if (pending) ok = tc_readback<NC>(prev, A, ld, tbase, bar, phase);
-                prev    = t;
-                pending = true;
-                buf ^= 1;
             }
             chi = clo;
             cbe = cb;
@@ -250,12 +280,8 @@ __device__ bool tc_trailing_update(cx<float>* A, int n, int ld, int q0, const cx
         rhi = rlo;
         rbe = rb;
     }
-    if (pending) {
-        const bool ok2 = tc_readback<NC>(prev, A, ld, tbase, bar, phase);
-        ok             = ok && ok2;
-    }
-    __syncthreads();
-    return ok;
+    if (worker && pending) ok = tc_readback<NC>(prev, A, ld, tbase, done) && ok;
+    return __syncthreads_and(ok) != 0;
 }
 
 template <typename S>
@@ -272,8 +298,9 @@ __global__ void __launch_bounds__(kBlkNT, 1)
     S* tdot = v + (n + 32);                             // t1 (W^H v) then t2 (V^H v), NB each
     R* red  = reinterpret_cast<R*>(tdot + 2 * kBlkNB);  // 4 x NW
     __shared__ S s_c0;
-    __shared__ uint64_t s_bar[2];  // tensor-core completion, per operand / accumulator buffer
-    __shared__ uint32_t s_tmem;    // TMEM base address
+    __shared__ uint64_t s_staged[2];  // tensor-core update: tile staged (worker warps -> issuer), per buffer
+    __shared__ uint64_t s_done[2];    // its MMAs complete (tcgen05.commit -> worker warps), per buffer
+    __shared__ uint32_t s_tmem;       // TMEM base address
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     // With an even order every column starts at an even element, so row pairs from an even row are
     // 16-byte (8-byte for real) aligned: the product's tiles then start at o rounded down to even.
@@ -282,12 +309,14 @@ __global__ void __launch_bounds__(kBlkNT, 1)
     // accumulators, an mbarrier per buffer for its MMAs
     constexpr bool TC = ST<S>::cplx;
     bool           tc_on = TC && use_tc != 0;
-    uint32_t       tc_phase = 0, tbase = 0;  // bit b: parity of buffer b's next phase
+    uint32_t       tc_seq = 0, tbase = 0;  // tiles so far (buffer and mbarrier phase parity)
     if constexpr (TC) {
         if (tc_on) {
             if (tid == 0) {
-                tc::mbar_init(&s_bar[0], 1);
-                tc::mbar_init(&s_bar[1], 1);
+                tc::mbar_init(&s_staged[0], kBlkNT - 32);
+                tc::mbar_init(&s_staged[1], kBlkNT - 32);
+                tc::mbar_init(&s_done[0], 1);
+                tc::mbar_init(&s_done[1], 1);
                 asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
             }
             if (warp == 0) {
@@ -547,9 +576,10 @@ __global__ void __launch_bounds__(kBlkNT, 1)
                 if (tc_on && mt >= kTcMinRows) {
                     simt = false;
                     float* stage = reinterpret_cast<float*>(yp);
-                    const bool ok = use_tc == 64   ? tc_trailing_update<64>(A, n, ld, q0, Vp, Wp, stage, tbase, s_bar, tc_phase)
-                                    : use_tc == 48 ? tc_trailing_update<48>(A, n, ld, q0, Vp, Wp, stage, tbase, s_bar, tc_phase)
-                                                   : tc_trailing_update<32>(A, n, ld, q0, Vp, Wp, stage, tbase, s_bar, tc_phase);
+                    const bool ok =
+                        use_tc == 64   ? tc_trailing_update<64>(A, n, ld, q0, Vp, Wp, stage, tbase, s_staged, s_done, tc_seq)
+                        : use_tc == 48 ? tc_trailing_update<48>(A, n, ld, q0, Vp, Wp, stage, tbase, s_staged, s_done, tc_seq)
+                                       : tc_trailing_update<32>(A, n, ld, q0, Vp, Wp, stage, tbase, s_staged, s_done, tc_seq);
                     if (!ok) {
                         // a wait gave up: this matrix is incomplete, and the CTA keeps to the SIMT update
                         if (tid == 0 && status) atomicOr(status + b, 1);  // UEPM_K_NOCONVERGE
@@ -611,9 +641,9 @@ __global__ void __launch_bounds__(kBlkNT, 1)
     }
     if constexpr (TC) {
         if (use_tc) {
-            if (!tc_on) {  // a wait gave up: give the MMAs in flight once more a bounded wait
-                tc_wait(&s_bar[0], (tc_phase & 1u) ^ 1u);
-                tc_wait(&s_bar[1], ((tc_phase >> 1) & 1u) ^ 1u);
+            if (!tc_on && tid == 0 && tc_seq > 0) {  // a wait gave up: the last tiles' MMAs get one more bounded wait
+                tc_wait(&s_done[(tc_seq - 1) & 1u], ((tc_seq - 1) >> 1) & 1u);
+                if (tc_seq > 1) tc_wait(&s_done[tc_seq & 1u], ((tc_seq - 2) >> 1) & 1u);
             }
             tc::fence_before_sync();
             __syncthreads();
