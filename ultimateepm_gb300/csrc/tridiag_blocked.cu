@@ -44,8 +44,10 @@ constexpr int kBlkNB = 16;   // panel width
 // Tensor-core trailing update (complex matrices): tiles of 128 rows x NC columns (NC = 64, 48 or
 // 32, the widest whose operand staging fits shared memory) of the trailing matrix, D = P_rows
 // Q_cols^T in the real form with K = 64 (Re V, Im V, Re W, Im W of the panel's 16 reflectors), each
-// operand split into TF32 hi + lo parts (hi hi + hi lo + lo hi: FP32-level products), accumulated in
-// TMEM. The column operand and the accumulators are double-buffered, so that the MMAs of one tile run
+// operand split into TF32 hi + lo parts, both rounded to nearest, and all four products taken
+// (about 2^-23 relative per product, the FP32 pipe's level: the spin-orbit matrices' Kramers pairs
+// need it; hi hi + hi lo + lo hi with an unrounded lo left one pair in a few thousand split in the
+// FP32 tridiagonal), accumulated in TMEM. The column operand and the accumulators are double-buffered, so that the MMAs of one tile run
 // while the previous tile is read back and the next one staged.
 constexpr int      kTcM       = 128;
 constexpr int      kTcK       = 4 * kBlkNB;
@@ -95,8 +97,9 @@ struct BlkSmem {
 
 // Rows [r0, r0 + ROWS) of the panel in the real K-major form of the tensor-core operands: K index
 // 0..15 Re V_k, 16..31 Im V_k, 32..47 Re W_k, 48..63 Im W_k; element (r, k) at float
-// (k / 4) * ROWS * 4 + (r - r0) * 4 + k % 4, split into TF32 hi (rounded to nearest) and the FP32
-// remainder lo. Rows past n are zero. Written by the worker warps (1..15).
+// (k / 4) * ROWS * 4 + (r - r0) * 4 + k % 4, split into TF32 hi (rounded to nearest) and the
+// remainder rounded to TF32 lo (x - hi - lo is below 2^-24 |x|). Rows past n are zero. Written by
+// the worker warps (1..15).
 template <int ROWS>
 __device__ __forceinline__ void tc_stage(const cx<float>* Vp, const cx<float>* Wp, int n, int r0, float* hi, float* lo) {
     for (int it = threadIdx.x - 32; it < ROWS * 8; it += kBlkNT - 32) {
@@ -113,11 +116,11 @@ __device__ __forceinline__ void tc_stage(const cx<float>* Vp, const cx<float>* W
         const int gre = w * 8 + g, gim = gre + 4;  // 4-wide K groups of the Re and Im parts
         float4    h, l;
         h.x = tc::to_tf32(re[0]); h.y = tc::to_tf32(re[1]); h.z = tc::to_tf32(re[2]); h.w = tc::to_tf32(re[3]);
-        l   = make_float4(re[0] - h.x, re[1] - h.y, re[2] - h.z, re[3] - h.w);
+        l   = make_float4(tc::to_tf32(re[0] - h.x), tc::to_tf32(re[1] - h.y), tc::to_tf32(re[2] - h.z), tc::to_tf32(re[3] - h.w));
         *reinterpret_cast<float4*>(hi + ((size_t)gre * ROWS + rl) * 4) = h;
         *reinterpret_cast<float4*>(lo + ((size_t)gre * ROWS + rl) * 4) = l;
         h.x = tc::to_tf32(im[0]); h.y = tc::to_tf32(im[1]); h.z = tc::to_tf32(im[2]); h.w = tc::to_tf32(im[3]);
-        l   = make_float4(im[0] - h.x, im[1] - h.y, im[2] - h.z, im[3] - h.w);
+        l   = make_float4(tc::to_tf32(im[0] - h.x), tc::to_tf32(im[1] - h.y), tc::to_tf32(im[2] - h.z), tc::to_tf32(im[3] - h.w));
         *reinterpret_cast<float4*>(hi + ((size_t)gim * ROWS + rl) * 4) = h;
         *reinterpret_cast<float4*>(lo + ((size_t)gim * ROWS + rl) * 4) = l;
     }
@@ -139,8 +142,8 @@ struct TcTile {
     uint32_t seq;
 };
 
-// The issuer (one thread): waits for the workers' staging of tile t, issues its 48 MMAs (Re: 8 chunk
-// pairs, Im+ and Im-: 4 each, 3 split products per pair) into TMEM buffer seq & 1 and commits them to
+// The issuer (one thread): waits for the workers' staging of tile t, issues its 64 MMAs (Re: 8 chunk
+// pairs, Im+ and Im-: 4 each, 4 split products per pair) into TMEM buffer seq & 1 and commits them to
 // that buffer's MMA mbarrier. False if the wait gave up (nothing issued).
 template <int NC>
 __device__ __forceinline__ bool tc_issue(const TcTile& t, const float* aH, const float* aL, const float* bH0,
@@ -168,6 +171,7 @@ __device__ __forceinline__ bool tc_issue(const TcTile& t, const float* aH, const
         tc::mma_tf32(d, ah0 + oa, bh0 + ob, idesc, accum);
         tc::mma_tf32(d, ah0 + oa, bl0 + ob, idesc, 1u);
         tc::mma_tf32(d, al0 + oa, bh0 + ob, idesc, 1u);
+        tc::mma_tf32(d, al0 + oa, bl0 + ob, idesc, 1u);
     }
     tc::mma_commit(done + buf);
     return true;
