@@ -191,9 +191,7 @@ int uepm_measure_peak(int precision, double* tflops);
  *                 beyond the on-chip sizes, n <= 512), 5 the same with every other update deferred
  *                 to the next pass (a read-only pass, then a rank-4 pass: 3 passes per two steps), 6 blocked:
  *                 panels of 16 columns whose updates are applied once per panel, only the lower
- *                 triangle read and written, one matrix per SM (FP32, n <= 512), the complex panel
- *                 updates on the tensor cores (tcgen05, TF32 with hi/lo operand splits: FP32-level
- *                 products), 7 the same blocked reduction with every update on the FP32 pipe;
+ *                 triangle read and written, one matrix per SM (FP32, n <= 512);
  *                 automatic: 1 where it applies, 6 for the FP32 orders 300..512, 5 for the other FP32
  *                 matrices, else 2
  *   ctas_per_sm   CTAs per SM of the global-memory reduction (its L2 working set), 1..8
@@ -208,6 +206,11 @@ int uepm_measure_peak(int precision, double* tflops);
  *                 UEPM_ERR_NOT_CONVERGED (the reference throws "Eigenvalue decomposition failed"
  *                 when Eigen reports NoConvergence, Hamiltonian.cpp:129-133). Not a shape: the
  *                 autotuner keeps the context's value.
+ *   tensor_cores  0 (automatic): the mixed path's complex contractions run on the tensor cores
+ *                 (tcgen05) where they apply: the blocked reduction's panel updates (TF32 with
+ *                 hi/lo operand splits, FP32-level products) and, from order 150, the Rayleigh-Ritz
+ *                 product H X (BF16 integer slices of H and X, exact to double-single level);
+ *                 1: every product on the FP32 pipe (SIMT). Kept by the autotuner.
  * Every choice gives results within the parity tolerances; a given choice is deterministic.
  * uepm_ctx_autotune times candidate shapes on sample_k seeded random first-zone k-points (coordinate
  * descent over the fields, CUDA events on `stream`) and keeps the fastest; results are cached
@@ -220,6 +223,7 @@ typedef struct uepm_tuning {
     int32_t chunk;
     int32_t cluster;
     int32_t max_iter;
+    int32_t tensor_cores;
 } uepm_tuning;
 int uepm_ctx_get_tuning(const uepm_ctx* ctx, uepm_tuning* out);
 int uepm_ctx_set_tuning(uepm_ctx* ctx, const uepm_tuning* t);

@@ -177,7 +177,7 @@ def test_every_tuning_choice_keeps_parity(gpu, oracle, mats, prec, tuning):
 
 def test_set_tuning_rejects_out_of_range_fields(gpu, oracle, mats):
     ctx = api._Context(_mat(mats["Si-CB"]), oracle.generate_basis(8), False, False)
-    for bad in (dict(reduction=8), dict(ctas_per_sm=9), dict(vector_lanes=12), dict(chunk=10), dict(cluster=3)):
+    for bad in (dict(reduction=7), dict(tensor_cores=2), dict(ctas_per_sm=9), dict(vector_lanes=12), dict(chunk=10), dict(cluster=3)):
         assert gpu.uepm_ctx_set_tuning(ctx.h, C.byref(N.UepmTuning(**bad))) == N.UEPM_ERR_OUT_OF_RANGE
     ctx.close()
 

@@ -233,11 +233,11 @@ def test_vectors_at_size_are_orthonormal_eigenvectors(gpu, oracle, mats, precisi
     ctx.close()
 
 
-@pytest.mark.parametrize("reduction", [2, 3, 4, 5, 6, 7])
+@pytest.mark.parametrize("reduction", [2, 3, 4, 5, 6])
 def test_mixed_precision_complex_reductions(gpu, oracle, mats, reduction):
     """Every FP32 reduction kernel on a complex matrix (InP with nonlocal wells, n = 113, which fits
-    shared memory): 2 shared memory, 3 cluster, 4 fused, 5 deferred, 6 blocked with the first
-    panel's trailing update on the tensor cores, 7 blocked with SIMT updates only."""
+    shared memory): 2 shared memory, 3 cluster, 4 fused, 5 deferred, 6 blocked (its first panel's
+    trailing update on the tensor cores)."""
     key, shells, nl, soc, _ = _case("inp_nl_113")
     G = oracle.generate_basis(shells)
     ks = _kset(oracle, 37, 10)
@@ -407,19 +407,20 @@ def test_real_and_complex_kernels_agree(gpu, oracle, mats):
         assert np.abs(Er - Ec).max() <= tol
 
 
-@pytest.mark.parametrize("reduction", [6, 7])
+@pytest.mark.parametrize("tensor_cores", [0, 1])
 @pytest.mark.parametrize("case,nb", [("ge_nl_soc_181", 16), ("gaas_nl_soc_89", 16), ("si_d_nonlocal_137", 12),
                                      ("alas_local_169", 16)])
-def test_blocked_reduction_against_the_oracle(gpu, oracle, mats, case, nb, reduction):
-    """The blocked reduction (panels of 16 columns, lower triangle only; tuning 6 with the complex
-    trailing updates on the tensor cores, tcgen05 TF32 with hi/lo splits, 7 with SIMT updates) on
-    complex orders 362, 178 and 169 (odd: unaligned row pairs) and the real order 137, mixed
-    precision: eigenvalues against the oracle within 1e-6 eV, Ritz vectors orthonormal."""
+def test_blocked_reduction_against_the_oracle(gpu, oracle, mats, case, nb, tensor_cores):
+    """The blocked reduction (tuning 6: panels of 16 columns, lower triangle only) on complex orders
+    362, 178 and 169 (odd: unaligned row pairs) and the real order 137, mixed precision, with the
+    tensor cores (tensor_cores 0: the complex trailing updates on tcgen05, TF32 with hi/lo splits,
+    and from order 150 the projection H X with BF16 integer slices) and without (1): eigenvalues
+    against the oracle within 1e-6 eV, Ritz vectors orthonormal."""
     key, shells, nl, soc, fcx = _case(case)
     G = oracle.generate_basis(shells)
     ks = _kset(oracle, 41, 6)
     ctx = _ctx(mats[key], G, nl, soc, N.UEPM_PREC_MIXED, force_complex=fcx)
-    N.check(gpu.uepm_ctx_set_tuning(ctx.h, C.byref(N.UepmTuning(reduction=reduction))))
+    N.check(gpu.uepm_ctx_set_tuning(ctx.h, C.byref(N.UepmTuning(reduction=6, tensor_cores=tensor_cores))))
     E, X, _, st = ctx.solve(ks, nb, vectors=True)
     Eo = oracle.band_structure(mats[key], G, ks, nb, nl=nl, soc=soc)["E"]
     assert not st.any()
@@ -428,3 +429,44 @@ def test_blocked_reduction_against_the_oracle(gpu, oracle, mats, case, nb, reduc
     gram = np.einsum("kbi,kci->kbc", X.conj(), X) - np.eye(nb)[None]
     assert np.abs(gram).max() <= 1e-9
     ctx.close()
+
+
+def test_tensor_core_update_keeps_kramers_pairs(gpu, oracle, mats):
+    """A Ge spin-orbit k-point (order 362) whose band-15/16 Kramers pair the tensor-core trailing
+    update once left split in the FP32 tridiagonal (hi hi + hi lo + lo hi with an unrounded lo part:
+    band 16 off by 2.4e-4 eV), solved with the tensor-core update among seeded neighbours: every band
+    within 1e-6 eV of the oracle."""
+    key, shells, nl, soc, _ = _case("ge_nl_soc_181")
+    G = oracle.generate_basis(shells)
+    k0 = np.array([0.5494544861023094, -0.7040934208086767, -0.04903435918750576])
+    ks = np.vstack([k0, k0 + 1e-3 * np.random.default_rng(7).standard_normal((5, 3))])
+    ctx = _ctx(mats[key], G, nl, soc, N.UEPM_PREC_MIXED)
+    N.check(gpu.uepm_ctx_set_tuning(ctx.h, C.byref(N.UepmTuning(reduction=6))))
+    E, _, _, st = ctx.solve(ks, 16)
+    Eo = oracle.band_structure(mats[key], G, ks, 16, nl=nl, soc=soc)["E"]
+    assert not st.any()
+    err = np.abs(E - Eo).max(axis=0)
+    assert err.max() <= MIXED_TOL, f"per-band max |dE| = {err}"
+    ctx.close()
+
+
+@pytest.mark.parametrize("case,nb", [("ge_nl_soc_181", 16), ("gaas_nl_soc_89", 16), ("gap_soc_89", 12)])
+def test_tensor_core_projection_matches_the_fp32_pipe(gpu, oracle, mats, case, nb):
+    """The Rayleigh-Ritz product H X on the tensor cores (BF16 integer slices of H and X with
+    power-of-two row and vector scales, exact FP32 accumulation, double-single sum of the weights)
+    against the double-single FP32-pipe product, same reduction and vectors (tuning 5, so that only
+    the projection differs): eigenvalues within 1e-9 eV of each other and of the oracle within 1e-6."""
+    key, shells, nl, soc, fcx = _case(case)
+    G = oracle.generate_basis(shells)
+    ks = _kset(oracle, 43, 8)
+    out = []
+    for tc in (0, 1):
+        ctx = _ctx(mats[key], G, nl, soc, N.UEPM_PREC_MIXED, force_complex=fcx)
+        N.check(gpu.uepm_ctx_set_tuning(ctx.h, C.byref(N.UepmTuning(reduction=5, tensor_cores=tc))))
+        E, _, _, st = ctx.solve(ks, nb)
+        assert not st.any()
+        out.append(E)
+        ctx.close()
+    Eo = oracle.band_structure(mats[key], G, ks, nb, nl=nl, soc=soc)["E"]
+    assert np.abs(out[0] - out[1]).max() <= 1e-9, f"tensor cores vs FP32 pipe: {np.abs(out[0] - out[1]).max():.3e} eV"
+    assert np.abs(out[0] - Eo).max() <= MIXED_TOL

@@ -32,7 +32,7 @@ PER_FILE = {"assemble.cu": ["--fmad=false"]}
 # x86 and Arm (gcc contracts a * b + c into one fma by default where the target has one).
 CXX_FLAGS = ["-O3", "-std=c++17", "-fPIC", "-Wall", "-ffp-contract=off", "-I" + INCLUDE, "-I" + CSRC]
 
-CU_SOURCES = ["assemble.cu", "tridiag.cu", "tridiag_reg.cu", "tridiag_cluster.cu", "tridiag_blocked.cu", "tridiag_eig.cu", "backtransform.cu", "refine.cu", "capi.cu", "batch.cu", "server.cu", "star.cu", "peak.cu",
+CU_SOURCES = ["assemble.cu", "tridiag.cu", "tridiag_reg.cu", "tridiag_cluster.cu", "tridiag_blocked.cu", "tridiag_eig.cu", "backtransform.cu", "refine.cu", "refine_tc.cu", "capi.cu", "batch.cu", "server.cu", "star.cu", "peak.cu",
               "noalloc.cu", "dielectric.cu"]
 CXX_SOURCES = ["host.cpp"]
 

@@ -51,12 +51,13 @@ TuneKey tune_key(const uepm_ctx* ctx, int nb, uint32_t want) {
 }
 
 bool valid_tuning(const uepm_ctx* ctx, const uepm_tuning& t) {
-    if (t.reduction < 0 || t.reduction > 7) return false;
+    if (t.reduction < 0 || t.reduction > 6) return false;
     if (t.ctas_per_sm < 0 || t.ctas_per_sm > 8) return false;
     if (t.cluster != 0 && t.cluster != 2 && t.cluster != 4 && t.cluster != 8 && t.cluster != 16) return false;
     if (t.vector_lanes != 0 && t.vector_lanes != 8 && t.vector_lanes != 16 && t.vector_lanes != 32) return false;
     if (t.chunk != 0 && (t.chunk < 64 || t.chunk > 32768)) return false;
     if (t.max_iter < 0 || t.max_iter > 1000) return false;
+    if (t.tensor_cores < 0 || t.tensor_cores > 1) return false;
     (void)ctx;
     return true;
 }
@@ -177,6 +178,7 @@ int uepm_ctx_autotune(uepm_ctx* ctx, int nb, uint32_t want, size_t sample_k, voi
 
     uepm_tuning best = uepm_tuning{};
     best.max_iter    = saved.max_iter;  // not a shape: kept as the caller set it
+    best.tensor_cores = saved.tensor_cores;
     ctx->tune        = best;
     double best_ms   = 0;
     rc               = timed(&best_ms);

@@ -300,7 +300,7 @@ void run_chunk(uepm_ctx* ctx, const Layout& L, char* ws, const double* kk, int c
                                     ctx->tune.cluster);
         } else {
             launch_tridiag<S32>(H32, n, n, mstride, d, e, tq, st, c, s, ctx->tune.reduction, ctx->tune.ctas_per_sm,
-                                ctx->tune.cluster);
+                                ctx->tune.cluster, ctx->tune.tensor_cores == 0);
         }
     }
     {
@@ -320,7 +320,7 @@ void run_chunk(uepm_ctx* ctx, const Layout& L, char* ws, const double* kk, int c
         ProfScope p(ctx, s, KK_REFINE_PROJECT);
         const SparseV sv{ctx->sparse_local, ctx->ell_w,  ctx->d_ell_col, ctx->d_ell_re,
                          ctx->d_ell_im,       ctx->d_Vloc, rows,            ctx->N};
-        launch_refine_project<S>(Hs, n, n, mstride, X32, m, rw, small, c, s, sv);
+        launch_refine_project<S>(Hs, n, n, mstride, X32, m, rw, small, c, s, sv, st, ctx->tune.tensor_cores == 0);
     }
     S* W = small + (size_t)2 * m * m;  // W block of the first matrix; matrices are refine_small_elems apart
     {

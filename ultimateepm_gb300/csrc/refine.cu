@@ -96,7 +96,7 @@ __device__ __forceinline__ void proj_accumulate(dsacc (&yr)[kProjVB], dsacc (&yi
     }
 }
 
-template <typename S, bool STAGED, bool SPARSE>
+template <typename S, bool STAGED, bool SPARSE, bool YDONE = false>
 __global__ void __launch_bounds__(kProjNT) k_refine_project(const typename Split<S>::type* __restrict__ H, int n, int ld,
                                                             size_t mstride, const cx<float>* __restrict__ X32, int m,
                                                             void* __restrict__ work, S* __restrict__ small, int batch,
@@ -130,7 +130,7 @@ __global__ void __launch_bounds__(kProjNT) k_refine_project(const typename Split
     YT*       Y    = reinterpret_cast<YT*>(work) + (size_t)b * refine_work_elems(n, m) * sizeof(S) / sizeof(YT);  // [r][mp]
     const SE* A    = H + (size_t)b * mstride;
     const int nblk = mp / kProjVB;
-    for (int item = tid; item < nblk * n; item += kProjNT) {
+    for (int item = tid; item < (YDONE ? 0 : nblk * n); item += kProjNT) {  // YDONE: Y came from the tensor cores
         const int r = item / nblk, jb = item - r * nblk, j0 = jb * kProjVB;
         dsacc     yr[kProjVB], yi[kProjVB];
 #pragma unroll
@@ -652,25 +652,37 @@ __global__ void k_refine_vectors(int n, int m, int nb, const cx<float>* __restri
     }
 }
 
-template <typename S, bool SPARSE>
+template <typename S, bool SPARSE, bool YDONE>
 static void refine_project_t(const typename Split<S>::type* H, int n, int ld, size_t mstride, const cx<float>* X32, int m,
                              S* work, S* small, int batch, cudaStream_t s, const SparseV& sv) {
     const size_t stage = proj_stage_bytes<S>(n, m);
     if (stage <= kProjStageBytes) {
-        auto kern = k_refine_project<S, true, SPARSE>;
+        auto kern = k_refine_project<S, true, SPARSE, YDONE>;
         if (stage > 48 * 1024) cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)stage);
         kern<<<batch, kProjNT, stage, s>>>(H, n, ld, mstride, X32, m, work, small, batch, sv);
     } else {
-        k_refine_project<S, false, SPARSE><<<batch, kProjNT, 0, s>>>(H, n, ld, mstride, X32, m, work, small, batch, sv);
+        k_refine_project<S, false, SPARSE, YDONE><<<batch, kProjNT, 0, s>>>(H, n, ld, mstride, X32, m, work, small, batch, sv);
     }
     count_launch();
 }
 
 template <typename S>
 void launch_refine_project(const typename Split<S>::type* H, int n, int ld, size_t mstride, const cx<float>* X32, int m,
-                           S* work, S* small, int batch, cudaStream_t s, const SparseV& sv) {
-    if (sv.on) refine_project_t<S, true>(H, n, ld, mstride, X32, m, work, small, batch, s, sv);
-    else refine_project_t<S, false>(H, n, ld, mstride, X32, m, work, small, batch, s, sv);
+                           S* work, S* small, int batch, cudaStream_t s, const SparseV& sv, int* status, bool tensor_cores) {
+    if (sv.on) {
+        refine_project_t<S, true, false>(H, n, ld, mstride, X32, m, work, small, batch, s, sv);
+        return;
+    }
+    if constexpr (!std::is_same<S, double>::value) {
+        // complex dense H from order kRefineTcMinN: Y = H X on the tensor cores (Ozaki splitting,
+        // refine_tc.cu), then S and A here
+        if (tensor_cores && n >= kRefineTcMinN &&
+            launch_refine_y_tc(H, n, ld, mstride, X32, m, proj_mp<S>(m), work, refine_work_elems(n, m), status, batch, s)) {
+            refine_project_t<S, false, true>(H, n, ld, mstride, X32, m, work, small, batch, s, sv);
+            return;
+        }
+    }
+    refine_project_t<S, false, false>(H, n, ld, mstride, X32, m, work, small, batch, s, sv);
 }
 
 template <typename S>
@@ -692,7 +704,7 @@ void launch_refine_vectors(int n, int m, int nb, const cx<float>* X32, const S* 
 
 #define UEPM_RF_INST(S)                                                                                             \
     template void launch_refine_project<S>(const typename Split<S>::type*, int, int, size_t, const cx<float>*, int, S*, S*, \
-                                           int, cudaStream_t, const SparseV&);                                    \
+                                           int, cudaStream_t, const SparseV&, int*, bool);                        \
     template void launch_small_eigh<S>(S*, int, int, double*, S*, int*, int, cudaStream_t, int);                   \
     template void launch_refine_vectors<S>(int, int, int, const cx<float>*, const S*, cx<double>*, double*, const DevParams&, \
                                            const double*, const int*, int, cudaStream_t);

@@ -769,7 +769,7 @@ static void tridiag_pick(S* H, int n, int ld, size_t mstride, typename ST<S>::R*
 
 template <typename S>
 void launch_tridiag(S* H, int n, int ld, size_t mstride, typename ST<S>::R* d, typename ST<S>::R* e, S* tq, int* status,
-                    int batch, cudaStream_t s, int variant, int ctas_per_sm, int cluster) {
+                    int batch, cudaStream_t s, int variant, int ctas_per_sm, int cluster, bool tensor_cores) {
     if constexpr (std::is_same<S, float>::value) {
         if ((variant == 0 || variant == 1) && n <= tridiag_reg_max_n()) {
             launch_tridiag_reg(H, n, ld, mstride, d, e, tq, status, batch, s);
@@ -788,8 +788,8 @@ void launch_tridiag(S* H, int n, int ld, size_t mstride, typename ST<S>::R* d, t
         // the blocked kernel (6) is automatic from order 300 (2000 k, mixed: Ge SOC n = 362 81.3 ->
         // 47.5 ms, Si SOC n = 338 67.1 -> 41.7, GaP SOC n = 458 198.3 -> 81.8); below, the deferred
         // kernel stays ahead (GaAs SOC n = 178 9.5 against 12.6 ms, InAs n = 229 equal)
-        if ((variant == 6 || variant == 7 || (variant == 0 && n >= 300)) &&
-            launch_tridiag_blocked<S>(H, n, ld, mstride, d, e, tq, status, batch, s, variant != 7))
+        if ((variant == 6 || (variant == 0 && n >= 300)) &&
+            launch_tridiag_blocked<S>(H, n, ld, mstride, d, e, tq, status, batch, s, tensor_cores))
             return;
         // automatic: the deferred kernel for every FP32 order beyond the register kernel, also where
         // the matrix would fit shared memory (2000 k: Ge nonlocal n = 181 real 5.85 ms against 14.3
@@ -821,9 +821,9 @@ void launch_tridiag(S* H, int n, int ld, size_t mstride, typename ST<S>::R* d, t
     else tridiag_pick<S, 16>(H, n, ld, mstride, d, e, tq, status, batch, s, ctas_per_sm);
 }
 
-template void launch_tridiag<cx<double>>(cx<double>*, int, int, size_t, double*, double*, cx<double>*, int*, int, cudaStream_t, int, int, int);
-template void launch_tridiag<cx<float>>(cx<float>*, int, int, size_t, float*, float*, cx<float>*, int*, int, cudaStream_t, int, int, int);
-template void launch_tridiag<double>(double*, int, int, size_t, double*, double*, double*, int*, int, cudaStream_t, int, int, int);
-template void launch_tridiag<float>(float*, int, int, size_t, float*, float*, float*, int*, int, cudaStream_t, int, int, int);
+template void launch_tridiag<cx<double>>(cx<double>*, int, int, size_t, double*, double*, cx<double>*, int*, int, cudaStream_t, int, int, int, bool);
+template void launch_tridiag<cx<float>>(cx<float>*, int, int, size_t, float*, float*, cx<float>*, int*, int, cudaStream_t, int, int, int, bool);
+template void launch_tridiag<double>(double*, int, int, size_t, double*, double*, double*, int*, int, cudaStream_t, int, int, int, bool);
+template void launch_tridiag<float>(float*, int, int, size_t, float*, float*, float*, int*, int, cudaStream_t, int, int, int, bool);
 
 }  // namespace uepm

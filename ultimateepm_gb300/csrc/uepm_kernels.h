@@ -48,7 +48,8 @@ void launch_assemble(const DevParams& P, const cx<double>* Vloc, const double2* 
 // variant 3.
 template <typename S>
 void launch_tridiag(S* H, int n, int ld, size_t mstride, typename ST<S>::R* d, typename ST<S>::R* e, S* tq, int* status,
-                    int batch, cudaStream_t s, int variant = 0, int ctas_per_sm = 0, int cluster = 0);
+                    int batch, cudaStream_t s, int variant = 0, int ctas_per_sm = 0, int cluster = 0,
+                    bool tensor_cores = true);
 // tridiag_cluster.cu: cluster size for order n (want = 0: automatic; 0 returned when it cannot fit)
 // and the launch (false when the cluster kernel cannot run this case).
 template <typename S>
@@ -117,9 +118,17 @@ struct SparseV {
     const double*     rows;  // [batch][N][ROW_STRIDE], for the kinetic term
     int               N;
 };
+// tensor_cores: a complex dense H of order >= kRefineTcMinN takes Y = H X on the tensor cores
+// (refine_tc.cu); status gets UEPM_K_NOCONVERGE there if a bounded wait gives up.
+constexpr int kRefineTcMinN = 150;
 template <typename S>
 void launch_refine_project(const typename Split<S>::type* H, int n, int ld, size_t mstride, const cx<float>* X32, int m,
-                           S* work, S* small, int batch, cudaStream_t s, const SparseV& sv);
+                           S* work, S* small, int batch, cudaStream_t s, const SparseV& sv, int* status = nullptr,
+                           bool tensor_cores = true);
+// refine_tc.cu: Y (double-single, [r][mp] per matrix, ystride float4 apart) = H X for complex H on
+// the tensor cores; false when it does not apply (nothing launched).
+bool launch_refine_y_tc(const ds4* H, int n, int ld, size_t mstride, const cx<float>* X32, int m, int mp, void* work,
+                        size_t ystride, int* status, int batch, cudaStream_t s);
 template <typename S>
 void launch_small_eigh(S* small, int m, int nb, double* Eout, S* W, int* status, int batch, cudaStream_t s, int cap = 0);
 template <typename S>
