@@ -179,3 +179,61 @@ def test_band_structure_over_a_symmetric_mesh(gpu, oracle):
     dE, dg = m.distribute_on_device(Eiw, giw, pos[m.src])
     torch.cuda.synchronize()
     assert np.array_equal(dE.cpu().numpy(), E) and np.array_equal(dg.cpu().numpy(), g)
+
+
+def _small_mesh(tmp_path, seed=3):
+    """A mesh file (ASCII MSH 4.1, 8 nodes, 5 tetrahedra of a cube) read into a MeshBZ, with
+    synthetic band energies (4 valence bands <= 0.1 eV at the first vertex, 3 conduction) and
+    gradients on its vertices."""
+    cube = np.array([[0, 0, 0], [1, 0, 0], [1, 1, 0], [0, 1, 0], [0, 0, 1], [1, 0, 1], [1, 1, 1], [0, 1, 1]], float) * 0.3
+    tets = np.array([[1, 2, 4, 5], [2, 3, 4, 7], [2, 5, 6, 7], [4, 5, 7, 8], [2, 4, 5, 7]])
+    src = tmp_path / "cube.msh"
+    with open(src, "w") as f:
+        f.write("$MeshFormat\n4.1 0 8\n$EndMeshFormat\n$Nodes\n1 8 1 8\n3 1 0 8\n")
+        f.write("".join(f"{i}\n" for i in range(1, 9)))
+        f.write("".join(f"{x} {y} {z}\n" for x, y, z in cube))
+        f.write("$EndNodes\n$Elements\n1 5 1 5\n3 1 4 5\n")
+        f.write("".join(f"{e + 1} " + " ".join(str(v) for v in t) + "\n" for e, t in enumerate(tets)))
+        f.write("$EndElements\n")
+    m = MeshBZ(_si()).read_mesh_geometry_from_msh_file(str(src))
+    rng = np.random.default_rng(seed)
+    E = np.concatenate([np.sort(rng.uniform(-12.0, 0.0, (8, 4)), axis=1), 1.0 + np.sort(rng.uniform(0.0, 5.0, (8, 3)), axis=1)],
+                       axis=1)
+    E[0, 3] = 0.0  # the valence maximum at the first vertex, as after AdjustValues
+    m.energies, m.gradients = E, rng.standard_normal((8, 7, 3)) * 1e-29
+    return m, src
+
+
+def test_gmsh_band_views_follow_the_reference_order(tmp_path):
+    """MeshBZ::export_selected_bands_to_gmsh (bz_mesh.cpp:1426-1549): the mesh once, then band_<i>
+    views, valence from the highest down (or from the lowest up), then conduction; gradients as
+    3-component views after their band; values read back exactly; a second export appends views
+    without rewriting the mesh."""
+    from ultimateepm_gb300.mesh import read_msh_node_data, read_msh_tetrahedra
+
+    m, src = _small_mesh(tmp_path)
+    assert m.band_ranges() == ((0, 4), (4, 3))
+    out = tmp_path / "bands.msh"
+    order = m.export_selected_bands_to_gmsh(str(out), 2, 2, highest_valence_as_band0=True, write_gradients=True)
+    assert order == [3, 2, 4, 5]
+    tags, xyz = read_msh_nodes(str(out))
+    t0, x0 = read_msh_nodes(str(src))
+    assert (tags == t0).all() and np.array_equal(xyz, x0)
+    assert np.array_equal(read_msh_tetrahedra(str(out)), read_msh_tetrahedra(str(src)))
+    views = read_msh_node_data(str(out))
+    assert [(v[0], v[1]) for v in views] == [("band_0", 1), ("grad_band_0", 3), ("band_1", 1), ("grad_band_1", 3),
+                                             ("band_2", 1), ("grad_band_2", 3), ("band_3", 1), ("grad_band_3", 3)]
+    for q, g in enumerate(order):
+        assert np.array_equal(views[2 * q][3][:, 0], m.energies[:, g])
+        assert np.array_equal(views[2 * q + 1][3], m.gradients[:, g, :])
+    order2 = m.export_selected_bands_to_gmsh(str(out), 3, 0, highest_valence_as_band0=False)
+    assert order2 == [0, 1, 2]
+    text = open(out).read()
+    assert text.count("$Nodes") == 1 and text.count("$NodeData") == 11
+    # read back as the reference's loader does: bands in file order, valence by the first value
+    back = MeshBZ(_si()).read_mesh_geometry_from_msh_file(str(out))
+    Eb, gb = back.read_mesh_bands_from_msh_file(str(out))
+    assert Eb.shape == (8, 7) and gb is None  # 7 bands, 4 gradient views
+    assert np.array_equal(Eb[:, :4], m.energies[:, order])
+    with pytest.raises(IndexError):
+        m.export_selected_bands_to_gmsh(str(tmp_path / "x.msh"), 0, 4)

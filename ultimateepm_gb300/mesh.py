@@ -14,6 +14,13 @@ Mirrors MeshBZ (src/BZ_MESH/bz_mesh.cpp) for the band-structure part:
                                      energies copied, gradients taken through the signed permutation
                                      apply_same_symmetry_operation finds (:1312-1414): on the host, or
                                      as one device gather (uepm_star_expand_device) after a device solve
+  export_selected_bands_to_gmsh      the band views (:1426-1549): the mesh once, then one node-data
+                                     view per exported band ("band_<i>"), and per gradient
+                                     ("grad_band_<i>", 3 components), valence bands first (highest as
+                                     band 0 on request), then conduction bands; written as ASCII MSH
+                                     4.1 (the reference lets gmsh write binary; gmsh reads both)
+  read_mesh_bands_from_msh_file      the views back, classified as the reference does (:330-392): a
+                                     band is valence when its value at the first vertex is <= 0.1 eV
 Energies in eV, gradients in eV m (the reference's units), vertex positions in SI (1/m).
 """
 from __future__ import annotations
@@ -119,6 +126,38 @@ def read_msh_tetrahedra(path: str) -> np.ndarray:
     raise ValueError(f"{path}: no $Elements section")
 
 
+def read_msh_node_data(path: str) -> list[tuple[str, int, np.ndarray, np.ndarray]]:
+    """The $NodeData views of an ASCII MSH file in file order: (name, components, node tags, values
+    [n][components])."""
+    with open(path, "r") as f:
+        lines = f.read().splitlines()
+    out = []
+    i = 0
+    while i < len(lines):
+        if lines[i].strip() != "$NodeData":
+            i += 1
+            continue
+        i += 1
+        ns = int(lines[i]); i += 1
+        strs = [lines[i + q].strip().strip('"') for q in range(ns)]; i += ns
+        nr = int(lines[i]); i += 1 + nr
+        ni = int(lines[i]); i += 1
+        ints = [int(lines[i + q]) for q in range(ni)]; i += ni
+        ncomp, nn = ints[1], ints[2]
+        tags = np.empty(nn, dtype=np.int64)
+        vals = np.empty((nn, ncomp))
+        for q in range(nn):
+            p = lines[i + q].split()
+            tags[q] = int(p[0])
+            vals[q] = [float(x) for x in p[1:1 + ncomp]]
+        i += nn
+        if lines[i].strip() != "$EndNodeData":
+            raise ValueError(f"{path}: malformed $NodeData")
+        out.append((strs[0] if strs else "", ncomp, tags, vals))
+        i += 1
+    return out
+
+
 def tetra_signed_volumes(positions: np.ndarray, tetra: np.ndarray) -> np.ndarray:
     """Tetra::compute_signed_volume (mesh_tetra.cpp:128-132): (1/6) e0 . (e1 x e2) with
     e_j = v_{j+1} - v_0."""
@@ -157,9 +196,13 @@ class MeshBZ:
         self.node_tags = tags
         self.positions = xyz * f
         self.filename = filename
+        self._file_xyz = xyz  # the model's own coordinates, for writing the mesh back
         try:
-            self.set_tetrahedra(read_msh_tetrahedra(filename) - 1)  # vertex = node tag - 1 (bz_mesh.cpp:135-138)
+            raw = read_msh_tetrahedra(filename)
+            self._file_tetra = raw
+            self.set_tetrahedra(raw - 1)  # vertex = node tag - 1 (bz_mesh.cpp:135-138)
         except ValueError:
+            self._file_tetra = np.zeros((0, 4), dtype=np.int64)
             self.tetra = np.zeros((0, 4), dtype=np.int64)
             self.tetra_volumes = np.zeros(0)
         return self
@@ -190,6 +233,98 @@ class MeshBZ:
         x, y, z = k[:, 0], k[:, 1], k[:, 2]
         eps = 1e-12
         return (z >= -eps) & (z <= y + eps) & (y <= x + eps) & (x <= 1.0 + eps) & ((x + y + z) <= 1.5 + eps)
+
+    # ---- band views (gmsh node data) --------------------------------------------------------------
+    def band_ranges(self) -> tuple[tuple[int, int], tuple[int, int]]:
+        """(first index, count) of the valence and of the conduction bands, by the reference's rule
+        (bz_mesh.cpp:365-378): band b is valence when its energy at the first vertex is <= 0.1 eV."""
+        if self.energies is None:
+            raise RuntimeError("no band energies on the mesh")
+        E = np.asarray(self.energies)
+        val = [b for b in range(E.shape[1]) if E[0, b] <= 0.1]
+        con = [b for b in range(E.shape[1]) if E[0, b] > 0.1]
+        return (val[0] if val else -1, len(val)), (con[0] if con else -1, len(con))
+
+    def _write_mesh_msh41(self, f):
+        tags = np.asarray(self.node_tags, dtype=np.int64)
+        xyz = getattr(self, "_file_xyz", None)
+        if xyz is None:
+            xyz = self.positions
+        tet = getattr(self, "_file_tetra", None)
+        if tet is None:
+            tet = self.tetra + 1
+        f.write("$MeshFormat\n4.1 0 8\n$EndMeshFormat\n")
+        f.write(f"$Nodes\n1 {len(tags)} {int(tags.min())} {int(tags.max())}\n3 1 0 {len(tags)}\n")
+        f.write("".join(f"{int(t)}\n" for t in tags))
+        f.write("".join(f"{x!r} {y!r} {z!r}\n" for x, y, z in np.asarray(xyz, dtype=np.float64).tolist()))
+        f.write("$EndNodes\n")
+        f.write(f"$Elements\n1 {len(tet)} 1 {len(tet)}\n3 1 4 {len(tet)}\n")
+        f.write("".join(f"{e + 1} {a} {b} {c} {d}\n" for e, (a, b, c, d) in enumerate(np.asarray(tet).tolist())))
+        f.write("$EndElements\n")
+
+    def _write_view(self, f, name: str, vals: np.ndarray):
+        vals = np.asarray(vals, dtype=np.float64).reshape(len(self.node_tags), -1)
+        f.write(f'$NodeData\n1\n"{name}"\n1\n0\n3\n0\n{vals.shape[1]}\n{len(self.node_tags)}\n')
+        f.write("".join(f"{int(t)} " + " ".join(repr(x) for x in row) + "\n"
+                        for t, row in zip(np.asarray(self.node_tags).tolist(), vals.tolist())))
+        f.write("$EndNodeData\n")
+
+    def export_selected_bands_to_gmsh(self, out_filename: str, nb_valence_to_export: int, nb_conduction_to_export: int,
+                                      highest_valence_as_band0: bool = True, model_name_or_msh_path: str = "",
+                                      write_gradients: bool = False):
+        """MeshBZ::export_selected_bands_to_gmsh (bz_mesh.cpp:1426-1549). The mesh is written only when
+        out_filename does not exist yet; the views are appended. Valence bands: from the highest down
+        when highest_valence_as_band0, else from the lowest up; then the conduction bands in order.
+        Views are named band_<i> (and grad_band_<i>) with i counting the exported bands. Values are
+        written with 17 significant digits (they read back exactly). model_name_or_msh_path is
+        accepted for signature compatibility: the mesh written is the one this object read."""
+        del model_name_or_msh_path
+        if len(self.node_tags) == 0 or self.energies is None or len(self.energies) != len(self.node_tags):
+            raise RuntimeError("Mesh vertices/tags not initialized or inconsistent.")
+        E = np.asarray(self.energies)
+        G = None if self.gradients is None else np.asarray(self.gradients)
+        if write_gradients and G is None:
+            raise RuntimeError("Vertex gradient vector too small for requested band index.")
+        (v0, nv), (c0, nc) = self.band_ranges()
+        order = []
+        if nb_valence_to_export > 0:
+            if highest_valence_as_band0:
+                last = v0 + nv - 1
+                order += list(range(last, last - int(nb_valence_to_export), -1))
+            else:
+                order += list(range(v0, v0 + int(nb_valence_to_export)))
+        for g in range(int(nb_conduction_to_export)):
+            if g >= nc:
+                raise IndexError("conduction band index out of range")  # get_global_band_index throws
+            order.append(c0 + g)
+        for g in order:
+            if g < 0 or g >= E.shape[1]:
+                raise RuntimeError("Vertex band vector too small for requested band index.")
+        write_mesh = not os.path.exists(out_filename)
+        with open(out_filename, "a") as f:
+            if write_mesh:
+                self._write_mesh_msh41(f)
+            for idx, g in enumerate(order):
+                self._write_view(f, f"band_{idx}", E[:, g])
+                if write_gradients:
+                    self._write_view(f, f"grad_band_{idx}", G[:, g, :])
+        return order
+
+    def read_mesh_bands_from_msh_file(self, filename: str):
+        """MeshBZ::read_mesh_bands_from_msh_file (bz_mesh.cpp:330-392): every 1-component view is a band
+        (valence when its first value is <= 0.1 eV), every 3-component view the gradient of the band
+        before it. Returns (energies [n][nb], gradients [n][nb][3] or None) and keeps them."""
+        bands, grads = [], []
+        for name, ncomp, tags, vals in read_msh_node_data(filename):
+            if ncomp == 1:
+                bands.append(vals[:, 0])
+            elif ncomp == 3:
+                grads.append(vals)
+            else:
+                raise RuntimeError(f"read_mesh_bands_from_msh_file: unsupported number of components per view: {ncomp}")
+        self.energies = np.stack(bands, axis=1) if bands else None
+        self.gradients = np.stack(grads, axis=1) if grads and len(grads) == len(bands) else None
+        return self.energies, self.gradients
 
     # ---- the k-star of every wedge vertex ---------------------------------------------------------
     def build_kstar_ibz_to_bz(self, digits: int = 9):
