@@ -5,7 +5,9 @@
 // the basis (the caller keeps them alive) and one instance is not thread-safe.
 #pragma once
 
+#include <map>
 #include <memory>
+#include <tuple>
 #include <vector>
 
 #include "DenseTypes.h"
@@ -30,6 +32,17 @@ class Hamiltonian {
     // Throws std::runtime_error("Eigenvalue decomposition failed") on a non-finite solve.
     void Diagonalize(bool keep_eigenvectors = false);
 
+    // No reference counterpart: solves every k of `kpoints` in one batched device solve and keeps the
+    // results, so that a caller's loop SetMatrix(k, nl, soc) / Diagonalize(keep) over these k-points
+    // (bz_states.cpp:30-47, DielectricFunction.cpp:92-119) takes them from the batch instead of one
+    // launch per k. The results are bit-identical to the per-k solve (the same kernels per matrix).
+    // A k (compared exactly) or flags not in the batch, or eigenvectors asked when the batch kept
+    // none, fall back to the per-k solve. Host memory: n doubles per k, plus n x n complex per k with
+    // keep_eigenvectors. A new call replaces the batch; ClearBatch() drops it.
+    void PrepareBatch(const std::vector<Vector3D<double>>& kpoints, bool add_non_local_correction = false,
+                      bool enable_soc = false, bool keep_eigenvectors = false);
+    void ClearBatch();
+
     const RealVector&    get_eigenvalues() const { return m_values; }
     const ComplexMatrix& get_eigenvectors() const { return m_vectors; }
     const RealVector&    eigenvalues() const { return m_values; }
@@ -53,6 +66,11 @@ class Hamiltonian {
     bool              m_nl = false, m_soc = false, m_set = false;
     RealVector       m_values;
     ComplexMatrix    m_vectors;
+    // the prefetched batch: k -> row, its flags, values [nk][n] and vectors [nk][n][n] (re, im)
+    std::map<std::tuple<double, double, double>, size_t> m_batch_row;
+    bool                m_batch_nl = false, m_batch_soc = false, m_batch_vec = false;
+    int                 m_batch_n  = 0;
+    std::vector<double> m_batch_E, m_batch_X;
 };
 
 }  // namespace uepm::pseudopotential

@@ -1,7 +1,10 @@
 // adapter_driver.cpp -- exercises the C++ adapter the way the reference's apps use src/EPP:
 // Materials -> BandStructure::Initialize(path) -> Compute_parallel(true) -> AdjustValues -> export,
-// and Hamiltonian::SetMatrix / Diagonalize(true) / compute_gradient_at_level at one k-point.
+// and Hamiltonian::SetMatrix / Diagonalize(true) / compute_gradient_at_level at one k-point, and the
+// same loop over a few k-points after Hamiltonian::PrepareBatch against the per-k solves.
 //   adapter_driver <yaml> <material> <path> <npoints> <nbands> <shells> <nl 0|1> <soc 0|1> <fp64|mixed> <out_prefix>
+#include <algorithm>
+#include <cmath>
 #include <cstdio>
 #include <cstdlib>
 #include <string>
@@ -55,6 +58,23 @@ int main(int argc, char** argv) {
         std::fprintf(fh, "G %u %.17g %.17g %.17g\n", lvl, gr.X, gr.Y, gr.Z);
     }
     std::fclose(fh);
+    // a caller's loop over k-points (bz_states.cpp:30-47) after one batched solve, against per-k solves
+    std::vector<Vector3D<double>> ks;
+    for (int q = 0; q < 6; ++q) ks.emplace_back(0.11 - 0.05 * q, 0.27 + 0.03 * q, -0.05 + 0.02 * q);
+    Hamiltonian hb(mat, bs.get_basis_vectors()), h1(mat, bs.get_basis_vectors());
+    hb.PrepareBatch(ks, nl, soc, true);
+    double dv = 0.0, dx = 0.0;
+    for (const auto& kq : ks) {
+        hb.SetMatrix(kq, nl, soc);
+        hb.Diagonalize(true);
+        h1.SetMatrix(kq, nl, soc);
+        h1.Diagonalize(true);
+        for (long i = 0; i < h1.eigenvalues().size(); ++i) dv = std::max(dv, std::fabs(hb.eigenvalues()(i) - h1.eigenvalues()(i)));
+        for (long b = 0; b < h1.get_eigenvectors().cols(); ++b)
+            for (long r = 0; r < h1.get_eigenvectors().rows(); ++r)
+                dx = std::max(dx, std::abs(hb.get_eigenvectors()(r, b) - h1.get_eigenvectors()(r, b)));
+    }
+    std::printf("batchdiff %.17g %.17g\n", dv, dx);
     std::printf("gap %.17g\nfile %s\n", gap, bs.path_band_filename().c_str());
     return 0;
 }

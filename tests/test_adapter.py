@@ -91,6 +91,9 @@ def test_adapter_matches_oracle(gpu, oracle, mats, tmp_path, yaml, mat, key, nl,
     H = oracle.assemble(mats[key], G, [0.11, 0.27, -0.05], nl=bool(nl), soc=bool(soc))
     Eoh = oracle.eigh(H)
     assert (np.abs(Eh - Eoh) <= np.maximum(1e-10, 1e-12 * np.abs(Eoh))).all()
+    # Hamiltonian::PrepareBatch: a caller's per-k loop served from one batched solve, bit-identical
+    dv, dx = [float(x) for x in [l for l in r.stdout.splitlines() if l.startswith("batchdiff")][0].split()[1:]]
+    assert dv == 0.0 and dx == 0.0
 
 
 @pytest.mark.gpu

@@ -74,7 +74,63 @@ bool Hamiltonian::check_matrix_is_symmetric() const {
     return uepm_ctx_force_complex(context(m_nl, m_soc), 0) == 1;
 }
 
+void Hamiltonian::PrepareBatch(const std::vector<Vector3D<double>>& kpoints, bool add_non_local_correction,
+                               bool enable_soc, bool keep_eigenvectors) {
+    ClearBatch();
+    if (kpoints.empty()) return;
+    uepm_ctx*           ctx = context(add_non_local_correction, enable_soc);
+    const int           n   = uepm_ctx_order(ctx);
+    const size_t        nk  = kpoints.size();
+    std::vector<double> k(3 * nk), E(nk * (size_t)n), X(keep_eigenvectors ? nk * 2 * (size_t)n * n : 0);
+    std::vector<int32_t> st(nk, 0);
+    for (size_t i = 0; i < nk; ++i) {
+        k[3 * i]     = kpoints[i].X;
+        k[3 * i + 1] = kpoints[i].Y;
+        k[3 * i + 2] = kpoints[i].Z;
+    }
+    const int rc = uepm_solve(ctx, k.data(), nk, n, keep_eigenvectors ? UEPM_WANT_VECTORS : 0u, E.data(),
+                              keep_eigenvectors ? X.data() : nullptr, nullptr, st.data());
+    // k-points whose solve failed are left out: their own Diagonalize re-solves and throws
+    if (rc != UEPM_ERR_NOT_CONVERGED) throw_for(rc, "Hamiltonian::PrepareBatch");
+    for (size_t i = 0; i < nk; ++i)
+        if (st[i] == 0) m_batch_row.emplace(std::make_tuple(k[3 * i], k[3 * i + 1], k[3 * i + 2]), i);
+    m_batch_nl  = add_non_local_correction;
+    m_batch_soc = enable_soc;
+    m_batch_vec = keep_eigenvectors;
+    m_batch_n   = n;
+    m_batch_E   = std::move(E);
+    m_batch_X   = std::move(X);
+}
+
+void Hamiltonian::ClearBatch() {
+    m_batch_row.clear();
+    m_batch_E.clear();
+    m_batch_E.shrink_to_fit();
+    m_batch_X.clear();
+    m_batch_X.shrink_to_fit();
+    m_batch_n = 0;
+}
+
 void Hamiltonian::Diagonalize(bool keep_eigenvectors) {
+    if (m_batch_n > 0 && m_nl == m_batch_nl && m_soc == m_batch_soc && (!keep_eigenvectors || m_batch_vec)) {
+        const auto it = m_batch_row.find(std::make_tuple(m_k.X, m_k.Y, m_k.Z));
+        if (it != m_batch_row.end()) {
+            const int    n   = m_batch_n;
+            const size_t row = it->second;
+            m_values.resize(n);
+            for (int i = 0; i < n; ++i) m_values(i) = m_batch_E[row * n + i];
+            if (keep_eigenvectors) {
+                const double* X = m_batch_X.data() + row * 2 * (size_t)n * n;
+                m_vectors.resize(n, n);
+                for (int b = 0; b < n; ++b)
+                    for (int r = 0; r < n; ++r)
+                        m_vectors(r, b) = std::complex<double>(X[2 * ((size_t)b * n + r)], X[2 * ((size_t)b * n + r) + 1]);
+            } else {
+                m_vectors.resize(0, 0);
+            }
+            return;
+        }
+    }
     uepm_ctx*         ctx = context(m_nl, m_soc);
     const int         n   = uepm_ctx_order(ctx);
     const double      k[3] = {m_k.X, m_k.Y, m_k.Z};
