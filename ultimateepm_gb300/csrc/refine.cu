@@ -675,7 +675,9 @@ void launch_refine_project(const typename Split<S>::type* H, int n, int ld, size
     }
     if constexpr (!std::is_same<S, double>::value) {
         // complex dense H from order kRefineTcMinN: Y = H X on the tensor cores (Ozaki splitting,
-        // refine_tc.cu), then S and A here
+        // refine_tc.cu), then S and A here. A real H stays on the FP32 pipe: with a quarter of the
+        // complex multiply-adds per element there, the tensor-core form's slicing and second pass over
+        // H do not pay (Ge nonlocal n = 181, 2000 k: 0.96 ms against 0.83)
         if (tensor_cores && n >= kRefineTcMinN &&
             launch_refine_y_tc(H, n, ld, mstride, X32, m, proj_mp<S>(m), work, refine_work_elems(n, m), status, batch, s)) {
             refine_project_t<S, false, true>(H, n, ld, mstride, X32, m, work, small, batch, s, sv);
