@@ -192,7 +192,7 @@ int uepm_measure_peak(int precision, double* tflops);
  *                 to the next pass (a read-only pass, then a rank-4 pass: 3 passes per two steps), 6 blocked:
  *                 panels of 16 columns whose updates are applied once per panel, only the lower
  *                 triangle read and written, one matrix per SM (FP32, n <= 512);
- *                 automatic: 1 where it applies, 6 for the FP32 orders 300..512, 5 for the other FP32
+ *                 automatic: 1 where it applies, 6 for the FP32 orders 200..512 (real: 300..512), 5 for the other FP32
  *                 matrices, else 2
  *   ctas_per_sm   CTAs per SM of the global-memory reduction (its L2 working set), 1..8
  *   vector_lanes  lanes per eigenvector in the back-transformation: 8, 16 or 32

@@ -785,10 +785,13 @@ void launch_tridiag(S* H, int n, int ld, size_t mstride, typename ST<S>::R* d, t
     // update deferred, 3 passes per two steps, 5 and automatic). Reduction time per 2000 k: Ge SOC
     // n = 362 222 ms unfused, 102.7 fused, 81.3 deferred; GaP SOC n = 458 230.6 -> 198.3 ms.
     if constexpr (F32) {
-        // the blocked kernel (6) is automatic from order 300 (2000 k, mixed: Ge SOC n = 362 81.3 ->
-        // 47.5 ms, Si SOC n = 338 67.1 -> 41.7, GaP SOC n = 458 198.3 -> 81.8); below, the deferred
-        // kernel stays ahead (GaAs SOC n = 178 9.5 against 12.6 ms, InAs n = 229 equal)
-        if ((variant == 6 || (variant == 0 && n >= 300)) &&
+        // the blocked kernel (6) is automatic from order 200 (2000 k, mixed: Ge SOC n = 362 81.3 ->
+        // 47.5 ms, Si SOC n = 338 67.1 -> 41.7, GaP SOC n = 458 198.3 -> 81.8; with its trailing updates
+        // on the tensor cores, whole solves against the deferred kernel: Si SOC n = 274 33.4 against
+        // 45.5 ms, InAs n = 229 27.2 against 27.7); below, the deferred kernel stays ahead (GaAs SOC
+        // n = 178 16.5 against 19.3 ms per solve). Real matrices, whose updates stay on the FP32 pipe,
+        // keep the order-300 switch it was measured at.
+        if ((variant == 6 || (variant == 0 && n >= (ST<S>::cplx ? 200 : 300))) &&
             launch_tridiag_blocked<S>(H, n, ld, mstride, d, e, tq, status, batch, s, tensor_cores))
             return;
         // automatic: the deferred kernel for every FP32 order beyond the register kernel, also where
