@@ -585,7 +585,11 @@ template <typename T>
 void launch_invit(const T* d, const T* e, const T* ev, int ev_ld, int n, int nb, T* work, T* z, int* status, int batch,
                   cudaStream_t s, int cap) {
     const size_t smem = invit_smem_bytes<T>(n, std::min(nb, 32));
-    if (smem <= 200 * 1024) {
+    // shared memory where at least four warps fit per SM; beyond that the latency-bound recurrences
+    // run better from the L1/L2-cached workspace at higher occupancy (FP32, 2000 k: Ge SOC n = 362
+    // 1.9 -> 1.6 ms, one warp per SM in shared memory; Si n = 137 0.13 ms in shared memory against
+    // 0.18 from the workspace)
+    if (smem <= 56 * 1024 || (sizeof(T) == 8 && smem <= 200 * 1024)) {
         auto kern = k_invit<T, true>;
         if (smem > 48 * 1024) cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         kern<<<batch, 32, smem, s>>>(d, e, ev, ev_ld, n, nb, work, z, status, batch, cap);
