@@ -627,6 +627,42 @@ def run_configs(seed: int = 20261203):
             ctx.close()
         n64 = res["fp64"][2]
         err = (res["mixed"][0][:n64] - res["fp64"][0]).abs().amax(dim=0).cpu().numpy()
+        tc_block = None
+        if soc:
+            # the mixed solve's kernels on 2000 of the k-points, CUDA events per kernel (a separate,
+            # profiled solve: the timed one above runs without events), with the tensor-core kernels'
+            # work: the reduction's panel updates (tcgen05 kind::tf32) and Y = H X (kind::f16 on BF16
+            # slices: 36 slice pairs x 2 x 128 x N x K per 128-row tile)
+            ctx = api._Context(m, G, nl, soc, N.UEPM_PREC_MIXED)
+            n, mm = ctx.n, nbt + 4
+            kk = dk[:2000].contiguous()
+            solve_timed(ctx, kk, nbt)
+            N.check(L.uepm_ctx_set_profiling(ctx.h, 1))
+            solve_timed(ctx, kk, nbt)
+            kms = (C.c_double * N.KERNEL_KINDS)()
+            kcnt = (C.c_uint64 * N.KERNEL_KINDS)()
+            N.check(L.uepm_ctx_read_profile(ctx.h, kms, kcnt, N.KERNEL_KINDS))
+            prof = {L.uepm_kernel_name(q).decode(): kms[q] for q in range(N.KERNEL_KINDS) if kcnt[q]}
+            ctx.close()
+            mpad = (mm + 3) // 4 * 4
+            ncol = (2 * mpad + 15) // 16 * 16
+            kdim = 32 * ((n + 15) // 16)
+            bf16_flop = 36 * 2 * 128 * ncol * kdim * ((n + 127) // 128) * 2000
+            rp_ms = prof.get("refine_project", float("nan"))
+            tc_block = {
+                "kernels_ms_per_2000_k": {q: round(v, 3) for q, v in prof.items()},
+                "tensor_core_kernels": ["k_tridiag_blocked (panel updates, tcgen05.mma kind::tf32, hi/lo splits)",
+                                        "k_refine_y_tc (Y = H X, tcgen05.mma kind::f16 on exact BF16 slices)"],
+                "refine_project_bf16_issued_tflops": bf16_flop / (rp_ms * 1e-3) / 1e12,
+                "refine_project_note": "refine_project = k_refine_y_tc + the double-single S, A kernel; BF16 "
+                                       "flops issued by the slice products over that time",
+            }
+            try:
+                mpk = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+                tc_block["refine_project_frac_of_measured_bf16_peak"] = tc_block["refine_project_bf16_issued_tflops"] / float(
+                    mpk["bf16_tflops"])
+            except (OSError, KeyError, ValueError):
+                pass
         fp64_rate = n64 / (res["fp64"][1] * 1e-3)
         mixed_rate = res["mixed"][2] / (res["mixed"][1] * 1e-3)
         out[name] = {
@@ -639,6 +675,8 @@ def run_configs(seed: int = 20261203):
             "mixed_ms": res["mixed"][1], "fp64_ms": res["fp64"][1],
             "mixed_max_err_ev": float(err.max()), "mixed_max_err_ev_per_band": [float(x) for x in err],
         }
+        if tc_block:
+            out[name]["profiled"] = tc_block
         del dk, res
         torch.cuda.empty_cache()
     return out
