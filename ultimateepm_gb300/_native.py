@@ -42,7 +42,7 @@ EXPORTED = [
     "uepm_batch_add", "uepm_batch_clear", "uepm_batch_set_graph", "uepm_batch_run", "uepm_batch_kernels_per_run",
     "uepm_server_create", "uepm_server_destroy", "uepm_server_submit", "uepm_server_wait", "uepm_server_stats",
     "uepm_server_reset_stats", "uepm_star_expand_device", "uepm_star_operations", "uepm_dielectric_sums_device",
-    "uepm_pivot_reciprocal_device",
+    "uepm_pivot_reciprocal_device", "uepm_ds_special_device",
 ]
 UEPM_SERVE_VELOCITY = 1
 NOALLOC_SCRATCH_BYTES = 16 << 20
@@ -148,6 +148,7 @@ def load():
             "uepm_star_expand_device": (C.c_int, [vp, vp, vp, vp, C.c_size_t, C.c_int, vp, vp, vp]),
             "uepm_star_operations": (C.c_int, [dp, dp, C.c_size_t, C.POINTER(C.c_uint16), ip]),
             "uepm_pivot_reciprocal_device": (C.c_int, [vp, C.c_double, C.c_size_t, vp, vp]),
+            "uepm_ds_special_device": (C.c_int, [C.c_int, vp, C.c_size_t, vp, vp]),
             "uepm_dielectric_sums_device": (C.c_int, [vp, vp, vp, vp, C.c_size_t, C.c_int, C.c_int, C.c_int, vp, C.c_int,
                                                       C.c_double, vp, vp, vp]),
         }

@@ -27,6 +27,7 @@
 #include <type_traits>
 
 #include "uepm_common.cuh"
+#include "ctx_internal.h"
 #include "uepm_kernels.h"
 
 namespace uepm {
@@ -294,10 +295,54 @@ __device__ __forceinline__ ds VF_l_ds(int l, ds n1s, bool far, bool big, ds inv,
     }
     return (l == 0) ? VR3t : ds{0.f, 0.f};
 }
-// The gaussian well's i2(x) = ((x^2 + 3) sinh x - 3 x cosh x) / x^3 for x > 2 (callers route smaller x
-// to the FP64 element): e^x from the FP64 exponential (one FP64 call), the rest in double-single.
+// Double-single constants from double values (rounded at compile time): ln 2 in three FP32 parts
+// (the first of 16 bits, so that k L1 is exact for |k| < 256) from the double-double value of ln 2,
+// and the reciprocal factorials of the exponential's Taylor series.
+constexpr double kLn2Hi = 0.6931471805599453, kLn2Lo = 2.3190468138462996e-17;
+constexpr float  kLn2P1 = 0.693145751953125f;  // 45426 / 65536
+constexpr float  kLn2P2 = (float)(kLn2Hi - 0.693145751953125);
+constexpr float  kLn2P3 = (float)((kLn2Hi - 0.693145751953125 - (double)kLn2P2) + kLn2Lo);
+__host__ __device__ constexpr double inv_fact(int j) { return j <= 1 ? 1.0 : inv_fact(j - 1) / j; }
+// 1 / (2^k k! (2k + 5)!!): the power series of i2(x) = x^2 sum_k (x^2)^k a_k
+__host__ __device__ constexpr double dfact(int m) { return m <= 1 ? 1.0 : m * dfact(m - 2); }
+__host__ __device__ constexpr double i2_coef(int k) { return 1.0 / ((double)(1ull << k) / inv_fact(k) * dfact(2 * k + 5)); }
+// Horner steps p <- p y + c_J, ..., p y + c_0 with the coefficients (1 / J! for e^x, i2_coef for
+// i2) split into FP32 pairs at compile time
+template <bool EXP, int J>
+__device__ __forceinline__ ds horner_ds(ds p, ds y) {
+    constexpr double c  = EXP ? inv_fact(J) : i2_coef(J);
+    constexpr float  ch = (float)c, cl = (float)(c - (double)(float)c);
+    p = ds_add(ds_mul(p, y), ds{ch, cl});
+    if constexpr (J > 0) return horner_ds<EXP, J - 1>(p, y);
+    else return p;
+}
+
+// e^x for 2 < x <= 80 in double-single arithmetic: Cody and Waite's argument reduction
+// (W. J. Cody, W. Waite, Software Manual for the Elementary Functions, 1980) x = k ln 2 + r with
+// |r| <= ln 2 / 2, the Taylor series of e^r to degree 13 by Horner's rule (remainder below 2^-50),
+// then 2^k. Relative error about 2^-47 (checked against a 40-digit reference over the range).
+__device__ __forceinline__ ds ds_exp_pos(ds x) {
+    const float k = rintf(__fmul_rn(x.h, 1.4426950408889634f));
+    ds          r = ds_add(x, ds{-k * kLn2P1, 0.f});  // k L1 exact; the difference exact (close operands)
+    r             = ds_add(r, ds_mulf(ds{-kLn2P2, -kLn2P3}, k));
+    constexpr float c13h = (float)inv_fact(13), c13l = (float)(inv_fact(13) - (double)(float)inv_fact(13));
+    const ds  p    = horner_ds<true, 12>(ds{c13h, c13l}, r);
+    const int ki   = (int)k;
+    return ds{ldexpf(p.h, ki), ldexpf(p.l, ki)};
+}
+
+// The gaussian well's i2(x) = ((x^2 + 3) sinh x - 3 x cosh x) / x^3 (the modified spherical Bessel
+// function of order 2; the reference's closed form, bessel_func.hpp:47-52), in double-single. For
+// x <= 2, where the closed form cancels, its power series x^2 sum_k (x^2 / 2)^k / (k! (2k + 5)!!) to
+// k = 13 (remainder below 2^-50 of the sum); above, the closed form with e^x from ds_exp_pos (callers
+// route x > 80 to the FP64 element: e^x would leave FP32's range).
 __device__ __forceinline__ ds i2_ds(ds x) {
-    const ds E  = ds_of_double(exp((double)x.h + (double)x.l));
+    if (x.h <= 2.f) {
+        constexpr float a13h = (float)i2_coef(13), a13l = (float)(i2_coef(13) - (double)(float)i2_coef(13));
+        const ds        y    = ds_mul(x, x);
+        return ds_mul(horner_ds<false, 12>(ds{a13h, a13l}, y), y);
+    }
+    const ds E  = ds_exp_pos(x);
     const ds Ei = ds_div(ds{1.f, 0.f}, E);
     const ds sh = ds_mulf(ds_sub(E, Ei), 0.5f), ch = ds_mulf(ds_add(E, Ei), 0.5f);
     const ds x2 = ds_mul(x, x);
@@ -470,15 +515,15 @@ __global__ void __launch_bounds__(256) k_assemble_tiles(const DevParams P, const
 
 // Whether the double-single nonlocal element must give way to the FP64 one for the pair of norms
 // (n1, n2): where the reference's far branch divides rounding-level differences (|n1 - n2| within
-// 1e-5 of the norms), and for gaussian wells where i2's closed form cancels (x <= 2). far returns
-// the reference's branch.
+// 1e-5 of the norms), and for gaussian wells where i2's argument x exceeds 80 (e^x beyond FP32's
+// range). far returns the reference's branch.
 __device__ __forceinline__ bool nl_needs_fp64(const DevParams& P, double n1, double n2, bool& far) {
     const double dn = fabs(n1 - n2);
     far             = F_l_far(n1, n2);
     if (far && dn < 1.0e-5 * fmax(n1, n2)) return true;
     if (!P.square) {
-        if (P.has_A2a && 0.5 * (P.R2a * P.R2a) * (n1 * n2) <= 2.0) return true;
-        if (!P.same_nl && P.has_A2c && 0.5 * (P.R2c * P.R2c) * (n1 * n2) <= 2.0) return true;
+        if (P.has_A2a && 0.5 * (P.R2a * P.R2a) * (n1 * n2) > 80.0) return true;
+        if (!P.same_nl && P.has_A2c && 0.5 * (P.R2c * P.R2c) * (n1 * n2) > 80.0) return true;
     }
     return false;
 }
@@ -782,4 +827,26 @@ template void launch_assemble_soc_ds<ds4>(const DevParams&, const DevParamsDS&, 
                                           const float2*, const cx<double>*, const double2*, const double2*, const double*,
                                           ds4*, int, size_t, cx<float>*, size_t, int, cudaStream_t);
 
+// ---- diagnostics: the mixed path's double-single special functions on device values -----------
+__global__ void k_ds_special(int fn, const double* __restrict__ x, size_t n, double* __restrict__ y) {
+    const size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    const ds v = ds_of_double(x[t]);
+    const ds r = fn == 0 ? ds_exp_pos(v) : i2_ds(v);
+    y[t]       = (double)r.h + (double)r.l;
+}
+
 }  // namespace uepm
+
+extern "C" int uepm_ds_special_device(int fn, const double* d_x, size_t n, double* d_y, void* stream) {
+    if ((fn != 0 && fn != 1) || (n && (!d_x || !d_y))) {
+        uepm::set_error("uepm_ds_special_device: fn must be 0 (e^x) or 1 (i2), and the buffers non-null");
+        return UEPM_ERR_INVALID;
+    }
+    if (n == 0) return UEPM_OK;
+    const unsigned blocks = (unsigned)((n + 255) / 256);
+    uepm::k_ds_special<<<blocks, 256, 0, (cudaStream_t)stream>>>(fn, d_x, n, d_y);
+    uepm::count_launch();
+    return cudaGetLastError() == cudaSuccess ? UEPM_OK : UEPM_ERR_CUDA;
+}
+
