@@ -166,9 +166,9 @@ int uepm_pivot_reciprocal_device(const double* d_q, double pivmin, size_t n, dou
 /* Diagnostics (no reference counterpart): the double-single special functions the mixed path's
  * gaussian-well elements use, on n device values x (rounded to FP32 pairs), written to device y as
  * h + l, enqueued on `stream`. fn 0: e^x for 2 < x <= 80 (Cody-Waite reduction and a degree-13
- * Taylor series); fn 1: i2(x) = ((x^2 + 3) sinh x - 3 x cosh x) / x^3 for 0 <= x <= 80 (its power
- * series up to x = 2, the closed form above), as bessel_func.hpp:47-52 defines it. Lets tests bound
- * them against high-precision values. */
+ * Taylor series); fn 1: i2(x) = ((x^2 + 3) sinh x - 3 x cosh x) / x^3 for 2 < x <= 80, the closed
+ * form bessel_func.hpp:47-52 defines, with that e^x. Lets tests bound them against high-precision
+ * values. */
 int uepm_ds_special_device(int fn, const double* d_x, size_t n, double* d_y, void* stream);
 
 /* Launch counters (kernels enqueued by this library since load), for launch accounting. */

@@ -303,17 +303,14 @@ constexpr float  kLn2P1 = 0.693145751953125f;  // 45426 / 65536
 constexpr float  kLn2P2 = (float)(kLn2Hi - 0.693145751953125);
 constexpr float  kLn2P3 = (float)((kLn2Hi - 0.693145751953125 - (double)kLn2P2) + kLn2Lo);
 __host__ __device__ constexpr double inv_fact(int j) { return j <= 1 ? 1.0 : inv_fact(j - 1) / j; }
-// 1 / (2^k k! (2k + 5)!!): the power series of i2(x) = x^2 sum_k (x^2)^k a_k
-__host__ __device__ constexpr double dfact(int m) { return m <= 1 ? 1.0 : m * dfact(m - 2); }
-__host__ __device__ constexpr double i2_coef(int k) { return 1.0 / ((double)(1ull << k) / inv_fact(k) * dfact(2 * k + 5)); }
-// Horner steps p <- p y + c_J, ..., p y + c_0 with the coefficients (1 / J! for e^x, i2_coef for
-// i2) split into FP32 pairs at compile time
-template <bool EXP, int J>
-__device__ __forceinline__ ds horner_ds(ds p, ds y) {
-    constexpr double c  = EXP ? inv_fact(J) : i2_coef(J);
+// Horner steps p <- p y + 1 / J!, ..., p y + 1 / 0! with the coefficients split into FP32 pairs at
+// compile time
+template <int J>
+__device__ __forceinline__ ds horner_exp_ds(ds p, ds y) {
+    constexpr double c  = inv_fact(J);
     constexpr float  ch = (float)c, cl = (float)(c - (double)(float)c);
     p = ds_add(ds_mul(p, y), ds{ch, cl});
-    if constexpr (J > 0) return horner_ds<EXP, J - 1>(p, y);
+    if constexpr (J > 0) return horner_exp_ds<J - 1>(p, y);
     else return p;
 }
 
@@ -326,22 +323,18 @@ __device__ __forceinline__ ds ds_exp_pos(ds x) {
     ds          r = ds_add(x, ds{-k * kLn2P1, 0.f});  // k L1 exact; the difference exact (close operands)
     r             = ds_add(r, ds_mulf(ds{-kLn2P2, -kLn2P3}, k));
     constexpr float c13h = (float)inv_fact(13), c13l = (float)(inv_fact(13) - (double)(float)inv_fact(13));
-    const ds  p    = horner_ds<true, 12>(ds{c13h, c13l}, r);
+    const ds  p    = horner_exp_ds<12>(ds{c13h, c13l}, r);
     const int ki   = (int)k;
     return ds{ldexpf(p.h, ki), ldexpf(p.l, ki)};
 }
 
 // The gaussian well's i2(x) = ((x^2 + 3) sinh x - 3 x cosh x) / x^3 (the modified spherical Bessel
-// function of order 2; the reference's closed form, bessel_func.hpp:47-52), in double-single. For
-// x <= 2, where the closed form cancels, its power series x^2 sum_k (x^2 / 2)^k / (k! (2k + 5)!!) to
-// k = 13 (remainder below 2^-50 of the sum); above, the closed form with e^x from ds_exp_pos (callers
-// route x > 80 to the FP64 element: e^x would leave FP32's range).
+// function of order 2; the reference's closed form, bessel_func.hpp:47-52) for 2 < x <= 80, in
+// double-single with e^x from ds_exp_pos. At x <= 2 the closed form cancels (absolute error ~3 eps /
+// x^2 in the reference's FP64 evaluation): callers take the FP64 bessel_i2 of the FP64 argument
+// there, the very value the FP64 path (and the reference) uses, so that the two paths do not differ
+// by that cancellation; x > 80 goes to the FP64 element (e^x would leave FP32's range).
 __device__ __forceinline__ ds i2_ds(ds x) {
-    if (x.h <= 2.f) {
-        constexpr float a13h = (float)i2_coef(13), a13l = (float)(i2_coef(13) - (double)(float)i2_coef(13));
-        const ds        y    = ds_mul(x, x);
-        return ds_mul(horner_ds<false, 12>(ds{a13h, a13l}, y), y);
-    }
     const ds E  = ds_exp_pos(x);
     const ds Ei = ds_div(ds{1.f, 0.f}, E);
     const ds sh = ds_mulf(ds_sub(E, Ei), 0.5f), ch = ds_mulf(ds_add(E, Ei), 0.5f);
@@ -350,10 +343,19 @@ __device__ __forceinline__ ds i2_ds(ds x) {
     return ds_div(num, ds_mul(x2, x));
 }
 
+// i2 of the gaussian well with radius R: x = R^2 / 2 n1 n2, from the FP64 norms where x <= 2 (the
+// FP64 element's own operands and function), else in double-single (R2h = R^2 / 2 as a pair, np =
+// n1 n2 in double-single).
+__device__ __forceinline__ ds i2_gauss(double R, ds R2h, ds np, double n1d, double n2d) {
+    const double argd = 0.5 * (R * R) * n1d * n2d;
+    return argd <= 2.0 ? ds_of_double(bessel_i2(argd)) : i2_ds(ds_mul(R2h, np));
+}
+
 // far: the reference's branch |n1 - n2| > 1e-4, decided on the FP64 norms by the caller (the
 // double-single difference is not resolved finely enough for it).
-__device__ void nl_element_ds(const DevParamsDS& Q, const float2* Ri, const float2* Rj, ds pc, ds ps, bool far, ds& re,
-                              ds& im) {
+// n1d, n2d: the FP64 norms (the gaussian well's argument at x <= 2, as the FP64 element forms it).
+__device__ void nl_element_ds(const DevParams& P, const DevParamsDS& Q, const float2* Ri, const float2* Rj, ds pc, ds ps,
+                              bool far, double n1d, double n2d, ds& re, ds& im) {
     const ds   n1  = rd(Ri, RF_NK), n2 = rd(Rj, RF_NK);
     const ds   dp  = ds_add(ds_add(ds_mul(rd(Ri, RF_KX), rd(Rj, RF_KX)), ds_mul(rd(Ri, RF_KY), rd(Rj, RF_KY))),
                             ds_mul(rd(Ri, RF_KZ), rd(Rj, RF_KZ)));
@@ -374,7 +376,7 @@ __device__ void nl_element_ds(const DevParamsDS& Q, const float2* Ri, const floa
             Va = ds_add(Va, ds_mul(ds_mul(Q.A2a_5, lg2),
                                    VF_l_ds(2, n1s, far, big, inv, Ri, Rj, RF_J2A, n2s, Q.VR2a2s, Q.VR2a3h, ds{0.f, 0.f})));
         else
-            Va = ds_add(Va, ds_mul(ds_mul(Q.gA2a, lg2), ds_mul(i2_ds(ds_mul(Q.R2a2h, np)), ds_mul(rd(Ri, RF_GEA), rd(Rj, RF_GEA)))));
+            Va = ds_add(Va, ds_mul(ds_mul(Q.gA2a, lg2), ds_mul(i2_gauss(P.R2a, Q.R2a2h, np, n1d, n2d), ds_mul(rd(Ri, RF_GEA), rd(Rj, RF_GEA)))));
     }
     if (Q.same_nl) {
         re = ds_mul(pc, Va);
@@ -389,7 +391,7 @@ __device__ void nl_element_ds(const DevParamsDS& Q, const float2* Ri, const floa
             Vc = ds_add(Vc, ds_mul(ds_mul(Q.A2c_5, lg2),
                                    VF_l_ds(2, n1s, far, big, inv, Ri, Rj, RF_J2C, n2s, Q.VR2c2s, Q.VR2c3h, ds{0.f, 0.f})));
         else
-            Vc = ds_add(Vc, ds_mul(ds_mul(Q.gA2c, lg2), ds_mul(i2_ds(ds_mul(Q.R2c2h, np)), ds_mul(rd(Ri, RF_GEC), rd(Rj, RF_GEC)))));
+            Vc = ds_add(Vc, ds_mul(ds_mul(Q.gA2c, lg2), ds_mul(i2_gauss(P.R2c, Q.R2c2h, np, n1d, n2d), ds_mul(rd(Ri, RF_GEC), rd(Rj, RF_GEC)))));
     }
     re = ds_mul(pc, ds_mulf(ds_add(Va, Vc), 0.5f));
     im = ds_mul(ps, ds_mulf(ds_sub(Va, Vc), 0.5f));
@@ -609,7 +611,7 @@ __global__ void __launch_bounds__(256) k_assemble_tiles_ds(const DevParams P, co
                 const float4  vl = Vloc32[(size_t)j * N + i];
                 const float4  ph = phNL32[(size_t)j * N + i];
                 ds            vr, vi;
-                nl_element_ds(Q, Ri, Rj, ds{ph.x, ph.y}, ds{ph.z, ph.w}, far, vr, vi);
+                nl_element_ds(P, Q, Ri, Rj, ds{ph.x, ph.y}, ds{ph.z, ph.w}, far, n1, n2, vr, vi);
                 ds hr = ds{vl.x, vl.y}, hi = ds{vl.z, vl.w};
                 if (i == j) hr = ds_add(hr, rd(Ri, RF_KIN));
                 hr = ds_add(hr, vr);
@@ -710,7 +712,7 @@ __global__ void __launch_bounds__(256) k_assemble_soc_tiles(const DevParams P, c
                     if (!fp64) {
                         const float4 pn = phNL32[(size_t)j * N + i];
                         ds           vr, vi;
-                        nl_element_ds(Q, Ri32, Rj32, ds{pn.x, pn.y}, ds{pn.z, pn.w}, far, vr, vi);
+                        nl_element_ds(P, Q, Ri32, Rj32, ds{pn.x, pn.y}, ds{pn.z, pn.w}, far, n1, n2, vr, vi);
                         hr = ds_add(hr, vr);
                         hm = ds_add(hm, vi);
                     }
@@ -832,7 +834,7 @@ __global__ void k_ds_special(int fn, const double* __restrict__ x, size_t n, dou
     const size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= n) return;
     const ds v = ds_of_double(x[t]);
-    const ds r = fn == 0 ? ds_exp_pos(v) : i2_ds(v);
+    const ds r = fn == 0 ? ds_exp_pos(v) : i2_ds(v);  // both for 2 < x <= 80
     y[t]       = (double)r.h + (double)r.l;
 }
 
