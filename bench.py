@@ -636,9 +636,12 @@ def run_configs(seed: int = 20261203):
             ctx = api._Context(m, G, nl, soc, N.UEPM_PREC_MIXED)
             n, mm = ctx.n, nbt + 4
             kk = dk[:2000].contiguous()
-            solve_timed(ctx, kk, nbt)
+            solve_timed(ctx, kk, nbt)  # warm
             N.check(L.uepm_ctx_set_profiling(ctx.h, 1))
-            solve_timed(ctx, kk, nbt)
+            dE2 = torch.zeros((2000, nbt), dtype=torch.float64, device="cuda")
+            st2 = torch.zeros(2000, dtype=torch.int32, device="cuda")
+            N.check(L.uepm_solve_device(ctx.h, p(kk), 2000, nbt, N.UEPM_WANT_VALUES, p(dE2), None, None, p(st2), sp))
+            torch.cuda.synchronize()
             kms = (C.c_double * N.KERNEL_KINDS)()
             kcnt = (C.c_uint64 * N.KERNEL_KINDS)()
             N.check(L.uepm_ctx_read_profile(ctx.h, kms, kcnt, N.KERNEL_KINDS))
