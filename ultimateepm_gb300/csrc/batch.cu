@@ -417,8 +417,20 @@ int uepm_batch_run(uepm_batch* b, void* stream) {
     if (cudaEventRecord(b->fork, s) != cudaSuccess) rc = UEPM_ERR_CUDA;
     for (size_t c = 0; !rc && c < ctxs.size(); ++c)
         if (cudaStreamWaitEvent(b->streams[c], b->fork, 0) != cudaSuccess) rc = UEPM_ERR_CUDA;
-    for (size_t g = 0; !rc && g < b->groups.size(); ++g) {
-        const auto& gr = b->groups[g];
+    // groups enqueued by estimated cost, largest first (the reduction's n^3 per k-point, 4x for
+    // complex matrices), so that the longest pipelines start first and the cheap ones fill in behind
+    // them (longest-processing-time order); each group's results do not depend on the order
+    std::vector<size_t> order(b->groups.size());
+    for (size_t g = 0; g < order.size(); ++g) order[g] = g;
+    auto cost = [&](size_t g) {
+        const auto&  gr = b->groups[g];
+        const double n  = (double)gr.ctx->n;
+        return n * n * n * (double)gr.nk * (gr.ctx->real ? 1.0 : 4.0);
+    };
+    std::stable_sort(order.begin(), order.end(), [&](size_t x, size_t y) { return cost(x) > cost(y); });
+    for (size_t q = 0; !rc && q < order.size(); ++q) {
+        const size_t g  = order[q];
+        const auto&  gr = b->groups[g];
         rc = enqueue_solve(gr.ctx, plans[g], gr.k, gr.nk, gr.nb, gr.want, gr.E, gr.X, gr.grad, gr.st, b->streams[gctx[g]]);
     }
     for (size_t c = 0; !rc && c < ctxs.size(); ++c) {
