@@ -53,10 +53,17 @@ constexpr size_t    kYtStage  = kYtSl * (kYtASlice + kYtBSlice);  // 84 KB
 constexpr size_t    kYtSmem   = 2 * kYtStage;
 constexpr long long kYtWaitCycles = 2000000000ll;  // ~1 s at the SM clock
 
-__device__ __forceinline__ bool yt_wait(uint64_t* bar, uint32_t parity) {
+// Bounded wait (~1 s) for the phase of the given parity; a wait that gives up sets the CTA's fail
+// flag, and every later wait of the CTA returns at once (so a failed CTA ends in about a second).
+__device__ __forceinline__ bool yt_wait(uint64_t* bar, uint32_t parity, volatile int* fail) {
     const long long t0 = clock64();
-    while (!tc::mbar_try_wait(bar, parity))
-        if (clock64() - t0 > kYtWaitCycles) return false;
+    while (!tc::mbar_try_wait(bar, parity)) {
+        if (*fail) return false;
+        if (clock64() - t0 > kYtWaitCycles) {
+            *fail = 1;
+            return false;
+        }
+    }
     return true;
 }
 
@@ -103,6 +110,7 @@ __global__ void __launch_bounds__(kYtNT, 1)
     __shared__ int      s_rE[kYtM], s_cE[kYtNmax / 2];
     __shared__ uint64_t s_staged[2], s_done[2];
     __shared__ uint32_t s_tmem;
+    __shared__ int      s_fail;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int b = blockIdx.x / ntile, r0 = (blockIdx.x - b * ntile) * kYtM;
     const ds4*       A  = H + (size_t)b * mstride;
@@ -112,6 +120,7 @@ __global__ void __launch_bounds__(kYtNT, 1)
     if (tid < kYtM) s_rmax[tid] = 0.f;
     if (tid < kYtNmax / 2) s_cmax[tid] = 0.f;
     if (tid == 0) {
+        s_fail = 0;
         tc::mbar_init(&s_staged[0], kYtNT - 32);
         tc::mbar_init(&s_staged[1], kYtNT - 32);
         tc::mbar_init(&s_done[0], 1);
@@ -153,7 +162,7 @@ __global__ void __launch_bounds__(kYtNT, 1)
         const int wid = tid - 32;
         for (int q = 0; q < nch; ++q) {
             const int buf = q & 1;
-            if (q >= 2) ok = yt_wait(&s_done[buf], ((q - 2) >> 1) & 1) && ok;  // the MMAs of chunk q - 2 read it
+            if (q >= 2) ok = yt_wait(&s_done[buf], ((q - 2) >> 1) & 1, &s_fail) && ok;  // the MMAs of chunk q - 2 read it
             unsigned char* st = smraw + (size_t)buf * kYtStage;
             unsigned char* sa = st;                                // slice s at s * kYtASlice
             unsigned char* sb = st + (size_t)kYtSl * kYtASlice;   // slice t at t * kYtBSlice
@@ -213,7 +222,7 @@ __global__ void __launch_bounds__(kYtNT, 1)
         const uint32_t base  = tc::smem_addr(smraw);
         for (int q = 0; q < nch; ++q) {
             const int buf = q & 1;
-            if (!yt_wait(&s_staged[buf], (q >> 1) & 1)) {
+            if (!yt_wait(&s_staged[buf], (q >> 1) & 1, &s_fail)) {
                 ok = false;
                 break;
             }
@@ -241,7 +250,7 @@ __global__ void __launch_bounds__(kYtNT, 1)
     // ---- read back: D_w of this warp's lane quarter, 8-column units, summed in double-single -------
     {
         const int  last = nch - 1;
-        const bool okw  = yt_wait(&s_done[last & 1], (last >> 1) & 1);  // the last commit covers all MMAs
+        const bool okw  = yt_wait(&s_done[last & 1], (last >> 1) & 1, &s_fail);  // the last commit covers all MMAs
         ok              = __syncthreads_and(ok && okw) != 0;
         tc::fence_after_sync();
         if (ok) {

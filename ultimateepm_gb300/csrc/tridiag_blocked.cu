@@ -126,11 +126,17 @@ __device__ __forceinline__ void tc_stage(const cx<float>* Vp, const cx<float>* W
     }
 }
 
-// Waits (bounded, ~1 s) for the phase of the given parity of the mbarrier at bar.
-__device__ __forceinline__ bool tc_wait(uint64_t* bar, uint32_t parity) {
+// Waits (bounded, ~1 s) for the phase of the given parity of the mbarrier at bar. With a fail flag:
+// a wait that gives up sets it, and every later wait of the CTA returns at once.
+__device__ __forceinline__ bool tc_wait(uint64_t* bar, uint32_t parity, volatile int* fail = nullptr) {
     const long long t0 = clock64();
-    while (!tc::mbar_try_wait(bar, parity))
-        if (clock64() - t0 > kTcWaitCycles) return false;
+    while (!tc::mbar_try_wait(bar, parity)) {
+        if (fail && *fail) return false;
+        if (clock64() - t0 > kTcWaitCycles) {
+            if (fail) *fail = 1;
+            return false;
+        }
+    }
     return true;
 }
 
@@ -147,9 +153,9 @@ struct TcTile {
 // that buffer's MMA mbarrier. False if the wait gave up (nothing issued).
 template <int NC>
 __device__ __forceinline__ bool tc_issue(const TcTile& t, const float* aH, const float* aL, const float* bH0,
-                                         uint32_t tbase, uint64_t* staged, uint64_t* done) {
+                                         uint32_t tbase, uint64_t* staged, uint64_t* done, volatile int* fail) {
     const uint32_t buf = t.seq & 1u;
-    if (!tc_wait(staged + buf, (t.seq >> 1) & 1u)) return false;
+    if (!tc_wait(staged + buf, (t.seq >> 1) & 1u, fail)) return false;
     tc::fence_after_sync();
     constexpr uint32_t idesc = tc::idesc_tf32(kTcM, NC);
     const float*       bH    = bH0 + (size_t)buf * 2 * NC * kTcK;
@@ -193,7 +199,8 @@ struct TcShare {
     }
 };
 template <int NC>
-__device__ __forceinline__ bool tc_readback(const TcTile& t, cx<float>* A, int ld, uint32_t tbase, uint64_t* done) {
+__device__ __forceinline__ bool tc_readback(const TcTile& t, cx<float>* A, int ld, uint32_t tbase, uint64_t* done,
+                                            volatile int* fail) {
     const TcShare  sh;
     const int      r   = t.rb + 32 * sh.qd + (threadIdx.x & 31);
     const bool     rok = r >= t.rlo && r < t.rhi;
@@ -209,7 +216,7 @@ __device__ __forceinline__ bool tc_readback(const TcTile& t, cx<float>* A, int l
                                                                                : cx<float>{0.f, 0.f};
         }
     }
-    bool ok = tc_wait(done + buf, (t.seq >> 1) & 1u);
+    bool ok = tc_wait(done + buf, (t.seq >> 1) & 1u, fail);
     ok      = __all_sync(0xffffffffu, ok);
     tc::fence_after_sync();
     if (ok) {
@@ -242,7 +249,8 @@ __device__ __forceinline__ bool tc_readback(const TcTile& t, cx<float>* A, int l
 // false if a wait gave up (the update is then incomplete).
 template <int NC>
 __device__ bool tc_trailing_update(cx<float>* A, int n, int ld, int q0, const cx<float>* Vp, const cx<float>* Wp,
-                                   float* stage, uint32_t tbase, uint64_t* staged, uint64_t* done, uint32_t& seq) {
+                                   float* stage, uint32_t tbase, uint64_t* staged, uint64_t* done, uint32_t& seq,
+                                   volatile int* fail) {
     float*         aH = stage;
     float*         aL = aH + (size_t)kTcM * kTcK;
     float*         bH0 = aL + (size_t)kTcM * kTcK;  // buffer b: hi at bH0 + b * 2 NC K, lo NC K after it
@@ -260,7 +268,7 @@ __device__ bool tc_trailing_update(cx<float>* A, int n, int ld, int q0, const cx
                 if (worker) {
                     if (first) {
                         if (pending) {  // the row operand is about to change: drain the tile in flight
-                            ok      = tc_readback<NC>(prev, A, ld, tbase, done) && ok;
+                            ok      = tc_readback<NC>(prev, A, ld, tbase, done, fail) && ok;
                             pending = false;
                         }
                         tc_stage<kTcM>(Vp, Wp, n, rb, aH, aL);
@@ -270,11 +278,11 @@ __device__ bool tc_trailing_update(cx<float>* A, int n, int ld, int q0, const cx
                     tc::fence_async_smem();
                     tc::fence_before_sync();
                     tc::mbar_arrive(staged + (t.seq & 1u));
-                    if (pending) ok = tc_readback<NC>(prev, A, ld, tbase, done) && ok;
+                    if (pending) ok = tc_readback<NC>(prev, A, ld, tbase, done, fail) && ok;
                     prev    = t;
                     pending = true;
                 } else if (issuer) {
-                    ok = tc_issue<NC>(t, aH, aL, bH0, tbase, staged, done) && ok;
+                    ok = tc_issue<NC>(t, aH, aL, bH0, tbase, staged, done, fail) && ok;
                 }
                 first = false;
             }
@@ -284,7 +292,7 @@ __device__ bool tc_trailing_update(cx<float>* A, int n, int ld, int q0, const cx
         rhi = rlo;
         rbe = rb;
     }
-    if (worker && pending) ok = tc_readback<NC>(prev, A, ld, tbase, done) && ok;
+    if (worker && pending) ok = tc_readback<NC>(prev, A, ld, tbase, done, fail) && ok;
     return __syncthreads_and(ok) != 0;
 }
 
@@ -305,6 +313,7 @@ __global__ void __launch_bounds__(kBlkNT, 1)
     __shared__ uint64_t s_staged[2];  // tensor-core update: tile staged (worker warps -> issuer), per buffer
     __shared__ uint64_t s_done[2];    // its MMAs complete (tcgen05.commit -> worker warps), per buffer
     __shared__ uint32_t s_tmem;       // TMEM base address
+    __shared__ int      s_tcfail;     // a tensor-core wait gave up
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     // With an even order every column starts at an even element, so row pairs from an even row are
     // 16-byte (8-byte for real) aligned: the product's tiles then start at o rounded down to even.
@@ -317,6 +326,7 @@ __global__ void __launch_bounds__(kBlkNT, 1)
     if constexpr (TC) {
         if (tc_on) {
             if (tid == 0) {
+                s_tcfail = 0;
                 tc::mbar_init(&s_staged[0], kBlkNT - 32);
                 tc::mbar_init(&s_staged[1], kBlkNT - 32);
                 tc::mbar_init(&s_done[0], 1);
@@ -581,9 +591,9 @@ __global__ void __launch_bounds__(kBlkNT, 1)
                     simt = false;
                     float* stage = reinterpret_cast<float*>(yp);
                     const bool ok =
-                        use_tc == 64   ? tc_trailing_update<64>(A, n, ld, q0, Vp, Wp, stage, tbase, s_staged, s_done, tc_seq)
-                        : use_tc == 48 ? tc_trailing_update<48>(A, n, ld, q0, Vp, Wp, stage, tbase, s_staged, s_done, tc_seq)
-                                       : tc_trailing_update<32>(A, n, ld, q0, Vp, Wp, stage, tbase, s_staged, s_done, tc_seq);
+                        use_tc == 64   ? tc_trailing_update<64>(A, n, ld, q0, Vp, Wp, stage, tbase, s_staged, s_done, tc_seq, &s_tcfail)
+                        : use_tc == 48 ? tc_trailing_update<48>(A, n, ld, q0, Vp, Wp, stage, tbase, s_staged, s_done, tc_seq, &s_tcfail)
+                                       : tc_trailing_update<32>(A, n, ld, q0, Vp, Wp, stage, tbase, s_staged, s_done, tc_seq, &s_tcfail);
                     if (!ok) {
                         // a wait gave up: this matrix is incomplete, and the CTA keeps to the SIMT update
                         if (tid == 0 && status) atomicOr(status + b, 1);  // UEPM_K_NOCONVERGE
