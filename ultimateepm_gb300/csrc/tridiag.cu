@@ -790,7 +790,8 @@ void launch_tridiag(S* H, int n, int ld, size_t mstride, typename ST<S>::R* d, t
         // on the tensor cores, whole solves against the deferred kernel: Si SOC n = 274 33.4 against
         // 45.5 ms, InAs n = 229 27.2 against 27.7); below, the deferred kernel stays ahead (GaAs SOC
         // n = 178 16.5 against 19.3 ms per solve). Real matrices, whose updates stay on the FP32 pipe,
-        // keep the order-300 switch it was measured at.
+        // keep the order-300 switch (real Sn and Ge n = 229: deferred 16.3 and 17.4 ms per solve,
+        // blocked 19.4 and 20.6).
         if ((variant == 6 || (variant == 0 && n >= (ST<S>::cplx ? 200 : 300))) &&
             launch_tridiag_blocked<S>(H, n, ld, mstride, d, e, tq, status, batch, s, tensor_cores))
             return;
