@@ -42,10 +42,10 @@ void launch_assemble(const DevParams& P, const cx<double>* Vloc, const double2* 
 // thread-block cluster per matrix (tridiag_cluster.cu), 4 one CTA per matrix in global memory with
 // each step's update fused into the next step's product (FP32, n <= 512), 5 the same with every
 // other update deferred to the next pass, 6 blocked (panels of 16 columns, lower triangle only, one
-// matrix per SM, tridiag_blocked.cu; FP32, n <= 512). Automatic: 1 where it applies, 6 for FP32 orders
-// 300..512, 5 for the other FP32 matrices, else 2. ctas_per_sm (0: automatic) caps the
-// persistent grid of the global-memory kernels; cluster (0: automatic) is the cluster size of
-// variant 3.
+// matrix per SM, tridiag_blocked.cu; FP32, n <= 512). Automatic: 1 where it applies, 6 for FP32
+// complex orders 200..512 and real orders 300..512, 5 for the other FP32 matrices, else 2.
+// ctas_per_sm (0: automatic) caps the persistent grid of the global-memory kernels; cluster (0:
+// automatic) is the cluster size of variant 3.
 template <typename S>
 void launch_tridiag(S* H, int n, int ld, size_t mstride, typename ST<S>::R* d, typename ST<S>::R* e, S* tq, int* status,
                     int batch, cudaStream_t s, int variant = 0, int ctas_per_sm = 0, int cluster = 0,
