@@ -136,18 +136,36 @@ __global__ void __launch_bounds__(kYtNT, 1)
     tc::fence_after_sync();
     const uint32_t tbase = s_tmem;
     {
-        const int rl = tid & (kYtM - 1), part = tid >> 7, r = r0 + rl;  // 4 threads per row
-        float     mx = 0.f;
-        if (r < n)
-            for (int c = part; c < n; c += kYtNT / kYtM) {
-                const ds4 v = A[(size_t)c * ld + r];
-                mx          = fmaxf(mx, fmaxf(fabsf(v.rhi), fabsf(v.ihi)));
+        // rows: 4 threads per row, each with kYtPass loads in flight (the pass is bound by load latency)
+        constexpr int kStep = kYtNT / kYtM, kYtPass = 8;
+        const int     rl = tid & (kYtM - 1), part = tid >> 7, r = r0 + rl;
+        const float4* Af = reinterpret_cast<const float4*>(A);  // (rhi, rlo, ihi, ilo)
+        float         mx = 0.f;
+        if (r < n) {
+            int c = part;
+            for (; c + (kYtPass - 1) * kStep < n; c += kYtPass * kStep) {
+                float4 v[kYtPass];
+#pragma unroll
+                for (int u = 0; u < kYtPass; ++u) v[u] = __ldg(Af + (size_t)(c + u * kStep) * ld + r);
+#pragma unroll
+                for (int u = 0; u < kYtPass; ++u) mx = fmaxf(mx, fmaxf(fabsf(v[u].x), fabsf(v[u].z)));
             }
+            for (; c < n; c += kStep) {
+                const float4 v = __ldg(Af + (size_t)c * ld + r);
+                mx             = fmaxf(mx, fmaxf(fabsf(v.x), fabsf(v.z)));
+            }
+        }
         atomicMax(reinterpret_cast<int*>(&s_rmax[rl]), __float_as_int(mx));  // non-negative: int order
-        for (int idx = tid; idx < m * n; idx += kYtNT) {
-            const int       j = idx / n;
-            const cx<float> x = Xg[idx];
-            atomicMax(reinterpret_cast<int*>(&s_cmax[j]), __float_as_int(fmaxf(fabsf(x.x), fabsf(x.y))));
+        // vectors: one warp per vector, reduced by shuffles (one store per vector)
+        for (int j = warp; j < m; j += kYtNT / 32) {
+            float xm = 0.f;
+            for (int c = lane; c < n; c += 32) {
+                const cx<float> x = Xg[(size_t)j * n + c];
+                xm                = fmaxf(xm, fmaxf(fabsf(x.x), fabsf(x.y)));
+            }
+#pragma unroll
+            for (int o = 16; o; o >>= 1) xm = fmaxf(xm, __shfl_xor_sync(0xffffffffu, xm, o));
+            if (lane == 0) s_cmax[j] = xm;
         }
     }
     __syncthreads();
