@@ -282,6 +282,9 @@ def run_ours(args):
     pipe_of = {"tridiag_fp32": "fp32", "backtransform": "fp32"}
     # DRAM bytes per launch of the reduction on this 2000-matrix workload: dram__bytes_read.sum +
     # dram__bytes_write.sum from one ncu capture of the same kernels (ncu cannot run inside a bench).
+    # The mixed solve runs its 2000 k-points as two concurrent halves (two streams); the profile
+    # counts the pair as one launch, timed from the first start to the last end, and its traffic is
+    # the sum of the halves'.
     # Each figure belongs to the kernel named beside it and holds until that kernel changes: the
     # mixed path's k_tridiag_reg_local (profiles/k_tridiag_si137_2000k.md) and the FP64 path's
     # k_tridiag<double> (profiles/launches_si137_2000k.md); re-capture them whenever either is edited.

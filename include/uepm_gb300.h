@@ -128,7 +128,10 @@ int uepm_ctx_force_complex(uepm_ctx* ctx, int on);
  *   status nk int32 per-k status                         (may be NULL)
  * nb must be in [1, n]. uepm_solve takes HOST buffers and copies in and out; uepm_solve_device
  * takes DEVICE buffers and enqueues on `stream` (a cudaStream_t, NULL = legacy default stream)
- * without synchronising.
+ * without synchronising. Mixed-precision solves of 1024 or more k-points with real local-potential
+ * matrices of order <= 176 split the batch between `stream` and a second stream of the context,
+ * forked from and joined back to `stream` (work enqueued on `stream` afterwards waits for both; the
+ * results are the same). With profiling on, the two halves of a kernel count as one launch.
  */
 int uepm_solve(uepm_ctx* ctx, const double* k, size_t nk, int nb, uint32_t want, double* E, double* X, double* grad,
                int32_t* status);

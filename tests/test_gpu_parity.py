@@ -319,6 +319,30 @@ def test_chunked_solve_is_identical(gpu, oracle, mats):
     np.testing.assert_array_equal(g1, g2)
 
 
+def test_two_lane_solve_is_identical(gpu, oracle, mats):
+    """A mixed solve of 1024 or more real local-potential k-points splits the batch between the
+    caller's stream and the context's second stream: the same bits as one-lane solves of its halves
+    (values, vectors, gradients). With profiling on, each kernel counts one launch for the pass."""
+    G = oracle.generate_basis(10)
+    ks = _kset(oracle, 31, 1400)
+    ctx = _ctx(mats["Si-CB"], G, False, False, N.UEPM_PREC_MIXED)
+    N.check(gpu.uepm_ctx_set_profiling(ctx.h, 1))
+    E2, X2, g2, st = ctx.solve(ks, 8, vectors=True, gradient=True)
+    ms = (C.c_double * N.KERNEL_KINDS)()
+    cnt = (C.c_uint64 * N.KERNEL_KINDS)()
+    N.check(gpu.uepm_ctx_read_profile(ctx.h, ms, cnt, N.KERNEL_KINDS))
+    prof = {gpu.uepm_kernel_name(q).decode(): (ms[q], int(cnt[q])) for q in range(N.KERNEL_KINDS) if cnt[q]}
+    N.check(gpu.uepm_ctx_set_profiling(ctx.h, 0))
+    assert not st.any()
+    for kind in ("tridiag_fp32", "bisect", "invit", "backtransform", "refine_project", "small_eigh"):
+        assert prof[kind][1] == 1 and prof[kind][0] > 0, (kind, prof[kind])
+    h = len(ks) // 2
+    parts = [ctx.solve(ks[:h], 8, vectors=True, gradient=True), ctx.solve(ks[h:], 8, vectors=True, gradient=True)]
+    np.testing.assert_array_equal(E2, np.concatenate([p[0] for p in parts]))
+    np.testing.assert_array_equal(X2, np.concatenate([p[1] for p in parts]))
+    np.testing.assert_array_equal(g2, np.concatenate([p[2] for p in parts]))
+
+
 def test_device_entry_point_matches_host_entry_point(gpu, oracle, mats):
     import torch
 

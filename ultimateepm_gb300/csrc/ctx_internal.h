@@ -45,6 +45,10 @@ struct uepm_ctx {
     float*        d_V32     = nullptr;  // [N][N] Re V rounded to FP32 (the diagonal is formed per k)
     void*         d_ws      = nullptr;
     size_t        ws_bytes  = 0;
+    // second lane of a two-lane solve (created on first use) and its fork / join events
+    cudaStream_t  lane_stream = nullptr;
+    cudaEvent_t   lane_fork   = nullptr;
+    cudaEvent_t   lane_join   = nullptr;
     // buffers of the host-pointer entry point
     cudaStream_t  stream    = nullptr;
     void*         d_io      = nullptr;
@@ -53,9 +57,11 @@ struct uepm_ctx {
     // per-kernel timing (uepm_ctx_set_profiling)
     struct Rec {
         int         kind;
+        unsigned    group;  // the pass (both lanes of a two-lane pass share it)
         cudaEvent_t a, b;
     };
     int                      profiling = 0;
+    unsigned                 prof_group = 0;
     std::vector<Rec>         pending;
     std::vector<cudaEvent_t> pool;
     double                   prof_ms[UEPM_KERNEL_KINDS] = {0};
@@ -67,12 +73,17 @@ namespace uepm {
 void set_error(const std::string& msg);
 
 // Workspace plan of one pipeline pass: chunk (k-points per pass) and the bytes it needs.
+// lanes = 2: consecutive chunks alternate between the caller's stream and the context's second
+// stream, each lane with its own workspace half (ws_bytes covers both).
 struct SolvePlan {
     size_t chunk = 0, ws_bytes = 0;
     int    m     = 0;
+    int    lanes = 1;
 };
 // Validates nb / want against the context and plans the passes of an nk-point solve (no allocation).
-int plan_solve(uepm_ctx* ctx, size_t nk, int nb, uint32_t want, SolvePlan* out);
+// two_lanes lets the plan take two lanes where they pay (the register-resident reduction of real
+// local-potential matrices, 1024 k-points or more).
+int plan_solve(uepm_ctx* ctx, size_t nk, int nb, uint32_t want, SolvePlan* out, bool two_lanes = false);
 // Grows the context's device workspace to at least `bytes` (allocates: not while capturing).
 int ensure_workspace(uepm_ctx* ctx, size_t bytes);
 // Enqueues the solve on s; the workspace (the context's own, or ws / ws_bytes when given, so that
