@@ -353,6 +353,8 @@ def run_ours(args):
                 "d2h_bytes_per_step": int(hE.numel() * 8 + hs.numel() * 4), "entry_point": "uepm_solve"},
         "roofline": roof_mixed,
         "kernels_ms": {q: v[0] / max(v[1], 1) for q, v in prof_mixed.items()},
+        "kernels_ms_note": "per solve; the mixed solve runs its 2000 k-points as two halves on two streams, "
+                           "and each kernel's time spans the first half's start to the second half's end",
         "gpu_launches": launches_mixed,
         "cpu_baseline": {"value": cpu_v, "unit": "k-points/s", "cores": cores, "kind": "port", "flags": CPU_FLAGS,
                          "sample": f"{cpu_done} k-points ({cpu_done // nk} passes over the 2000-point path), "
@@ -637,6 +639,9 @@ def run_configs(seed: int = 20261203):
             # work: the reduction's panel updates (tcgen05 kind::tf32) and Y = H X (kind::f16 on BF16
             # slices: 36 slice pairs x 2 x 128 x N x K per 128-row tile)
             ctx = api._Context(m, G, nl, soc, N.UEPM_PREC_MIXED)
+            # one stream, so that each kernel's events time that kernel alone (the timed solve above
+            # runs its chunks on two streams)
+            N.check(L.uepm_ctx_set_tuning(ctx.h, C.byref(N.UepmTuning(streams=1))))
             n, mm = ctx.n, nbt + 4
             kk = dk[:2000].contiguous()
             solve_timed(ctx, kk, nbt)  # warm

@@ -128,10 +128,11 @@ int uepm_ctx_force_complex(uepm_ctx* ctx, int on);
  *   status nk int32 per-k status                         (may be NULL)
  * nb must be in [1, n]. uepm_solve takes HOST buffers and copies in and out; uepm_solve_device
  * takes DEVICE buffers and enqueues on `stream` (a cudaStream_t, NULL = legacy default stream)
- * without synchronising. Mixed-precision solves of 1024 or more k-points with real local-potential
- * matrices of order <= 176 split the batch between `stream` and a second stream of the context,
- * forked from and joined back to `stream` (work enqueued on `stream` afterwards waits for both; the
- * results are the same). With profiling on, the two halves of a kernel count as one launch.
+ * without synchronising. A mixed-precision solve of 1024 or more k-points that fits one pipeline
+ * pass splits the batch between `stream` and a second stream of the context, forked from and joined
+ * back to `stream` (work enqueued on `stream` afterwards waits for both; the results are the same;
+ * uepm_tuning.streams). With profiling on, the two halves of a kernel count as one launch, timed
+ * from the first start to the last end.
  */
 int uepm_solve(uepm_ctx* ctx, const double* k, size_t nk, int nb, uint32_t want, double* E, double* X, double* grad,
                int32_t* status);
@@ -222,6 +223,12 @@ int uepm_measure_peak(int precision, double* tflops);
  *                 hi/lo operand splits, FP32-level products) and, from order 150, the Rayleigh-Ritz
  *                 product H X (BF16 integer slices of H and X, exact to double-single level);
  *                 1: every product on the FP32 pipe (SIMT). Kept by the autotuner.
+ *   streams       0 (automatic): a mixed-precision uepm_solve_device / uepm_solve of 1024 or more
+ *                 k-points that fits one pipeline pass runs as two halves on two streams (the
+ *                 caller's and one of the context, forked and joined on the caller's stream), so
+ *                 that one half's later kernels run beside the other half's reduction; 1: one
+ *                 stream; 2: two streams for any solve of two or more k-points, consecutive passes
+ *                 alternating. The results are the same bits. Kept by the autotuner.
  * Every choice gives results within the parity tolerances; a given choice is deterministic.
  * uepm_ctx_autotune times candidate shapes on sample_k seeded random first-zone k-points (coordinate
  * descent over the fields, CUDA events on `stream`) and keeps the fastest; results are cached
@@ -235,6 +242,7 @@ typedef struct uepm_tuning {
     int32_t cluster;
     int32_t max_iter;
     int32_t tensor_cores;
+    int32_t streams;
 } uepm_tuning;
 int uepm_ctx_get_tuning(const uepm_ctx* ctx, uepm_tuning* out);
 int uepm_ctx_set_tuning(uepm_ctx* ctx, const uepm_tuning* t);

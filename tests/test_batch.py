@@ -158,6 +158,9 @@ def test_batch_replay_reads_the_registered_buffers(gpu, oracle, mats):
     (N.UEPM_PREC_FP64, dict(ctas_per_sm=1, chunk=512)),
     (N.UEPM_PREC_FP64, dict(ctas_per_sm=8, vector_lanes=16)),
     (N.UEPM_PREC_FP64, dict(reduction=3, cluster=4)),
+    (N.UEPM_PREC_MIXED, dict(streams=2, chunk=64)),
+    (N.UEPM_PREC_MIXED, dict(streams=1)),
+    (N.UEPM_PREC_FP64, dict(streams=2)),
 ])
 def test_every_tuning_choice_keeps_parity(gpu, oracle, mats, prec, tuning):
     G = oracle.generate_basis(10)
@@ -177,7 +180,7 @@ def test_every_tuning_choice_keeps_parity(gpu, oracle, mats, prec, tuning):
 
 def test_set_tuning_rejects_out_of_range_fields(gpu, oracle, mats):
     ctx = api._Context(_mat(mats["Si-CB"]), oracle.generate_basis(8), False, False)
-    for bad in (dict(reduction=7), dict(tensor_cores=2), dict(ctas_per_sm=9), dict(vector_lanes=12), dict(chunk=10), dict(cluster=3)):
+    for bad in (dict(reduction=7), dict(tensor_cores=2), dict(streams=3), dict(ctas_per_sm=9), dict(vector_lanes=12), dict(chunk=10), dict(cluster=3)):
         assert gpu.uepm_ctx_set_tuning(ctx.h, C.byref(N.UepmTuning(**bad))) == N.UEPM_ERR_OUT_OF_RANGE
     ctx.close()
 

@@ -39,8 +39,8 @@ def _solve_raw(ctx, k, nb, want=0):
 
 
 def test_tuning_struct_has_the_iteration_cap():
-    assert [f for f, _ in N.UepmTuning._fields_][-2:] == ["max_iter", "tensor_cores"]
-    assert C.sizeof(N.UepmTuning) == 7 * 4
+    assert [f for f, _ in N.UepmTuning._fields_][-3:] == ["max_iter", "tensor_cores", "streams"]
+    assert C.sizeof(N.UepmTuning) == 8 * 4
 
 
 CASES = [("Si-CB", 8, False, False), ("Ge", 8, True, True), ("InP", 8, True, False)]

@@ -71,7 +71,8 @@ class UepmTuning(C.Structure):
     """struct uepm_tuning (include/uepm_gb300.h); 0 in a field means automatic."""
 
     _fields_ = [("reduction", C.c_int32), ("ctas_per_sm", C.c_int32), ("vector_lanes", C.c_int32),
-                ("chunk", C.c_int32), ("cluster", C.c_int32), ("max_iter", C.c_int32), ("tensor_cores", C.c_int32)]
+                ("chunk", C.c_int32), ("cluster", C.c_int32), ("max_iter", C.c_int32), ("tensor_cores", C.c_int32),
+                ("streams", C.c_int32)]
 
     def as_dict(self) -> dict:
         return {f: getattr(self, f) for f, _ in self._fields_}

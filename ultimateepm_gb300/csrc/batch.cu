@@ -58,6 +58,7 @@ bool valid_tuning(const uepm_ctx* ctx, const uepm_tuning& t) {
     if (t.chunk != 0 && (t.chunk < 64 || t.chunk > 32768)) return false;
     if (t.max_iter < 0 || t.max_iter > 1000) return false;
     if (t.tensor_cores < 0 || t.tensor_cores > 1) return false;
+    if (t.streams < 0 || t.streams > 2) return false;
     (void)ctx;
     return true;
 }
@@ -179,6 +180,7 @@ int uepm_ctx_autotune(uepm_ctx* ctx, int nb, uint32_t want, size_t sample_k, voi
     uepm_tuning best = uepm_tuning{};
     best.max_iter    = saved.max_iter;  // not a shape: kept as the caller set it
     best.tensor_cores = saved.tensor_cores;
+    best.streams      = saved.streams;
     ctx->tune        = best;
     double best_ms   = 0;
     rc               = timed(&best_ms);

@@ -343,17 +343,16 @@ namespace uepm {
 
 int ensure_workspace(uepm_ctx* ctx, size_t bytes) { return ensure_ws(ctx, bytes); }
 
-// Two lanes: the register-resident reduction of real local-potential matrices holds the whole
-// register file at two matrices per SM, and the kernels after it (bisection, inverse iteration, the
-// Rayleigh-Ritz products and the small solves) are bound by the latency of short per-matrix chains.
-// Splitting the batch over two streams lets one half's later kernels run beside the other half's
-// reduction: Si local n = 137, 2000 k, 16 bands: 2.00 -> 1.89 ms per solve (three and four lanes
-// measured no faster). Results are the same bits (every k-point is solved on its own).
+// Two lanes: a mixed solve's reduction holds the SMs' registers or shared memory, and the kernels
+// after it (bisection, inverse iteration, the Rayleigh-Ritz products and the small solves) are bound
+// by the latency of short per-matrix chains. Splitting the batch over two streams lets one half's
+// later kernels run beside the other half's reduction. Per solve, one lane against two: Si local
+// n = 137 (register-resident reduction), 2000 k, 16 bands: 2.00 -> 1.89 ms (three and four lanes no
+// faster); 12 bands, Si nonlocal n = 137, 65536 k: 100.8 -> 100.0 ms; InP n = 113 complex: 158.5 ->
+// 155.9; Ge n = 181 real, 32768 k: 151.2 -> 149.2; Ge SOC n = 362, 16 bands, 4000 k: 113.7 -> 111.0
+// (each half in one pass of its own). Results are the same bits (every k-point is solved on its own).
 constexpr size_t kLaneMinK = 1024;
-static bool lanes_pay(const uepm_ctx* ctx, size_t nk) {
-    return ctx->precision == UEPM_PREC_MIXED && ctx->real && ctx->sparse_local &&
-           (ctx->tune.reduction == 0 || ctx->tune.reduction == 1) && ctx->n <= tridiag_reg_max_n() && nk >= kLaneMinK;
-}
+static bool lanes_pay(const uepm_ctx* ctx, size_t nk) { return ctx->precision == UEPM_PREC_MIXED && nk >= kLaneMinK; }
 
 int plan_solve(uepm_ctx* ctx, size_t nk, int nb, uint32_t want, SolvePlan* out, bool two_lanes) {
     if (nb < 1 || nb > ctx->n) {
@@ -368,12 +367,18 @@ int plan_solve(uepm_ctx* ctx, size_t nk, int nb, uint32_t want, SolvePlan* out, 
         return UEPM_ERR_INVALID;
     }
     // chunk size from the workspace budget and the tuning
-    const size_t per   = plan(ctx, nb, want, 1).total;
-    size_t       chunk = std::max<size_t>(1, ctx->ws_limit / std::max<size_t>(per, 1));
-    const size_t cap   = ctx->tune.chunk > 0 ? std::min<size_t>((size_t)ctx->tune.chunk, kMaxChunk) : kMaxChunk;
-    chunk              = std::max<size_t>(1, std::min(std::min(chunk, nk), cap));
-    out->lanes         = two_lanes && lanes_pay(ctx, nk) ? 2 : 1;
-    if (out->lanes == 2) chunk = (chunk + 1) / 2;  // the same workspace, split between the lanes
+    const size_t per    = plan(ctx, nb, want, 1).total;
+    const size_t budget = std::max<size_t>(1, ctx->ws_limit / std::max<size_t>(per, 1));
+    const size_t cap    = ctx->tune.chunk > 0 ? std::min<size_t>((size_t)ctx->tune.chunk, kMaxChunk) : kMaxChunk;
+    size_t       chunk  = std::max<size_t>(1, std::min(std::min(budget, nk), cap));
+    // automatic: two lanes where the batch fits one pass, whose halves then run side by side (a
+    // batch of several passes keeps whole passes: halving them measured 1 % slower on 500 000 and
+    // 1 000 000 k, Si nonlocal n = 137 and Ge SOC n = 362)
+    const int want_l = ctx->tune.streams;  // 0 automatic, 1 or 2
+    out->lanes = two_lanes && (want_l == 2 ? nk >= 2 : want_l == 0 && lanes_pay(ctx, nk) && nk <= chunk) ? 2 : 1;
+    // two lanes: each lane's chunk within half the workspace budget, the tuned chunk, and half the
+    // batch (so that both lanes have work)
+    if (out->lanes == 2) chunk = std::max<size_t>(1, std::min(std::min(budget / 2, cap), (nk + 1) / 2));
     out->chunk    = chunk;
     out->m        = m;
     out->ws_bytes = out->lanes * plan(ctx, nb, want, chunk).total;
