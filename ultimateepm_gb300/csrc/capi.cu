@@ -351,6 +351,8 @@ int ensure_workspace(uepm_ctx* ctx, size_t bytes) { return ensure_ws(ctx, bytes)
 // faster); 12 bands, Si nonlocal n = 137, 65536 k: 100.8 -> 100.0 ms; InP n = 113 complex: 158.5 ->
 // 155.9; Ge n = 181 real, 32768 k: 151.2 -> 149.2; Ge SOC n = 362, 16 bands, 4000 k: 113.7 -> 111.0
 // (each half in one pass of its own). Results are the same bits (every k-point is solved on its own).
+// FP64 solves keep one stream: two measured 12.5 -> 12.9 ms (Si local, 2000 k), 601.7 -> 604.4 (Ge
+// SOC, 2000 k) and 138.5 -> 131.4 (Ge n = 181 real, 8000 k), no gain overall.
 constexpr size_t kLaneMinK = 1024;
 static bool lanes_pay(const uepm_ctx* ctx, size_t nk) { return ctx->precision == UEPM_PREC_MIXED && nk >= kLaneMinK; }
 
