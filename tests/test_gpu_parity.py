@@ -343,6 +343,37 @@ def test_two_lane_solve_is_identical(gpu, oracle, mats):
     np.testing.assert_array_equal(g2, np.concatenate([p[2] for p in parts]))
 
 
+def test_two_lane_solve_captures_into_a_graph(gpu, oracle, mats):
+    """The two-lane fork and join are stream-ordered, so a capture of the solve on one stream takes
+    in the second lane too; the replayed graph gives the same bits as the eager solve."""
+    import torch
+
+    G = oracle.generate_basis(10)
+    ks, _ = oracle.generate_path("LGXWKULWXKG", 2000)
+    ctx = _ctx(mats["Si-CB"], G, False, False, N.UEPM_PREC_MIXED)
+    dk = torch.from_numpy(np.ascontiguousarray(ks)).cuda()
+    dE = torch.zeros((len(ks), 16), dtype=torch.float64, device="cuda")
+    ds = torch.zeros(len(ks), dtype=torch.int32, device="cuda")
+
+    def call():
+        s = torch.cuda.current_stream().cuda_stream
+        N.check(gpu.uepm_solve_device(ctx.h, C.c_void_p(dk.data_ptr()), len(ks), 16, N.UEPM_WANT_VALUES,
+                                      C.c_void_p(dE.data_ptr()), None, None, C.c_void_p(ds.data_ptr()),
+                                      C.c_void_p(s)))
+
+    call()  # eager: sizes the workspace and makes the second lane
+    torch.cuda.synchronize()
+    E1 = dE.cpu().numpy().copy()
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g):
+        call()
+    dE.zero_()
+    g.replay()
+    torch.cuda.synchronize()
+    np.testing.assert_array_equal(dE.cpu().numpy(), E1)
+    assert not ds.cpu().numpy().any()
+
+
 def test_device_entry_point_matches_host_entry_point(gpu, oracle, mats):
     import torch
 

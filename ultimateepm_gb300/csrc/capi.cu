@@ -403,17 +403,30 @@ int enqueue_solve(uepm_ctx* ctx, const SolvePlan& sp, const double* d_k, size_t 
     const bool   want_grad = (want & UEPM_WANT_GRADIENT) != 0;
     const int    lanes     = sp.lanes == 2 ? 2 : 1;
     cudaStream_t ls[2]     = {s, s};
+    bool         forked    = false;
     if (lanes == 2) {  // fork: the second lane starts after everything enqueued on s so far
         if (!ctx->lane_stream) {
-            UEPM_CUDA(cudaStreamCreateWithFlags(&ctx->lane_stream, cudaStreamNonBlocking));
-            UEPM_CUDA(cudaEventCreateWithFlags(&ctx->lane_fork, cudaEventDisableTiming));
-            UEPM_CUDA(cudaEventCreateWithFlags(&ctx->lane_join, cudaEventDisableTiming));
+            // the stream and events are made outside stream capture only; a capture that meets
+            // none runs both lanes' chunks in order on s (same workspace halves, same results)
+            cudaStreamCaptureStatus cs = cudaStreamCaptureStatusActive;
+            if (cudaStreamIsCapturing(s, &cs) != cudaSuccess) {
+                cudaGetLastError();
+                cs = cudaStreamCaptureStatusActive;
+            }
+            if (cs == cudaStreamCaptureStatusNone) {
+                UEPM_CUDA(cudaStreamCreateWithFlags(&ctx->lane_stream, cudaStreamNonBlocking));
+                UEPM_CUDA(cudaEventCreateWithFlags(&ctx->lane_fork, cudaEventDisableTiming));
+                UEPM_CUDA(cudaEventCreateWithFlags(&ctx->lane_join, cudaEventDisableTiming));
+            }
         }
-        UEPM_CUDA(cudaEventRecord(ctx->lane_fork, s));
-        UEPM_CUDA(cudaStreamWaitEvent(ctx->lane_stream, ctx->lane_fork, 0));
-        ls[1] = ctx->lane_stream;
+        if (ctx->lane_stream) {
+            UEPM_CUDA(cudaEventRecord(ctx->lane_fork, s));
+            UEPM_CUDA(cudaStreamWaitEvent(ctx->lane_stream, ctx->lane_fork, 0));
+            ls[1] = ctx->lane_stream;
+            forked = true;
+        }
     }
-    int rc;
+    int rc = UEPM_OK;
     for (size_t off = 0, q = 0; off < nk; off += chunk, ++q) {
         const int          lane = (int)(q % lanes);
         const cudaStream_t sq   = ls[lane];
@@ -427,13 +440,13 @@ int enqueue_solve(uepm_ctx* ctx, const SolvePlan& sp, const double* d_k, size_t 
         double*       gr = want_grad ? d_grad + off * nb * 3 : nullptr;
         if (ctx->real) run_chunk<double>(ctx, L, wsq, kk, c, nb, sp.m, want_vec || want_grad, E, Xo, gr, st, sq);
         else run_chunk<cx<double>>(ctx, L, wsq, kk, c, nb, sp.m, want_vec || want_grad, E, Xo, gr, st, sq);
-        if ((rc = check_launch())) return rc;
+        if ((rc = check_launch())) break;
     }
-    if (lanes == 2) {  // join: work enqueued on s later waits for the second lane
+    if (forked) {  // join (also after a failed launch): work enqueued on s later waits for the second lane
         UEPM_CUDA(cudaEventRecord(ctx->lane_join, ctx->lane_stream));
         UEPM_CUDA(cudaStreamWaitEvent(s, ctx->lane_join, 0));
     }
-    return UEPM_OK;
+    return rc;
 }
 
 }  // namespace uepm
