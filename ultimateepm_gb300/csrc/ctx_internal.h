@@ -81,8 +81,8 @@ struct SolvePlan {
     int    lanes = 1;
 };
 // Validates nb / want against the context and plans the passes of an nk-point solve (no allocation).
-// two_lanes lets the plan take two lanes where they pay (the register-resident reduction of real
-// local-potential matrices, 1024 k-points or more).
+// two_lanes lets the plan take two lanes where they pay (mixed-precision solves of 1024 k-points or
+// more that fit one pass) or where uepm_tuning.streams = 2 asks for them.
 int plan_solve(uepm_ctx* ctx, size_t nk, int nb, uint32_t want, SolvePlan* out, bool two_lanes = false);
 // Grows the context's device workspace to at least `bytes` (allocates: not while capturing).
 int ensure_workspace(uepm_ctx* ctx, size_t bytes);
